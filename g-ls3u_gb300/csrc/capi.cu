@@ -1,0 +1,627 @@
+// capi.cu -- the C ABI (include/glsu.h): handles, buffers, streams, timing.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "glsu_internal.cuh"
+
+namespace glsu {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string &msg) { g_err = msg; }
+
+int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return GLSU_ERR_ALLOC;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return GLSU_ERR_NO_DEVICE;
+    return GLSU_ERR_CUDA;
+}
+
+int wff_count_public(double lo, double hi, double step, int prec);
+
+// Is p a page-locked (pinned or registered) host pointer?
+static bool is_pinned(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+static size_t elem_size(int t)
+{
+    return t == GLSU_U8 ? 1 : (t == GLSU_F32 ? 4 : (t == GLSU_F64 ? 8 : 0));
+}
+
+}  // namespace glsu
+
+using namespace glsu;
+
+// ===========================================================================
+// handles
+// ===========================================================================
+struct glsu_wff {
+    WffPlan plan;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+struct glsu_dpra {
+    int prec = GLSU_F32;
+    int W = 0, H = 0, rr = 1, r = 1;
+    WffPlan wff;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    void *d_img = nullptr;  // one frame, 8 bytes per pixel
+    void *d_z = nullptr;    // exp(j dphi), complex
+    void *d_phi[4] = {nullptr, nullptr, nullptr, nullptr};  // ref, curr, dphi_ref, dphi
+    void *h_in = nullptr, *h_out = nullptr;                 // pinned staging
+    bool synced = true;  // phi_curr/dphi equal phi_ref/dphi_ref (after an update)
+    bool timing = false;
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    int frames_done = 0;
+};
+
+struct glsu_aia {
+    int M = 0, cols = 0, rows = 0, N = 0;
+    AiaDev dev;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    void *d_frames = nullptr;  // M*N*4 bytes
+    float *d_phi = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+};
+
+// ===========================================================================
+// utilities
+// ===========================================================================
+extern "C" const char *glsu_last_error(void) { return g_err.c_str(); }
+
+extern "C" int glsu_version(void) { return 100; }
+
+extern "C" int glsu_opt_fft_size(int x)
+{
+    // even sizes 2^a 3^b 5^c 7^d up to 4096 (WFT/WFT.h:18-32), first >= x
+    if (x > 4096) return -1;
+    for (int v = (x < 2 ? 2 : x + (x & 1)); v <= 4096; v += 2) {
+        int t = v;
+        while (t % 2 == 0) t /= 2;
+        while (t % 3 == 0) t /= 3;
+        while (t % 5 == 0) t /= 5;
+        while (t % 7 == 0) t /= 7;
+        if (t == 1) return v;
+    }
+    return -1;
+}
+
+extern "C" int glsu_wft_default_params(int wft_type, glsu_wff_params *p)
+{
+    if (!p) return fail(GLSU_ERR_INVALID, "null params");
+    if (wft_type == GLSU_WFT_WFF) {
+        // WFT/WFT2_CUDAf.cu:852-861 (float arithmetic as in WFT2_CUDAF)
+        const float s = 10.0f;
+        p->sigma_x = s; p->wxl = -2.0f - 3.0f / s; p->wxi = 1.0f / s; p->wxh = 2.0f + 3.0f / s;
+        p->sigma_y = s; p->wyl = -2.0f - 3.0f / s; p->wyi = 1.0f / s; p->wyh = 2.0f + 3.0f / s;
+        p->thr = -1;
+        return GLSU_OK;
+    }
+    if (wft_type == GLSU_WFT_WFR) {
+        p->sigma_x = 10; p->wxl = -2; p->wxi = 0.025f; p->wxh = 2;
+        p->sigma_y = 10; p->wyl = -2; p->wyi = 0.025f; p->wyh = 2;
+        p->thr = -1;
+        return GLSU_OK;
+    }
+    return fail(GLSU_ERR_INVALID, "unknown WFT type");
+}
+
+extern "C" int glsu_dpra_default_wff_params(glsu_wff_params *p)
+{
+    if (!p) return fail(GLSU_ERR_INVALID, "null params");
+    // DPRA/dpra_cudaf.cu:116-118 (float literals)
+    p->sigma_x = 20; p->wxl = -0.15f; p->wxh = 0.15f; p->wxi = 0.05f;
+    p->sigma_y = 20; p->wyl = -0.15f; p->wyh = 0.15f; p->wyi = 0.05f;
+    p->thr = 15;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_wff_count(double lo, double hi, double step, int precision)
+{
+    if (!(step > 0)) return fail(GLSU_ERR_INVALID, "step must be positive");
+    return wff_count_public(lo, hi, step, precision);
+}
+
+// splitmix64 + Box-Muller: deterministic N(0,1) draws for the AIA start
+static uint64_t splitmix64(uint64_t &s)
+{
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+extern "C" int glsu_aia_random_deltas(int M, uint64_t seed, float *deltas)
+{
+    if (M < 1 || !deltas) return fail(GLSU_ERR_INVALID, "bad arguments");
+    uint64_t s = seed;
+    deltas[0] = 0;
+    for (int i = 1; i < M; i++) {
+        const double u1 = ((splitmix64(s) >> 11) + 1) * (1.0 / 9007199254740993.0);
+        const double u2 = (splitmix64(s) >> 11) * (1.0 / 9007199254740992.0);
+        deltas[i] = (float)(std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * M_PI * u2));
+    }
+    return GLSU_OK;
+}
+
+// ===========================================================================
+// WFF2
+// ===========================================================================
+static int wff_setup_stream(cudaStream_t *s, bool *own)
+{
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(GLSU_ERR_NO_DEVICE, "no CUDA device visible");
+    }
+    GLSU_CUDA_TRY(cudaStreamCreateWithFlags(s, cudaStreamNonBlocking));
+    *own = true;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_wff_create(glsu_wff **out, int precision, int width, int height, const glsu_wff_params *p)
+{
+    if (!out) return fail(GLSU_ERR_INVALID, "null handle pointer");
+    *out = nullptr;
+    glsu_wff_params prm;
+    if (p) prm = *p;
+    else glsu_wft_default_params(GLSU_WFT_WFF, &prm);
+    glsu_wff *h = new glsu_wff();
+    int rc = h->plan.init(precision, width, height, prm);
+    if (rc == GLSU_OK) rc = wff_setup_stream(&h->stream, &h->own_stream);
+    if (rc == GLSU_OK) rc = h->plan.alloc_device();
+    if (rc == GLSU_OK) rc = h->plan.upload_tables(h->stream);
+    if (rc == GLSU_OK) rc = h->plan.make_tensor_map();
+    if (rc == GLSU_OK && (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess))
+        rc = fail(GLSU_ERR_CUDA, "cudaEventCreate failed");
+    if (rc != GLSU_OK) {
+        glsu_wff_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_wff_destroy(glsu_wff *h)
+{
+    if (!h) return GLSU_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    h->plan.release();
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_wff_set_stream(glsu_wff *h, void *stream)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    if (h->own_stream && h->stream) {
+        cudaStreamSynchronize(h->stream);
+        cudaStreamDestroy(h->stream);
+    }
+    h->stream = (cudaStream_t)stream;
+    h->own_stream = false;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_wff_run_async(glsu_wff *h, const void *d_f, void *d_filtered)
+{
+    if (!h || !d_f || !d_filtered) return fail(GLSU_ERR_INVALID, "null argument");
+    return h->plan.enqueue(h->stream, d_f, d_filtered, 0, nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+
+extern "C" int glsu_wff_run(glsu_wff *h, const void *d_f, void *d_filtered, double *time_ms)
+{
+    if (!h || !d_f || !d_filtered) return fail(GLSU_ERR_INVALID, "null argument");
+    GLSU_CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+    GLSU_TRY(h->plan.enqueue(h->stream, d_f, d_filtered, 0, nullptr, nullptr, nullptr, nullptr, nullptr));
+    GLSU_CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
+    GLSU_TRY(h->plan.check_device_error(h->stream));
+    if (time_ms) {
+        float ms = 0;
+        GLSU_CUDA_TRY(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+        *time_ms = ms;
+    }
+    return GLSU_OK;
+}
+
+extern "C" int glsu_wff_threshold(glsu_wff *h, double *thr)
+{
+    if (!h || !thr) return fail(GLSU_ERR_INVALID, "null argument");
+    if (h->plan.p.thr >= 0) {
+        *thr = h->plan.p.thr;
+        return GLSU_OK;
+    }
+    if (!h->plan.thr_ready) {
+        *thr = -1;
+        return GLSU_OK;
+    }
+    GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (h->plan.prec == GLSU_F32) {
+        float t;
+        GLSU_CUDA_TRY(cudaMemcpy(&t, h->plan.d_thr, sizeof(float), cudaMemcpyDeviceToHost));
+        *thr = t;
+    } else {
+        GLSU_CUDA_TRY(cudaMemcpy(thr, h->plan.d_thr, sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    return GLSU_OK;
+}
+
+extern "C" int glsu_wff_padded_size(const glsu_wff *h, int *pw, int *ph)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    if (pw) *pw = h->plan.Wp;
+    if (ph) *ph = h->plan.Hp;
+    return GLSU_OK;
+}
+
+// ===========================================================================
+// DPRA
+// ===========================================================================
+extern "C" int glsu_dpra_create(glsu_dpra **out, int precision, const void *h_phi0, int width, int height,
+                                int ref_update_rate, int window_radius, const glsu_wff_params *wff)
+{
+    if (!out) return fail(GLSU_ERR_INVALID, "null handle pointer");
+    *out = nullptr;
+    if (!h_phi0) return fail(GLSU_ERR_INVALID, "null initial phase");
+    if (ref_update_rate < 1) return fail(GLSU_ERR_INVALID, "reference update rate must be >= 1");
+    if (window_radius < 1 || window_radius > 8) return fail(GLSU_ERR_UNSUPPORTED, "DPRA window radius must be 1..8");
+    glsu_wff_params prm;
+    if (wff) prm = *wff;
+    else glsu_dpra_default_wff_params(&prm);
+    glsu_dpra *h = new glsu_dpra();
+    h->prec = precision;
+    h->W = width;
+    h->H = height;
+    h->rr = ref_update_rate;
+    h->r = window_radius;
+    int rc = h->wff.init(precision, width, height, prm);
+    if (rc == GLSU_OK) rc = wff_setup_stream(&h->stream, &h->own_stream);
+    if (rc == GLSU_OK) rc = h->wff.alloc_device();
+    if (rc == GLSU_OK) rc = h->wff.upload_tables(h->stream);
+    if (rc == GLSU_OK) rc = h->wff.make_tensor_map();
+    const size_t N = (size_t)width * height;
+    const size_t es = precision == GLSU_F32 ? 4 : 8;
+    if (rc == GLSU_OK) {
+        bool ok = cudaMalloc(&h->d_img, 8 * N) == cudaSuccess && cudaMalloc(&h->d_z, 2 * es * N) == cudaSuccess;
+        for (int k = 0; k < 4 && ok; k++) ok = cudaMalloc(&h->d_phi[k], es * N) == cudaSuccess;
+        ok = ok && cudaMallocHost(&h->h_in, 8 * N) == cudaSuccess && cudaMallocHost(&h->h_out, es * N) == cudaSuccess;
+        if (!ok) rc = fail(GLSU_ERR_ALLOC, "DPRA buffer allocation failed");
+    }
+    if (rc == GLSU_OK) {
+        if (cudaMemcpy(h->d_phi[GLSU_PHI_REF], h_phi0, es * N, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(h->d_phi[GLSU_PHI_CURR], h_phi0, es * N, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemset(h->d_phi[GLSU_DPHI_REF], 0, es * N) != cudaSuccess ||
+            cudaMemset(h->d_phi[GLSU_DPHI], 0, es * N) != cudaSuccess)
+            rc = fail(GLSU_ERR_CUDA, "initial phase upload failed");
+    }
+    for (int k = 0; k < 6 && rc == GLSU_OK; k++)
+        if (cudaEventCreate(&h->ev[k]) != cudaSuccess) rc = fail(GLSU_ERR_CUDA, "cudaEventCreate failed");
+    if (rc == GLSU_OK && (cudaEventCreate(&h->t0) != cudaSuccess || cudaEventCreate(&h->t1) != cudaSuccess))
+        rc = fail(GLSU_ERR_CUDA, "cudaEventCreate failed");
+    if (rc != GLSU_OK) {
+        glsu_dpra_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_destroy(glsu_dpra *h)
+{
+    if (!h) return GLSU_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    h->wff.release();
+    cudaFree(h->d_img);
+    cudaFree(h->d_z);
+    for (int k = 0; k < 4; k++) cudaFree(h->d_phi[k]);
+    cudaFreeHost(h->h_in);
+    cudaFreeHost(h->h_out);
+    for (int k = 0; k < 6; k++)
+        if (h->ev[k]) cudaEventDestroy(h->ev[k]);
+    if (h->t0) cudaEventDestroy(h->t0);
+    if (h->t1) cudaEventDestroy(h->t1);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_set_stream(glsu_dpra *h, void *stream)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    if (h->own_stream && h->stream) {
+        cudaStreamSynchronize(h->stream);
+        cudaStreamDestroy(h->stream);
+    }
+    h->stream = (cudaStream_t)stream;
+    h->own_stream = false;
+    return GLSU_OK;
+}
+
+static int dpra_check_type(glsu_dpra *h, int img_type)
+{
+    if (img_type == GLSU_U8 || img_type == GLSU_F32) return GLSU_OK;
+    if (img_type == GLSU_F64 && h->prec == GLSU_F64) return GLSU_OK;
+    return fail(GLSU_ERR_INVALID, "frame type must be GLSU_U8, GLSU_F32 or (FP64 handles) GLSU_F64");
+}
+
+extern "C" int glsu_dpra_per_frame_device(glsu_dpra *h, const void *d_img, int img_type, void *d_dphi)
+{
+    if (!h || !d_img) return fail(GLSU_ERR_INVALID, "null argument");
+    GLSU_TRY(dpra_check_type(h, img_type));
+    cudaEvent_t *ev = h->timing ? h->ev : nullptr;
+    if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[4], h->stream));
+    GLSU_TRY(launch_dpra_ls(h->prec, img_type, d_img, h->d_phi[GLSU_PHI_REF], h->d_z, h->W, h->H, h->r, h->stream));
+    GLSU_TRY(h->wff.enqueue(h->stream, h->d_z, nullptr, 1, h->d_phi[GLSU_PHI_REF], h->d_phi[GLSU_DPHI_REF],
+                            h->d_phi[GLSU_PHI_CURR], h->d_phi[GLSU_DPHI], ev));
+    h->synced = false;
+    h->frames_done++;
+    if (d_dphi) {
+        const size_t es = h->prec == GLSU_F32 ? 4 : 8;
+        GLSU_CUDA_TRY(cudaMemcpyAsync(d_dphi, h->d_phi[GLSU_DPHI], es * (size_t)h->W * h->H,
+                                      cudaMemcpyDeviceToDevice, h->stream));
+    }
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_per_frame(glsu_dpra *h, const void *h_img, int img_type, void *h_dphi, double *time_ms)
+{
+    if (!h || !h_img || !h_dphi) return fail(GLSU_ERR_INVALID, "null argument");
+    GLSU_TRY(dpra_check_type(h, img_type));
+    const size_t N = (size_t)h->W * h->H;
+    const size_t in_bytes = elem_size(img_type) * N;
+    const size_t es = h->prec == GLSU_F32 ? 4 : 8;
+    const bool pin_in = is_pinned(h_img), pin_out = is_pinned(h_dphi);
+    if (!pin_in) std::memcpy(h->h_in, h_img, in_bytes);
+    GLSU_CUDA_TRY(cudaEventRecord(h->t0, h->stream));
+    GLSU_CUDA_TRY(cudaMemcpyAsync(h->d_img, pin_in ? h_img : h->h_in, in_bytes, cudaMemcpyHostToDevice, h->stream));
+    GLSU_TRY(glsu_dpra_per_frame_device(h, h->d_img, img_type, nullptr));
+    GLSU_CUDA_TRY(cudaMemcpyAsync(pin_out ? h_dphi : h->h_out, h->d_phi[GLSU_DPHI], es * N, cudaMemcpyDeviceToHost,
+                                  h->stream));
+    GLSU_CUDA_TRY(cudaEventRecord(h->t1, h->stream));
+    GLSU_TRY(h->wff.check_device_error(h->stream));
+    if (!pin_out) std::memcpy(h_dphi, h->h_out, es * N);
+    if (time_ms) {
+        float ms = 0;
+        GLSU_CUDA_TRY(cudaEventElapsedTime(&ms, h->t0, h->t1));
+        *time_ms = ms;
+    }
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_update_ref_phi(glsu_dpra *h)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    if (h->synced) return GLSU_OK;  // phi_curr already equals phi_ref
+    // The reference copies phi_curr -> phi_ref and dphi -> dphi_ref
+    // (DPRA/dpra_cudaf.cu:286-290); exchanging the buffers gives the same
+    // state without the copies.
+    std::swap(h->d_phi[GLSU_PHI_REF], h->d_phi[GLSU_PHI_CURR]);
+    std::swap(h->d_phi[GLSU_DPHI_REF], h->d_phi[GLSU_DPHI]);
+    h->synced = true;
+    return GLSU_OK;
+}
+
+static int dpra_plane(glsu_dpra *h, int which, void **p)
+{
+    if (which < 0 || which > 3) return fail(GLSU_ERR_INVALID, "bad plane id");
+    if (h->synced && which == GLSU_PHI_CURR) which = GLSU_PHI_REF;
+    if (h->synced && which == GLSU_DPHI) which = GLSU_DPHI_REF;
+    *p = h->d_phi[which];
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_get(glsu_dpra *h, int which, void *h_out)
+{
+    if (!h || !h_out) return fail(GLSU_ERR_INVALID, "null argument");
+    void *p = nullptr;
+    GLSU_TRY(dpra_plane(h, which, &p));
+    const size_t es = h->prec == GLSU_F32 ? 4 : 8;
+    GLSU_CUDA_TRY(cudaMemcpyAsync(h_out, p, es * (size_t)h->W * h->H, cudaMemcpyDeviceToHost, h->stream));
+    GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_get_lsq(glsu_dpra *h, void *h_out)
+{
+    if (!h || !h_out) return fail(GLSU_ERR_INVALID, "null argument");
+    const size_t es = h->prec == GLSU_F32 ? 4 : 8;
+    GLSU_CUDA_TRY(cudaMemcpyAsync(h_out, h->d_z, 2 * es * (size_t)h->W * h->H, cudaMemcpyDeviceToHost, h->stream));
+    GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_device_ptr(glsu_dpra *h, int which, void **d_ptr)
+{
+    if (!h || !d_ptr) return fail(GLSU_ERR_INVALID, "null argument");
+    return dpra_plane(h, which, d_ptr);
+}
+
+extern "C" int glsu_dpra_sequence(glsu_dpra *h, int nframes, const void *h_frames, int img_type, void *h_dphi_all,
+                                  double *time_ms)
+{
+    if (!h || !h_frames || !h_dphi_all || nframes < 0) return fail(GLSU_ERR_INVALID, "bad argument");
+    const size_t N = (size_t)h->W * h->H;
+    const size_t es = h->prec == GLSU_F32 ? 4 : 8;
+    double total = 0;
+    for (int i = 0; i < nframes; i++) {
+        double t = 0;
+        GLSU_TRY(glsu_dpra_per_frame(h, (const char *)h_frames + elem_size(img_type) * N * i, img_type,
+                                     (char *)h_dphi_all + es * N * i, &t));
+        total += t;
+        if (i % h->rr == 0) GLSU_TRY(glsu_dpra_update_ref_phi(h));
+    }
+    if (time_ms) *time_ms = total;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_stage_timing(glsu_dpra *h, int enable)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    h->timing = enable != 0;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_stage_times(glsu_dpra *h, float *ms, int n)
+{
+    if (!h || !ms) return fail(GLSU_ERR_INVALID, "null argument");
+    if (!h->timing || h->frames_done == 0) return 0;
+    GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    const cudaEvent_t seq[5] = {h->ev[4], h->ev[0], h->ev[1], h->ev[2], h->ev[3]};
+    int k = 0;
+    for (; k < 4 && k < n; k++) GLSU_CUDA_TRY(cudaEventElapsedTime(&ms[k], seq[k], seq[k + 1]));
+    return k;
+}
+
+// ===========================================================================
+// AIA
+// ===========================================================================
+extern "C" int glsu_aia_create(glsu_aia **out, int M, int cols, int rows)
+{
+    if (!out) return fail(GLSU_ERR_INVALID, "null handle pointer");
+    *out = nullptr;
+    if (M < 3 || M > 32) return fail(GLSU_ERR_INVALID, "AIA needs 3..32 frames");
+    if (cols < 1 || rows < 1) return fail(GLSU_ERR_INVALID, "image size must be positive");
+    glsu_aia *h = new glsu_aia();
+    h->M = M;
+    h->cols = cols;
+    h->rows = rows;
+    h->N = cols * rows;
+    int rc = wff_setup_stream(&h->stream, &h->own_stream);
+    h->dev.M = M;
+    h->dev.N = h->N;
+    h->dev.nblocks = 152 * 2;
+    if (rc == GLSU_OK) {
+        const size_t nv = 5 + 3 * (size_t)M;
+        bool ok = cudaMalloc(&h->d_frames, (size_t)M * h->N * 4) == cudaSuccess &&
+                  cudaMalloc((void **)&h->d_phi, sizeof(float) * h->N) == cudaSuccess &&
+                  cudaMalloc((void **)&h->dev.d_part, sizeof(double) * nv * h->dev.nblocks) == cudaSuccess &&
+                  cudaMalloc((void **)&h->dev.d_state, sizeof(double) * (2 * M + 3)) == cudaSuccess &&
+                  cudaMalloc((void **)&h->dev.d_done, sizeof(int)) == cudaSuccess;
+        if (!ok) rc = fail(GLSU_ERR_ALLOC, "AIA buffer allocation failed");
+    }
+    if (rc == GLSU_OK && (cudaEventCreate(&h->t0) != cudaSuccess || cudaEventCreate(&h->t1) != cudaSuccess))
+        rc = fail(GLSU_ERR_CUDA, "cudaEventCreate failed");
+    if (rc != GLSU_OK) {
+        glsu_aia_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_aia_destroy(glsu_aia *h)
+{
+    if (!h) return GLSU_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaFree(h->d_frames);
+    cudaFree(h->d_phi);
+    cudaFree(h->dev.d_part);
+    cudaFree(h->dev.d_state);
+    cudaFree(h->dev.d_done);
+    if (h->t0) cudaEventDestroy(h->t0);
+    if (h->t1) cudaEventDestroy(h->t1);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_aia_set_stream(glsu_aia *h, void *stream)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    if (h->own_stream && h->stream) {
+        cudaStreamSynchronize(h->stream);
+        cudaStreamDestroy(h->stream);
+    }
+    h->stream = (cudaStream_t)stream;
+    h->own_stream = false;
+    return GLSU_OK;
+}
+
+static int aia_core(glsu_aia *h, const void *d_frames, int img_type, float *d_phi, float *h_deltas, int n_deltas_in,
+                    int *iters, float *err, int max_iter, float max_err, uint64_t seed, double *time_ms)
+{
+    std::vector<float> d0(h->M);
+    if (n_deltas_in == h->M) {
+        for (int i = 0; i < h->M; i++) d0[i] = h_deltas[i];
+    } else {
+        GLSU_TRY(glsu_aia_random_deltas(h->M, seed, d0.data()));
+    }
+    std::vector<double> dd(d0.begin(), d0.end());
+    cudaStream_t s = h->stream;
+    GLSU_CUDA_TRY(cudaEventRecord(h->t0, s));
+    GLSU_TRY(aia_launch_init(h->dev, dd.data(), s));
+    for (int it = 0; it < max_iter; it++) {
+        GLSU_TRY(aia_launch_pass(h->dev, img_type, d_frames, 0, nullptr, s));
+        GLSU_TRY(aia_launch_solve(h->dev, max_iter, (double)max_err, s));
+    }
+    GLSU_CUDA_TRY(cudaEventRecord(h->t1, s));
+    GLSU_TRY(aia_launch_pass(h->dev, img_type, d_frames, 1, d_phi, s));
+    GLSU_TRY(aia_launch_finalize(h->dev, d_phi, s));
+    std::vector<double> st(2 * h->M + 3);
+    GLSU_CUDA_TRY(cudaMemcpyAsync(st.data(), h->dev.d_state, sizeof(double) * st.size(), cudaMemcpyDeviceToHost, s));
+    GLSU_CUDA_TRY(cudaStreamSynchronize(s));
+    if (st[2 * h->M + 2] != 0) return fail(GLSU_ERR_NOT_POSDEF, "The leading minor is not positive definite");
+    for (int i = 0; i < h->M; i++) h_deltas[i] = (float)st[i];
+    if (iters) *iters = (int)st[2 * h->M + 1];
+    if (err) *err = max_iter > 0 ? (float)st[2 * h->M] : 2.0f * max_err;
+    if (time_ms) {
+        float ms = 0;
+        GLSU_CUDA_TRY(cudaEventElapsedTime(&ms, h->t0, h->t1));
+        *time_ms = ms;
+    }
+    return GLSU_OK;
+}
+
+extern "C" int glsu_aia_run(glsu_aia *h, const void *const *h_frames, int img_type, float *h_phi, float *h_deltas,
+                            int n_deltas_in, double *time_ms, int *iters, float *err, int max_iter, float max_err,
+                            uint64_t seed)
+{
+    if (!h || !h_frames || !h_phi || !h_deltas) return fail(GLSU_ERR_INVALID, "null argument");
+    if (img_type != GLSU_U8 && img_type != GLSU_F32) return fail(GLSU_ERR_INVALID, "frames must be U8 or F32");
+    const size_t fb = elem_size(img_type) * (size_t)h->N;
+    for (int i = 0; i < h->M; i++) {
+        if (!h_frames[i]) return fail(GLSU_ERR_INVALID, "null frame");
+        GLSU_CUDA_TRY(cudaMemcpyAsync((char *)h->d_frames + fb * i, h_frames[i], fb, cudaMemcpyHostToDevice, h->stream));
+    }
+    GLSU_TRY(aia_core(h, h->d_frames, img_type, h->d_phi, h_deltas, n_deltas_in, iters, err, max_iter, max_err, seed,
+                      time_ms));
+    GLSU_CUDA_TRY(cudaMemcpy(h_phi, h->d_phi, sizeof(float) * h->N, cudaMemcpyDeviceToHost));
+    return GLSU_OK;
+}
+
+extern "C" int glsu_aia_run_device(glsu_aia *h, const void *d_frames, int img_type, float *d_phi, float *h_deltas,
+                                   int n_deltas_in, int *iters, float *err, int max_iter, float max_err,
+                                   uint64_t seed)
+{
+    if (!h || !d_frames || !d_phi || !h_deltas) return fail(GLSU_ERR_INVALID, "null argument");
+    if (img_type != GLSU_U8 && img_type != GLSU_F32) return fail(GLSU_ERR_INVALID, "frames must be U8 or F32");
+    return aia_core(h, d_frames, img_type, d_phi, h_deltas, n_deltas_in, iters, err, max_iter, max_err, seed,
+                    nullptr);
+}

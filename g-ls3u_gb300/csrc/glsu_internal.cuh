@@ -1,0 +1,120 @@
+// glsu_internal.cuh -- shared declarations of the G-LS3U CUDA library (sm_103a).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/glsu.h"
+
+namespace glsu {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define GLSU_CUDA_TRY(call)                                  \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);  \
+    } while (0)
+
+#define GLSU_TRY(call)                  \
+    do {                                \
+        int rc_ = (call);               \
+        if (rc_ != GLSU_OK) return rc_; \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// complex element types
+// ---------------------------------------------------------------------------
+template <typename T> struct C2T;
+template <> struct C2T<float> { using type = float2; };
+template <> struct C2T<double> { using type = double2; };
+template <typename T> using C2 = typename C2T<T>::type;
+
+// Largest supported window half-size round(3*sigma) of WFF2.  Kernels are
+// instantiated for half-sizes 12, 20, 30, 45 and 60; a smaller half-size
+// runs in the next instantiation with zero taps outside its window, which
+// leaves every sum unchanged.
+constexpr int kMaxHalf = 60;
+int instantiated_half(int s);  // -> 12/20/30/45/60, or -1 when s > kMaxHalf
+
+// Padding (in elements) of the phasor tables on each side.
+constexpr int kPhasorPad = 2 * kMaxHalf;
+
+// Bounded device-side waits: spin limit of an mbarrier wait before the
+// kernel records GLSU_ERR_TIMEOUT in its error word and returns.
+constexpr long long kSpinLimit = 1ll << 26;
+
+// ---------------------------------------------------------------------------
+// WFF2 plan: the frequency sweep on the device (see wff_kernels.cu)
+// ---------------------------------------------------------------------------
+struct WffPlan {
+    int prec = GLSU_F32;
+    int W = 0, H = 0, pitch = 0;  // pitch: row pitch (elements) of the internal planes
+    glsu_wff_params p{};
+    int sx = 0, sy = 0;          // true half window sizes
+    int sxi = 0, syi = 0;        // instantiated half sizes
+    int nfx = 0, nfy = 0;        // frequency counts
+    int Wp = 0, Hp = 0;          // FFT-padded plane of the reference formulation
+    double thr_host = -1;        // threshold in use (after the first run when automatic)
+    bool thr_ready = false;
+
+    // device buffers
+    void *d_ex = nullptr;   // nfx x (pitch + 2*pad) phasors exp(-j wx x)
+    void *d_ey = nullptr;   // nfy x (H + 2*pad)     phasors exp(-j wy y)
+    void *d_R = nullptr;    // nfx planes H x pitch: row-filtered, demodulated input
+    void *d_C = nullptr;    // nfx planes H x pitch: column sweep output
+    void *d_thr = nullptr;  // 1 element of T: threshold used by the kernels
+    double *d_part = nullptr;  // partial sums of the automatic threshold
+    int *d_err = nullptr;      // device error word (bounded waits)
+    CUtensorMap tmR;        // TMA descriptor of d_R (3D: 2*pitch floats x H x nfx)
+    bool external_scratch = false;  // d_R/d_C/d_thr/d_part/d_err owned elsewhere
+
+    // host copies of the taps (device code receives them as kernel parameters)
+    double gx[2 * kMaxHalf + 1], gy[2 * kMaxHalf + 1];
+    double inv_norm = 1, scale = 1;
+
+    int init(int precision, int width, int height, const glsu_wff_params &prm);
+    int alloc_device();
+    int upload_tables(cudaStream_t s);
+    int make_tensor_map();
+    void release();
+    size_t plane_bytes() const;  // bytes of one internal plane
+    // Enqueue one WFF2 of d_f (H x W complex).  final_mode 0 writes the
+    // filtered field to d_out; final_mode 1 applies the DPRA phase update
+    // instead (phi_ref, dphi_ref -> phi_curr, dphi).
+    int enqueue(cudaStream_t s, const void *d_f, void *d_out, int final_mode, const void *phi_ref,
+                const void *dphi_ref, void *phi_curr, void *dphi, cudaEvent_t *stage_ev);
+    int check_device_error(cudaStream_t s);
+};
+
+// ---------------------------------------------------------------------------
+// kernel launchers
+// ---------------------------------------------------------------------------
+int launch_dpra_ls(int prec, int img_type, const void *d_img, const void *d_phiref, void *d_z, int W, int H,
+                   int r, cudaStream_t s);
+int launch_dpra_update(int prec, const void *d_filtered, const void *phiref, const void *dphiref,
+                       void *phicurr, void *dphi, int n, cudaStream_t s);
+
+// AIA
+struct AiaDev {
+    int M = 0, N = 0;
+    int nblocks = 0;
+    double *d_part = nullptr;   // nblocks x (5 + 3M) partial sums
+    double *d_state = nullptr;  // deltas, old deltas, err, iteration, flags
+    int *d_done = nullptr;
+};
+int aia_launch_pass(const AiaDev &a, int img_type, const void *d_frames, int final_pass, float *d_phi,
+                    cudaStream_t s);
+int aia_launch_solve(const AiaDev &a, int max_iter, double max_err, cudaStream_t s);
+int aia_launch_init(const AiaDev &a, const double *h_deltas, cudaStream_t s);
+int aia_launch_finalize(const AiaDev &a, float *d_phi, cudaStream_t s);
+
+}  // namespace glsu

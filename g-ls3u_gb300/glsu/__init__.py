@@ -1,0 +1,352 @@
+"""Python host interface of the GB300 G-LS3U hot path (ctypes over ``libglsu.so``).
+
+The classes mirror the reference's C++ interfaces (paths inside the
+reference project):
+
+- :class:`WFF2` -- ``WFT_FPA::WFT::WFT2_CUDAF`` / ``WFT2_CUDA`` with
+  ``WFT_TYPE::WFF`` (``WFT/WFT2_CUDAf.h:11-40``); arguments in the C++ order
+  sigma, low, high, step.
+- :class:`DPRA` -- ``DPRA::DPRA_CUDAF`` (``DPRA/dpra_cudaf.h:21-46``) and the FP64
+  ``DPRA::DPRA_CUDA``, with ``DPRA_CPU::operator()`` semantics for sequences
+  (``DPRA/dpra_cpu.cpp:58-89``).
+- :class:`AIA` -- ``AIA::AIA_CUDAF`` (``AIA/aia_cudaf.h:15-38``).
+
+There is no CPU fallback: importing works anywhere, but every compute call
+goes through the CUDA library and raises if it is not built or no GPU is
+present.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+import threading
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.dirname(_HERE)
+LIB_PATH = os.path.join(PKG_ROOT, "lib", "libglsu.so")
+HEADER = os.path.join(os.path.dirname(PKG_ROOT), "include", "glsu.h")
+
+OK = 0
+ERR_INVALID, ERR_PADDING, ERR_CUDA, ERR_ALLOC = -1, -2, -3, -4
+ERR_UNSUPPORTED, ERR_NOT_POSDEF, ERR_TIMEOUT, ERR_NO_DEVICE = -5, -6, -7, -8
+F32, F64, U8 = 0, 1, 2
+PHI_REF, PHI_CURR, DPHI_REF, DPHI = 0, 1, 2, 3
+WFT_WFF, WFT_WFR = 0, 1
+
+_lock = threading.Lock()
+_lib = None
+
+
+class GlsuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("glsu error %d: %s" % (code, msg))
+        self.code = code
+
+
+class WffParamsC(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("sigma_x", "wxl", "wxh", "wxi", "sigma_y", "wyl", "wyh", "wyi", "thr")]
+
+
+@dataclass
+class WffParams:
+    """WFF2 parameters in the reference's C++ order (sigma, low, high, step)."""
+    sigma_x: float = 10.0
+    wxl: float = -1.0
+    wxh: float = 1.0
+    wxi: float = 0.1
+    sigma_y: float = 10.0
+    wyl: float = -1.0
+    wyh: float = 1.0
+    wyi: float = 0.1
+    thr: float = 0.2
+
+    def c(self) -> WffParamsC:
+        return WffParamsC(*[float(getattr(self, f[0])) for f in WffParamsC._fields_])
+
+    def tuple(self):
+        return tuple(float(getattr(self, f[0])) for f in WffParamsC._fields_)
+
+
+def exported_symbols() -> list[str]:
+    """Function names declared in include/glsu.h."""
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(glsu_\w+)\s*\(", txt, re.M)))
+
+
+def lib() -> ctypes.CDLL:
+    """Load libglsu.so; raises if the CUDA library has not been built."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libglsu.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        c_int, c_double, c_void_p, c_float = ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_float
+        pp = ctypes.POINTER(c_void_p)
+        dblp = ctypes.POINTER(c_double)
+        intp = ctypes.POINTER(c_int)
+        fltp = ctypes.POINTER(c_float)
+        prm = ctypes.POINTER(WffParamsC)
+        sig = {
+            "glsu_last_error": ([], ctypes.c_char_p),
+            "glsu_version": ([], c_int),
+            "glsu_opt_fft_size": ([c_int], c_int),
+            "glsu_wft_default_params": ([c_int, prm], c_int),
+            "glsu_dpra_default_wff_params": ([prm], c_int),
+            "glsu_wff_count": ([c_double, c_double, c_double, c_int], c_int),
+            "glsu_aia_random_deltas": ([c_int, ctypes.c_uint64, fltp], c_int),
+            "glsu_wff_create": ([pp, c_int, c_int, c_int, prm], c_int),
+            "glsu_wff_destroy": ([c_void_p], c_int),
+            "glsu_wff_set_stream": ([c_void_p, c_void_p], c_int),
+            "glsu_wff_run": ([c_void_p, c_void_p, c_void_p, dblp], c_int),
+            "glsu_wff_run_async": ([c_void_p, c_void_p, c_void_p], c_int),
+            "glsu_wff_threshold": ([c_void_p, dblp], c_int),
+            "glsu_wff_padded_size": ([c_void_p, intp, intp], c_int),
+            "glsu_dpra_create": ([pp, c_int, c_void_p, c_int, c_int, c_int, c_int, prm], c_int),
+            "glsu_dpra_destroy": ([c_void_p], c_int),
+            "glsu_dpra_set_stream": ([c_void_p, c_void_p], c_int),
+            "glsu_dpra_per_frame": ([c_void_p, c_void_p, c_int, c_void_p, dblp], c_int),
+            "glsu_dpra_per_frame_device": ([c_void_p, c_void_p, c_int, c_void_p], c_int),
+            "glsu_dpra_update_ref_phi": ([c_void_p], c_int),
+            "glsu_dpra_sequence": ([c_void_p, c_int, c_void_p, c_int, c_void_p, dblp], c_int),
+            "glsu_dpra_get": ([c_void_p, c_int, c_void_p], c_int),
+            "glsu_dpra_device_ptr": ([c_void_p, c_int, pp], c_int),
+            "glsu_dpra_get_lsq": ([c_void_p, c_void_p], c_int),
+            "glsu_dpra_stage_timing": ([c_void_p, c_int], c_int),
+            "glsu_dpra_stage_times": ([c_void_p, fltp, c_int], c_int),
+            "glsu_aia_create": ([pp, c_int, c_int, c_int], c_int),
+            "glsu_aia_destroy": ([c_void_p], c_int),
+            "glsu_aia_set_stream": ([c_void_p, c_void_p], c_int),
+            "glsu_aia_run": ([c_void_p, pp, c_int, fltp, fltp, c_int, dblp, intp, fltp, c_int, c_float,
+                              ctypes.c_uint64], c_int),
+            "glsu_aia_run_device": ([c_void_p, c_void_p, c_int, fltp, fltp, c_int, intp, fltp, c_int, c_float,
+                                     ctypes.c_uint64], c_int),
+        }
+        for name, (args, res) in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+        return _lib
+
+
+def check(rc: int) -> int:
+    if rc < 0:
+        raise GlsuError(rc, lib().glsu_last_error().decode(errors="replace"))
+    return rc
+
+
+def _ptr(a: np.ndarray) -> ctypes.c_void_p:
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def opt_fft_size(x: int) -> int:
+    return lib().glsu_opt_fft_size(int(x))
+
+
+def wff_count(lo: float, hi: float, step: float, precision: int = F64) -> int:
+    return check(lib().glsu_wff_count(lo, hi, step, precision))
+
+
+def default_params(wft_type: int = WFT_WFF) -> WffParams:
+    c = WffParamsC()
+    check(lib().glsu_wft_default_params(wft_type, ctypes.byref(c)))
+    return WffParams(*[getattr(c, f[0]) for f in WffParamsC._fields_])
+
+
+def dpra_default_params() -> WffParams:
+    c = WffParamsC()
+    check(lib().glsu_dpra_default_wff_params(ctypes.byref(c)))
+    return WffParams(*[getattr(c, f[0]) for f in WffParamsC._fields_])
+
+
+def random_deltas(M: int, seed: int) -> np.ndarray:
+    d = np.zeros(M, np.float32)
+    check(lib().glsu_aia_random_deltas(M, ctypes.c_uint64(seed), d.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+    return d
+
+
+def _prec(p) -> int:
+    if p in (F32, "f32", "float32", np.float32):
+        return F32
+    if p in (F64, "f64", "float64", np.float64):
+        return F64
+    raise ValueError("precision must be f32 or f64")
+
+
+def _img_type(a: np.ndarray) -> int:
+    if a.dtype == np.uint8:
+        return U8
+    if a.dtype == np.float32:
+        return F32
+    if a.dtype == np.float64:
+        return F64
+    raise TypeError("frames must be uint8, float32 or float64")
+
+
+class WFF2:
+    """Windowed Fourier filtering (WFT2_CUDAF / WFT2_CUDA with WFT_TYPE::WFF).
+
+    Operates on device buffers: ``run(d_f, d_out)`` takes device addresses of
+    H*W complex arrays (complex64 for f32, complex128 for f64)."""
+
+    def __init__(self, width: int, height: int, precision="f32", params: WffParams | None = None,
+                 wft_type: int = WFT_WFF):
+        if wft_type != WFT_WFF:
+            raise GlsuError(ERR_UNSUPPORTED, "only WFT_TYPE::WFF is implemented")
+        self.width, self.height, self.precision = width, height, _prec(precision)
+        h = ctypes.c_void_p()
+        pc = ctypes.byref(params.c()) if params is not None else None
+        check(lib().glsu_wff_create(ctypes.byref(h), self.precision, width, height, pc))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().glsu_wff_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def set_stream(self, stream_ptr: int):
+        check(lib().glsu_wff_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
+
+    def run(self, d_f: int, d_out: int) -> float:
+        t = ctypes.c_double(0)
+        check(lib().glsu_wff_run(self._h, ctypes.c_void_p(d_f), ctypes.c_void_p(d_out), ctypes.byref(t)))
+        return t.value
+
+    def run_async(self, d_f: int, d_out: int):
+        check(lib().glsu_wff_run_async(self._h, ctypes.c_void_p(d_f), ctypes.c_void_p(d_out)))
+
+    @property
+    def threshold(self) -> float:
+        t = ctypes.c_double(0)
+        check(lib().glsu_wff_threshold(self._h, ctypes.byref(t)))
+        return t.value
+
+    @property
+    def padded_size(self):
+        w, h = ctypes.c_int(0), ctypes.c_int(0)
+        check(lib().glsu_wff_padded_size(self._h, ctypes.byref(w), ctypes.byref(h)))
+        return w.value, h.value
+
+
+class DPRA:
+    """DPRA_CUDAF (precision f32) / DPRA_CUDA (precision f64)."""
+
+    def __init__(self, phi0: np.ndarray, ref_update_rate: int = 1, window_radius: int = 1, precision="f32",
+                 wff: WffParams | None = None):
+        self.precision = _prec(precision)
+        dt = np.float32 if self.precision == F32 else np.float64
+        phi0 = np.ascontiguousarray(phi0, dtype=dt)
+        self.height, self.width = phi0.shape
+        self.dtype = dt
+        self.rr = ref_update_rate
+        h = ctypes.c_void_p()
+        pc = ctypes.byref(wff.c()) if wff is not None else None
+        check(lib().glsu_dpra_create(ctypes.byref(h), self.precision, _ptr(phi0), self.width, self.height,
+                                     ref_update_rate, window_radius, pc))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().glsu_dpra_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def set_stream(self, stream_ptr: int):
+        check(lib().glsu_dpra_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
+
+    def per_frame(self, img: np.ndarray, out: np.ndarray | None = None):
+        img = np.ascontiguousarray(img)
+        if out is None:
+            out = np.empty((self.height, self.width), self.dtype)
+        t = ctypes.c_double(0)
+        check(lib().glsu_dpra_per_frame(self._h, _ptr(img), _img_type(img), _ptr(out), ctypes.byref(t)))
+        return out, t.value
+
+    def per_frame_ptr(self, h_img_ptr: int, img_type: int, h_out_ptr: int) -> float:
+        t = ctypes.c_double(0)
+        check(lib().glsu_dpra_per_frame(self._h, ctypes.c_void_p(h_img_ptr), img_type, ctypes.c_void_p(h_out_ptr),
+                                        ctypes.byref(t)))
+        return t.value
+
+    def per_frame_device(self, d_img: int, img_type: int, d_dphi: int = 0):
+        check(lib().glsu_dpra_per_frame_device(self._h, ctypes.c_void_p(d_img), img_type,
+                                               ctypes.c_void_p(d_dphi) if d_dphi else None))
+
+    def update_ref_phi(self):
+        check(lib().glsu_dpra_update_ref_phi(self._h))
+
+    def sequence(self, frames: np.ndarray):
+        frames = np.ascontiguousarray(frames)
+        out = np.empty((frames.shape[0], self.height, self.width), self.dtype)
+        t = ctypes.c_double(0)
+        check(lib().glsu_dpra_sequence(self._h, frames.shape[0], _ptr(frames), _img_type(frames), _ptr(out),
+                                       ctypes.byref(t)))
+        return out, t.value
+
+    def get(self, which: int) -> np.ndarray:
+        out = np.empty((self.height, self.width), self.dtype)
+        check(lib().glsu_dpra_get(self._h, which, _ptr(out)))
+        return out
+
+    def get_lsq(self) -> np.ndarray:
+        """exp(j dphi) of the last frame's least-squares stage (the WFF2 input)."""
+        out = np.empty((self.height, self.width), np.complex64 if self.precision == F32 else np.complex128)
+        check(lib().glsu_dpra_get_lsq(self._h, _ptr(out)))
+        return out
+
+    def device_ptr(self, which: int) -> int:
+        p = ctypes.c_void_p()
+        check(lib().glsu_dpra_device_ptr(self._h, which, ctypes.byref(p)))
+        return p.value
+
+    def stage_timing(self, enable: bool = True):
+        check(lib().glsu_dpra_stage_timing(self._h, int(enable)))
+
+    def stage_times(self):
+        ms = (ctypes.c_float * 4)()
+        n = check(lib().glsu_dpra_stage_times(self._h, ms, 4))
+        return list(ms[:n])
+
+
+class AIA:
+    """AIA_CUDAF: initial phase from M frames with unknown phase shifts."""
+
+    def __init__(self, M: int, cols: int, rows: int):
+        self.M, self.cols, self.rows = M, cols, rows
+        h = ctypes.c_void_p()
+        check(lib().glsu_aia_create(ctypes.byref(h), M, cols, rows))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().glsu_aia_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def run(self, frames, deltas=None, max_iter: int = 20, max_err: float = 1e-4, seed: int = 0):
+        frames = [np.ascontiguousarray(f) for f in frames]
+        it = _img_type(frames[0])
+        ptrs = (ctypes.c_void_p * len(frames))(*[f.ctypes.data for f in frames])
+        d = np.zeros(self.M, np.float32)
+        n_in = 0
+        if deltas is not None:
+            d[:len(deltas)] = np.asarray(deltas, np.float32)[:self.M]
+            n_in = len(deltas)
+        phi = np.empty((self.rows, self.cols), np.float32)
+        t, iters, err = ctypes.c_double(0), ctypes.c_int(0), ctypes.c_float(0)
+        fp = ctypes.POINTER(ctypes.c_float)
+        check(lib().glsu_aia_run(self._h, ptrs, it, phi.ctypes.data_as(fp), d.ctypes.data_as(fp), n_in,
+                                 ctypes.byref(t), ctypes.byref(iters), ctypes.byref(err), max_iter,
+                                 ctypes.c_float(max_err), ctypes.c_uint64(seed)))
+        return phi, d, t.value, iters.value, err.value

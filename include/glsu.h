@@ -1,0 +1,167 @@
+/*
+ * glsu.h -- C ABI of the GB300 (sm_103a) G-LS3U hot path.
+ *
+ * Plain pointers and sizes only.  Every call returns a status code (GLSU_OK or
+ * a negative GLSU_ERR_*) and never exits the process; glsu_last_error()
+ * returns a message for the calling thread's last failure.  Handles are not
+ * thread-safe: use one handle per host thread.  Each handle owns a CUDA
+ * stream unless one is set with *_set_stream.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   glsu_wff_*   WFT_FPA::WFT::WFT2_CUDAF / WFT2_CUDA with WFT_TYPE::WFF
+ *                (WFT/WFT2_CUDAf.h:11-40, WFT/WFT2_CUDA.h), whose CPU twin is
+ *                WFT/WFT2_CPU.cpp:190-390
+ *   glsu_dpra_*  DPRA::DPRA_CUDAF (DPRA/dpra_cudaf.h:21-46) and the empty
+ *                DPRA::DPRA_CUDA (DPRA/dpra_cuda.h:9-14), following the
+ *                semantics of DPRA_CPU (DPRA/dpra_cpu.h:30-64)
+ *   glsu_aia_*   AIA::AIA_CUDAF (AIA/aia_cudaf.h:15-38)
+ * The C++ classes with the reference's names and signatures live in
+ * glsu_classes.hpp and are implemented on top of these functions.
+ */
+#ifndef GLSU_H
+#define GLSU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GLSU_OK 0
+#define GLSU_ERR_INVALID (-1)     /* bad argument or size                      */
+#define GLSU_ERR_PADDING (-2)     /* padded size beyond 4096 (reference: throw -1) */
+#define GLSU_ERR_CUDA (-3)        /* a CUDA runtime call failed                */
+#define GLSU_ERR_ALLOC (-4)       /* device or pinned allocation failed        */
+#define GLSU_ERR_UNSUPPORTED (-5) /* e.g. WFT_TYPE::WFR, window beyond limits  */
+#define GLSU_ERR_NOT_POSDEF (-6)  /* AIA normal matrix not positive definite   */
+#define GLSU_ERR_TIMEOUT (-7)     /* a bounded device-side wait gave up        */
+#define GLSU_ERR_NO_DEVICE (-8)   /* no CUDA device visible                    */
+
+/* ---- element types ----------------------------------------------------- */
+#define GLSU_F32 0 /* float  / float2 complex  (the *_CUDAF classes)        */
+#define GLSU_F64 1 /* double / double2 complex (the *_CUDA classes)         */
+#define GLSU_U8 2  /* uint8 fringe frames (cv::Mat CV_8UC1 in the reference) */
+
+/* ---- which state plane (glsu_dpra_get / glsu_dpra_device_ptr) ----------- */
+#define GLSU_PHI_REF 0
+#define GLSU_PHI_CURR 1
+#define GLSU_DPHI_REF 2
+#define GLSU_DPHI 3
+
+/* WFT_TYPE of the reference (WFT-FPA.h enum WFT_TYPE) */
+#define GLSU_WFT_WFF 0
+#define GLSU_WFT_WFR 1
+
+typedef struct glsu_wff glsu_wff;
+typedef struct glsu_dpra glsu_dpra;
+typedef struct glsu_aia glsu_aia;
+
+/* WFF2 parameters, in the reference's C++ order: sigma, low, high, step
+ * (WFT/WFT2_CUDAf.h:27-33).  thr < 0 selects 6*sqrt(mean(|f|^2)/3), computed
+ * on the device at the first call and kept for later calls
+ * (WFT/WFT2_CPU.cpp:977-1005). */
+typedef struct glsu_wff_params {
+    double sigma_x, wxl, wxh, wxi;
+    double sigma_y, wyl, wyh, wyi;
+    double thr;
+} glsu_wff_params;
+
+/* ---- utilities (host only, no device needed) ---------------------------- */
+const char *glsu_last_error(void);
+int glsu_version(void);
+/* Smallest even 2^a3^b5^c7^d size >= x, or -1 (WFT/WFT.h:18-32, WFT/WFT.cpp:10-23). */
+int glsu_opt_fft_size(int x);
+/* Default WFF/WFR parameters of a WFT_TYPE (WFT/WFT2_CUDAf.cu:852-875). */
+int glsu_wft_default_params(int wft_type, glsu_wff_params *p);
+/* Parameters DPRA hard-wires for its WFF (DPRA/dpra_cudaf.cu:116-118). */
+int glsu_dpra_default_wff_params(glsu_wff_params *p);
+/* Number of frequencies on [lo, hi] with step, as the reference computes it
+ * in the given precision: int((hi-lo)*(1/step))+1 (WFT/WFT2_CPU.cpp:222-223). */
+int glsu_wff_count(double lo, double hi, double step, int precision);
+/* Seeded initial AIA phase shifts: d[0]=0, d[1..M-1] ~ N(0,1) (replaces the
+ * time-seeded draw of AIA/aia_cpu.cpp:32-46). */
+int glsu_aia_random_deltas(int M, uint64_t seed, float *deltas);
+
+/* ---- WFF2: WFT2_CUDAF / WFT2_CUDA with WFT_TYPE::WFF -------------------- */
+/* precision: GLSU_F32 or GLSU_F64.  p == NULL: reference WFF defaults.
+ * Windows up to half-size round(3*sigma) <= 60 are supported. */
+int glsu_wff_create(glsu_wff **out, int precision, int width, int height, const glsu_wff_params *p);
+int glsu_wff_destroy(glsu_wff *h);
+int glsu_wff_set_stream(glsu_wff *h, void *cuda_stream);
+/* d_f: device H*W complex input; d_filtered: device H*W complex output
+ * (WFT2_CUDAF::operator(), WFT/WFT2_CUDAf.cu:1003-1011).  Synchronous;
+ * *time_ms (may be NULL) receives the device time of the call. */
+int glsu_wff_run(glsu_wff *h, const void *d_f, void *d_filtered, double *time_ms);
+/* Same, enqueued on the handle's stream without waiting. */
+int glsu_wff_run_async(glsu_wff *h, const void *d_f, void *d_filtered);
+/* Threshold in use (after the first call when automatic). */
+int glsu_wff_threshold(glsu_wff *h, double *thr);
+/* FFT-padded plane of the reference's formulation (kept for API parity). */
+int glsu_wff_padded_size(const glsu_wff *h, int *padded_width, int *padded_height);
+
+/* ---- DPRA: DPRA_CUDAF (F32) / DPRA_CUDA (F64) --------------------------- */
+/* h_phi0: HOST pointer to W*H initial phase in the handle's precision
+ * (copied to the device, as DPRA_CUDAF's constructor does).
+ * window_radius r gives a (2r+1)^2 window (the reference hard-wires r=1);
+ * wff == NULL selects the reference's hard-wired WFF parameters. */
+int glsu_dpra_create(glsu_dpra **out, int precision, const void *h_phi0, int width, int height,
+                     int ref_update_rate, int window_radius, const glsu_wff_params *wff);
+int glsu_dpra_destroy(glsu_dpra *h);
+int glsu_dpra_set_stream(glsu_dpra *h, void *cuda_stream);
+/* DPRA_CUDAF::dpra_per_frame: h_img is a HOST frame (img_type GLSU_U8, or
+ * the handle's precision), h_dphi receives the HOST W*H phase change.
+ * Synchronous; *time_ms (may be NULL) gets the device time including copies. */
+int glsu_dpra_per_frame(glsu_dpra *h, const void *h_img, int img_type, void *h_dphi, double *time_ms);
+/* Same on device buffers, enqueued on the handle's stream.  d_dphi may be
+ * NULL (the phase change stays in the handle). */
+int glsu_dpra_per_frame_device(glsu_dpra *h, const void *d_img, int img_type, void *d_dphi);
+/* DPRA_CUDAF::update_ref_phi: phi_ref <- phi_curr, dphi_ref <- dphi. */
+int glsu_dpra_update_ref_phi(glsu_dpra *h);
+/* DPRA_CPU::operator() semantics for a block of frames: for frame i, run
+ * per_frame, store its dphi, update the reference when i % rr == 0
+ * (DPRA/dpra_cpu.cpp:58-89; the CUDA reference's overloads are empty,
+ * DPRA/dpra_cudaf.cu:193-205).  h_frames: nframes*W*H host frames;
+ * h_dphi_all: nframes*W*H host output. */
+int glsu_dpra_sequence(glsu_dpra *h, int nframes, const void *h_frames, int img_type, void *h_dphi_all,
+                       double *time_ms);
+/* Copy a state plane (GLSU_PHI_*) to the host. */
+int glsu_dpra_get(glsu_dpra *h, int which, void *h_out);
+/* Copy exp(j dphi) of the last frame's least-squares stage (W*H complex,
+ * the WFF2 input) to the host. */
+int glsu_dpra_get_lsq(glsu_dpra *h, void *h_out);
+/* Device address of a state plane (valid until the next call on h). */
+int glsu_dpra_device_ptr(glsu_dpra *h, int which, void **d_ptr);
+/* Record CUDA events between the stages of each frame (off by default). */
+int glsu_dpra_stage_timing(glsu_dpra *h, int enable);
+/* Device times (ms) of the stages of the last frame: [0] LS solve, [1] WFF
+ * row pass, [2] WFF column sweep, [3] WFF final row pass + phase update.
+ * Returns the number of stages written. */
+int glsu_dpra_stage_times(glsu_dpra *h, float *ms, int n);
+
+/* ---- AIA: AIA_CUDAF ----------------------------------------------------- */
+/* M frames of cols x rows pixels. */
+int glsu_aia_create(glsu_aia **out, int M, int cols, int rows);
+int glsu_aia_destroy(glsu_aia *h);
+int glsu_aia_set_stream(glsu_aia *h, void *cuda_stream);
+/* AIA_CUDAF::operator() (AIA/aia_cudaf.cu:308-401).  h_frames: M HOST
+ * pointers (img_type GLSU_U8 or GLSU_F32).  h_deltas holds n_deltas_in
+ * initial shifts; when n_deltas_in != M they are drawn with
+ * glsu_aia_random_deltas(M, seed).  On return h_deltas (M) holds the
+ * normalised shifts and h_phi (cols*rows) the wrapped phase. */
+int glsu_aia_run(glsu_aia *h, const void *const *h_frames, int img_type, float *h_phi, float *h_deltas,
+                 int n_deltas_in, double *time_ms, int *iters, float *err, int max_iter, float max_err,
+                 uint64_t seed);
+/* Same on M device frames stored back to back (M*cols*rows), enqueued on
+ * the stream; results stay on the device (d_phi, d_deltas) and *iters/*err
+ * are written after an internal synchronisation. */
+int glsu_aia_run_device(glsu_aia *h, const void *d_frames, int img_type, float *d_phi, float *h_deltas,
+                        int n_deltas_in, int *iters, float *err, int max_iter, float max_err,
+                        uint64_t seed);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GLSU_H */

@@ -1,0 +1,239 @@
+"""GPU parity tests: the CUDA path through the C ABI against the FP64 oracle.
+
+Tolerances (stated per test): the FP32 form must stay within 1e-3 rad of the
+FP64 oracle in phase, the FP64 form within 1e-10 rad.  Phase errors are
+measured on pixels whose filtered magnitude is not negligible (where the
+phase is defined)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+F32_PHASE_TOL = 1e-3
+F64_PHASE_TOL = 1e-10
+
+
+def _torch():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    return torch
+
+
+def wff_gpu(glsu, f, prec, params):
+    torch = _torch()
+    dt = np.complex64 if prec == "f32" else np.complex128
+    t = torch.from_numpy(np.ascontiguousarray(f, dt)).cuda()
+    out = torch.empty_like(t)
+    w = glsu.WFF2(f.shape[1], f.shape[0], prec, params)
+    ms = w.run(t.data_ptr(), out.data_ptr())
+    thr = w.threshold
+    w.close()
+    return out.cpu().numpy(), thr, ms
+
+
+def field(shape, seed, noise=0.1):
+    rng = np.random.default_rng(seed)
+    H, W = shape
+    y, x = np.mgrid[0:H, 0:W]
+    phi = 0.05 * x + 0.03 * y + 2.0 * np.sin(x / 17.0) * np.cos(y / 23.0)
+    return np.exp(1j * phi) * (1 + noise * rng.standard_normal(shape)) + noise * (
+        rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+
+
+def compare(out, ref, mask_frac=0.05):
+    mag = np.abs(ref)
+    m = mag > mask_frac * mag.max()
+    perr = np.abs(np.angle(out[m] * np.conj(ref[m]))).max()
+    rel = np.abs(out - ref).max() / mag.max()
+    return perr, rel
+
+
+WFF_CASES = [
+    # (shape, params: sigx, wxl, wxh, wxi, sigy, wyl, wyh, wyi, thr)
+    ((64, 80), (4.0, -1.0, 1.0, 0.25, 4.0, -1.0, 1.0, 0.25, 0.5)),         # half-size 12
+    ((37, 44), (3.0, -1.0, 1.0, 0.25, 4.0, -0.8, 0.8, 0.2, 0.5)),          # odd size, sigx != sigy
+    ((96, 130), (6.5, -0.9, 0.9, 0.3, 6.5, -0.9, 0.9, 0.3, 1.0)),          # half-size 20
+    ((128, 128), (10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)),       # the 21x21 sweep, half 30
+    ((140, 100), (15.0, -0.6, 0.6, 0.2, 15.0, -0.6, 0.6, 0.2, 0.3)),       # half-size 45
+    ((150, 170), (20.0, -0.15, 0.15, 0.05, 20.0, -0.15, 0.15, 0.05, 15)),  # DPRA defaults, half 60
+    ((64, 64), (4.0, 0.3, 0.3, 0.1, 4.0, -0.2, -0.2, 0.1, 0.3)),          # single frequency
+    ((72, 90), (5.0, -1.0, 1.0, 0.4, 5.0, -1.0, 1.0, 0.4, -1.0)),          # automatic threshold
+    ((5, 7), (2.0, -1.0, 1.0, 0.5, 2.0, -1.0, 1.0, 0.5, 0.1)),             # tiny image
+]
+
+
+@pytest.mark.parametrize("case", range(len(WFF_CASES)))
+def test_wff_f32_matches_oracle(glsu, oracle, case):
+    shape, p = WFF_CASES[case]
+    f = field(shape, case)
+    ref, rthr = oracle.wff2(f.astype(np.complex64).astype(np.complex128), *p)
+    out, thr, _ = wff_gpu(glsu, f, "f32", glsu.WffParams(*p))
+    perr, rel = compare(out, ref)
+    print("wff f32 case %d: phase err %.3g rad, rel err %.3g" % (case, perr, rel))
+    assert abs(thr - rthr) <= 1e-5 * rthr
+    assert perr < F32_PHASE_TOL and rel < 1e-4
+
+
+@pytest.mark.parametrize("case", [0, 1, 3, 5, 6, 7])
+def test_wff_f64_matches_oracle(glsu, oracle, case):
+    shape, p = WFF_CASES[case]
+    f = field(shape, case)
+    ref, rthr = oracle.wff2(f, *p)
+    out, thr, _ = wff_gpu(glsu, f, "f64", glsu.WffParams(*p))
+    perr, rel = compare(out, ref)
+    print("wff f64 case %d: phase err %.3g rad, rel err %.3g" % (case, perr, rel))
+    assert abs(thr - rthr) <= 1e-12 * rthr
+    assert perr < F64_PHASE_TOL and rel < 1e-11
+
+
+def test_wff_threshold_is_kept_after_first_call(glsu, oracle):
+    torch = _torch()
+    p = glsu.WffParams(4.0, -1, 1, 0.5, 4.0, -1, 1, 0.5, -1)
+    f1, f2 = field((40, 40), 1), 3 * field((40, 40), 2)
+    w = glsu.WFF2(40, 40, "f64", p)
+    a, b = torch.from_numpy(f1).cuda(), torch.from_numpy(f2).cuda()
+    out = torch.empty_like(a)
+    w.run(a.data_ptr(), out.data_ptr())
+    t1 = w.threshold
+    w.run(b.data_ptr(), out.data_ptr())
+    assert w.threshold == t1  # cached like the reference's m_rThr
+    ref, _ = oracle.wff2(f2, 4.0, -1, 1, 0.5, 4.0, -1, 1, 0.5, t1)
+    assert compare(out.cpu().numpy(), ref)[1] < 1e-11
+    w.close()
+
+
+@pytest.mark.parametrize("prec,r,img", [("f32", 1, "u8"), ("f32", 3, "f32"), ("f32", 4, "f32"),
+                                        ("f64", 2, "f32"), ("f64", 3, "f64"), ("f64", 1, "u8")])
+def test_dpra_least_squares_matches_oracle(glsu, oracle, synth, prec, r, img):
+    H, W = 61, 75
+    frames, phi0, _ = synth.sequence(H, W, 3, seed=r)
+    fr = frames[2]
+    if img == "u8":
+        fr = np.clip(np.round(fr * 255), 0, 255).astype(np.uint8)
+    elif img == "f64":
+        fr = fr.astype(np.float64)
+    phi_in = phi0.astype(np.float32 if prec == "f32" else np.float64)
+    d = glsu.DPRA(phi_in, 1, r, prec, glsu.WffParams(3.0, -0.5, 0.5, 0.5, 3.0, -0.5, 0.5, 0.5, 0.1))
+    d.per_frame(fr)
+    z = d.get_lsq()
+    zr = oracle.dpra_ls(fr.astype(np.float64), phi_in.astype(np.float64), r)
+    err = np.abs(np.angle(z * np.conj(zr)))
+    print("dpra LS %s r=%d %s: max %.3g rad, 99.9%% %.3g rad" % (prec, r, img, err.max(), np.quantile(err, 0.999)))
+    if prec == "f32":
+        assert np.quantile(err, 0.999) < 1e-3 and err.max() < 0.05
+    else:
+        assert err.max() < 1e-8
+    d.close()
+
+
+def run_sequence(glsu, frames, phi0, r, wp, prec, rr=1):
+    d = glsu.DPRA(phi0, rr, r, prec, wp)
+    pcs, dps = [], []
+    for i, fr in enumerate(frames):
+        dphi, _ = d.per_frame(fr)
+        pcs.append(d.get(glsu.PHI_CURR))
+        dps.append(dphi)
+        if i % rr == 0:
+            d.update_ref_phi()
+    d.close()
+    return np.stack(pcs), np.stack(dps)
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_glsu_sequence_256_matches_oracle(glsu, oracle, synth, prec):
+    """The FP64 reference path's workload: 256x256, DPRA 7x7, WFF2 sigma 10,
+    21x21 frequencies, threshold 0.2 (first 4 frames of the sequence)."""
+    frames, phi0, _ = synth.sequence(256, 256, 4, seed=0)
+    wp = glsu.WffParams(10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)
+    dt = np.float32 if prec == "f32" else np.float64
+    pcs, dps = run_sequence(glsu, frames.astype(dt), phi0.astype(dt), 3, wp, prec)
+    opc, odp = oracle.glsu_sequence(frames.astype(dt).astype(np.float64), phi0.astype(dt).astype(np.float64), 3,
+                                    oracle.WffParams(*wp.tuple()))
+    e_pc = np.abs(synth.phase_err(pcs, opc)).max()
+    e_dp = np.abs(dps - odp).max()
+    print("sequence %s: phi_curr max err %.3g rad, dphi max err %.3g rad" % (prec, e_pc, e_dp))
+    tol = F32_PHASE_TOL if prec == "f32" else F64_PHASE_TOL
+    assert e_pc < tol and e_dp < tol
+
+
+def test_reference_update_rate_semantics(glsu, oracle, synth):
+    frames, phi0, _ = synth.sequence(48, 40, 5, seed=9)
+    wp = glsu.WffParams(3.0, -0.5, 0.5, 0.25, 3.0, -0.5, 0.5, 0.25, 0.1)
+    d = glsu.DPRA(phi0, 2, 2, "f64", wp)
+    dps, _ = d.sequence(frames.astype(np.float64))
+    _, odp = oracle.glsu_sequence(frames.astype(np.float64), phi0, 2, oracle.WffParams(*wp.tuple()), rr=2)
+    assert np.abs(dps - odp).max() < F64_PHASE_TOL
+    d.close()
+
+
+def test_aia_reference_bmp_frames(glsu, oracle):
+    """AIA on the reference's own test frames Test/{1,2,3}.bmp with the
+    deltas of its tests (uint8 path, as AIA_CUDAF receives cv::Mat CV_8UC1)."""
+    import os
+    from conftest import GOLDEN
+    g = np.load(os.path.join(GOLDEN, "aia_bmp.npz"))
+    frames = g["frames"]
+    d0 = g["deltas0"]
+    a = glsu.AIA(3, 256, 256)
+    phi, d, ms, it, err = a.run(list(frames), d0, max_iter=20, max_err=1e-4)
+    ophi, od, oit, oerr = oracle.aia(frames.astype(np.float64), d0.astype(np.float64), 20, 1e-4)
+    e_phi = np.abs(np.angle(np.exp(1j * (phi - ophi)))).max()
+    print("aia bmp: iters %d/%d, delta err %.3g, phi err %.3g" % (it, oit, np.abs(d - od).max(), e_phi))
+    assert it == oit
+    assert np.abs(d - od).max() < 1e-4 and e_phi < 1e-3
+    a.close()
+
+
+def test_aia_synthetic_matches_oracle(glsu, oracle, synth):
+    frames, _, _ = synth.aia_frames(200, 180, 5, seed=4)
+    d0 = glsu.random_deltas(5, 11)
+    a = glsu.AIA(5, 180, 200)
+    phi, d, ms, it, err = a.run(list(frames), None, max_iter=30, max_err=1e-4, seed=11)
+    ophi, od, oit, oerr = oracle.aia(frames.astype(np.float64), d0.astype(np.float64), 30, 1e-4)
+    e_phi = np.abs(np.angle(np.exp(1j * (phi - ophi)))).max()
+    print("aia synthetic: iters %d/%d, delta err %.3g, phi err %.3g" % (it, oit, np.abs(d - od).max(), e_phi))
+    assert it == oit and np.abs(d - od).max() < 1e-4 and e_phi < 1e-3
+    a.close()
+
+
+def test_wff_phase_equivariance_full_size(glsu):
+    """Size-independent property at 1024x1024: WFF2(e^{ja} f) = e^{ja} WFF2(f)."""
+    torch = _torch()
+    f = field((1024, 1024), 3)
+    p = glsu.WffParams(10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)
+    a = torch.from_numpy(f.astype(np.complex64)).cuda()
+    b = a * np.exp(1j * 1.234)
+    oa, ob = torch.empty_like(a), torch.empty_like(a)
+    w = glsu.WFF2(1024, 1024, "f32", p)
+    w.run(a.data_ptr(), oa.data_ptr())
+    w.run(b.data_ptr(), ob.data_ptr())
+    oa = oa.cpu().numpy() * np.exp(1j * 1.234)
+    perr, rel = compare(ob.cpu().numpy(), oa)
+    assert perr < 1e-4 and rel < 1e-4
+    w.close()
+
+
+def test_glsu_frame_1024_matches_oracle(glsu, oracle, synth):
+    """One full-size frame (1024x1024, DPRA 7x7, 441 frequencies) against the oracle."""
+    frames, phi0, _ = synth.sequence(1024, 1024, 2, seed=1)
+    wp = glsu.WffParams(10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)
+    pcs, dps = run_sequence(glsu, frames[1:], phi0.astype(np.float32), 3, wp, "f32")
+    opc, odp, _, _ = oracle.glsu_frame(frames[1].astype(np.float64), phi0.astype(np.float32).astype(np.float64),
+                                       np.zeros((1024, 1024)), 3, oracle.WffParams(*wp.tuple()))
+    e_pc = np.abs(synth.phase_err(pcs[0], opc)).max()
+    rms = np.sqrt(np.mean(synth.phase_err(pcs[0], opc) ** 2))
+    print("1024 frame f32: max err %.3g rad, rms %.3g rad" % (e_pc, rms))
+    assert e_pc < F32_PHASE_TOL
+
+
+def test_error_codes_on_device(glsu):
+    with pytest.raises(glsu.GlsuError) as e:
+        glsu.WFF2(64, 64, "f32", glsu.WffParams(), wft_type=glsu.WFT_WFR)
+    assert e.value.code == glsu.ERR_UNSUPPORTED
+    with pytest.raises(glsu.GlsuError) as e:
+        glsu.WFF2(4090, 8, "f32", glsu.WffParams())
+    assert e.value.code == glsu.ERR_PADDING
+    d = glsu.DPRA(np.zeros((16, 16), np.float32), 1, 1, "f32", glsu.WffParams(2.0, -1, 1, 1, 2.0, -1, 1, 1, 0.1))
+    with pytest.raises((TypeError, glsu.GlsuError)):
+        d.per_frame(np.zeros((16, 16), np.int16))
+    d.close()
