@@ -1,0 +1,344 @@
+#!/usr/bin/env python
+"""G-LS3U benchmark: frames/s of the per-frame hot path at 1024x1024 FP32.
+
+A step is one frame of the plain G-LS3U path -- DPRA least squares (7x7
+window) -> WFF2 (sigma 10, 21x21 frequencies on [-1, 1], threshold 0.2) ->
+phase update -> reference update (rate 1) -- on a 1024x1024 frame of the
+seeded synthetic sequence generator (glsu/synth.py).  The sequence's initial
+phase comes from AIA on 5 phase-shifted frames (timed separately, reported
+under "aia").
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank runs its own sequence (weak scaling, no collective
+on the data path); the reported time is the max over ranks.
+``--impl reference`` times the reference's CPU algorithm (the FP64 oracle
+restatement of DPRA_CPU + WFT2_cpu; the reference's own MKL/FFTW/OpenCV/MSVC
+build cannot be compiled here) on the host cores, rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "g-ls3u_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "G-LS3U frames/s at 1024^2 FP32 (plain path: DPRA 7x7 + WFF2 21x21)"
+SIZE = 1024
+RADIUS = 3
+WFF = (10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)
+NFX = NFY = 21
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=SIZE)
+    ap.add_argument("--cpu-rows", type=int, default=8,
+                    help="frequency rows (of 21) in the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(size):
+    return {
+        "workload": "G-LS3U plain per-frame path, %dx%d FP32, DPRA %dx%d window, WFF2 sigma=%g, "
+                    "xi in [%g,%g] step %g (%dx%d frequencies), thr=%g, reference rate 1; 200-frame "
+                    "sequence generator with AIA (5 frames) initial phase"
+                    % (size, size, 2 * RADIUS + 1, 2 * RADIUS + 1, WFF[0], WFF[1], WFF[2], WFF[3], NFX, NFY,
+                       WFF[8]),
+        "frame": [size, size],
+        "dpra_window": 2 * RADIUS + 1,
+        "wff": {"sigma": WFF[0], "wl": WFF[1], "wh": WFF[2], "wi": WFF[3], "thr": WFF[8], "n_freq": NFX * NFY},
+        "l2": "flushed before every timed step (256 MiB device write outside the timed events)",
+    }
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.th = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.th.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def dist_init():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+    return rank, world, local
+
+
+def reduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(size, rows, seed=1000):
+    """Bounded CPU sample of the same frame with the oracle restatement of the
+    reference's CPU path: full DPRA LS + update, WFF2 over `rows` of the 21
+    frequency rows (extrapolated to 21).  Returns (frames_per_s, seconds, threads)."""
+    from oracle import oracle as O
+    from glsu import synth
+    O.build()
+    frames, phi0, _ = synth.sequence(size, size, 2, seed=seed)
+    img = frames[1].astype(np.float64)
+    threads = os.cpu_count() or 1
+    wp = O.WffParams(*WFF)
+    t0 = time.perf_counter()
+    z = O.dpra_ls(img, phi0, RADIUS, threads)
+    t1 = time.perf_counter()
+    filt, _ = O.wff2(z, *wp.tuple(), nthreads=threads, ky=(0, rows))
+    t2 = time.perf_counter()
+    O.dpra_update(filt, phi0, np.zeros_like(phi0))
+    t3 = time.perf_counter()
+    per_frame = (t1 - t0) + (t2 - t1) * NFY / rows + (t3 - t2)
+    return 1.0 / per_frame, t3 - t0, threads
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    steps, warm = args.steps, args.warmup
+    rows = 1
+    for _ in range(warm):
+        cpu_sample(args.size, rows)
+    tot, wall = 0.0, 0.0
+    vals = []
+    threads = os.cpu_count()
+    for _ in range(steps):
+        v, secs, threads = cpu_sample(args.size, rows)
+        vals.append(v)
+        tot += 1.0 / v
+        wall += secs
+    value = steps / tot
+    sample = ("per step: one %dx%d frame, DPRA LS + update in full, WFF2 over %d of 21 frequency rows "
+              "(%d frequencies) extrapolated to 441; FP64 oracle restatement of DPRA_CPU/WFT2_cpu, "
+              "%d OpenMP threads" % (args.size, args.size, rows, rows * NFX, threads))
+    return {
+        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": args.gpus, "steps": steps,
+        "warmup": warm, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(args.size),
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import glsu
+    from glsu import synth
+    if not torch.cuda.is_available():
+        raise RuntimeError("no CUDA device: the GB300 path has no CPU fallback")
+    torch.cuda.set_device(local)
+    size = args.size
+    N = size * size
+    wp = glsu.WffParams(*WFF)
+    seed = 1000 + rank
+    nfr = 8
+    frames, phi0, _ = synth.sequence(size, size, nfr, seed=seed)
+
+    # ---- AIA initial phase (5 frames, shifts U(0, 2pi), <= 30 iterations or 1e-4)
+    aframes, _, _ = synth.aia_frames(size, size, 5, seed=seed)
+    aia = glsu.AIA(5, size, size)
+    aia.run(list(aframes), None, max_iter=30, max_err=1e-4, seed=seed)  # warm
+    _, _, aia_ms, aia_iters, aia_err = aia.run(list(aframes), None, max_iter=30, max_err=1e-4, seed=seed)
+    aia.close()
+
+    stream = torch.cuda.Stream()
+    d = glsu.DPRA(phi0.astype(np.float32), 1, RADIUS, "f32", wp)
+    d.set_stream(stream.cuda_stream)
+    d.stage_timing(True)
+    dfr = torch.from_numpy(frames).cuda()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for k in range(args.warmup):
+        d.per_frame_device(dfr[k % nfr].data_ptr(), glsu.F32)
+        d.update_ref_phi()
+    torch.cuda.synchronize()
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stage = np.zeros(4)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        evs[k][0].record(stream)
+        d.per_frame_device(dfr[k % nfr].data_ptr(), glsu.F32)
+        d.update_ref_phi()
+        evs[k][1].record(stream)
+        stage += np.array(d.stage_times())  # synchronises the stream (outside the events)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(world)
+    dev_ms = sum(a.elapsed_time(b) for a, b in evs)
+    max_ms = reduce_max(dev_ms, world)
+    value = world * args.steps / (max_ms / 1e3)
+
+    # ---- end to end through the public API with pinned host buffers
+    hfr = torch.from_numpy(frames).pin_memory()
+    hout = torch.empty((size, size), dtype=torch.float32).pin_memory()
+    for k in range(2):
+        d.per_frame_ptr(hfr[k].data_ptr(), glsu.F32, hout.data_ptr())
+        d.update_ref_phi()
+    e2e_s = 0.0
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        stream.synchronize()
+        t0 = time.perf_counter()
+        d.per_frame_ptr(hfr[k % nfr].data_ptr(), glsu.F32, hout.data_ptr())
+        d.update_ref_phi()
+        e2e_s += time.perf_counter() - t0
+    e2e_s = reduce_max(e2e_s, world)
+    e2e = world * args.steps / e2e_s
+    d.close()
+
+    # ---- roofline of the dominant kernel (the WFF2 column sweep)
+    st = stage / args.steps  # ms: [LS, WFF rows, WFF column sweep, WFF final+update]
+    pitch = (size + 127) // 128 * 128
+    col_bytes = 2 * NFX * size * pitch * 8  # read R_i planes + write C_i planes (complex64)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
+    achieved = col_bytes / (st[2] * 1e-3) / 1e9
+    # FP32 work of the column sweep: 2 column filters of 2*sx+1 taps per
+    # frequency and output, complex data (2 FMA per tap), plus the halo rows.
+    sx = int(np.floor(3 * WFF[0] + 0.5))
+    col_fma = NFX * NFY * N * 2 * (2 * sx + 1) * 2
+    sm_mhz = clk.get("sm_mhz") or 1900.0
+    fp32_peak_tflops = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_tflops = 2 * col_fma / (st[2] * 1e-3) / 1e12
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(size),
+        "clocks": clk,
+        "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": 4 * N, "d2h_bytes_per_step": 4 * N},
+        "gpu_launches": 4 * args.steps,
+        "stages_ms": {"dpra_ls": st[0], "wff_rows": st[1], "wff_column_sweep": st[2], "wff_final_update": st[3]},
+        "roofline": {"kernel": "wff_cols_kernel (WFF2 column sweep)", "bound": "hbm", "achieved": achieved,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                     "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": col_bytes,
+                     "fp32_pipe": {"achieved_tflops": fp32_tflops, "peak_tflops_at_clock": fp32_peak_tflops,
+                                   "frac": fp32_tflops / fp32_peak_tflops}},
+        "aia": {"frames": 5, "ms": aia_ms, "iterations": aia_iters, "err": aia_err,
+                "ms_per_frame_over_200": aia_ms / 200},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        v, secs, threads = cpu_sample(size, args.cpu_rows)
+        out["cpu_baseline"] = {
+            "value": v, "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": "one %dx%d frame: DPRA LS + update in full, WFF2 over %d of 21 frequency rows extrapolated "
+                      "to 441 (%.1f s of CPU work); FP64 oracle restatement of DPRA_CPU/WFT2_cpu, %d OpenMP "
+                      "threads" % (size, size, args.cpu_rows, secs, threads)}
+    return out if rank == 0 else None
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_init()
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        res = run_ours(args, rank, world, local)
+    if rank == 0 and res is not None:
+        print(json.dumps(res))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

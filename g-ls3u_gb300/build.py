@@ -23,6 +23,7 @@ LIB = os.path.join(LIB_DIR, "libglsu.so")
 CPP_TEST_SRC = os.path.join(ROOT, "tests", "cpp", "test_classes.cpp")
 CPP_TEST_BIN = os.path.join(LIB_DIR, "glsu_cpp_test")
 NVCC = os.environ.get("NVCC", "nvcc")
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
 
@@ -76,8 +77,10 @@ def build(force: bool = False, jobs: int | None = None) -> str:
                 os.path.getmtime(LIB), os.path.getmtime(CPP_TEST_SRC), hdr_time):
             tmp = CPP_TEST_BIN + ".tmp"
             cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
-                   "-I", "/usr/local/cuda/include", CPP_TEST_SRC, "-o", tmp,
-                   "-L", LIB_DIR, "-lglsu", "-Wl,-rpath,$ORIGIN"]
+                   "-I", os.path.join(CUDA_HOME, "include"), CPP_TEST_SRC, "-o", tmp,
+                   "-L", LIB_DIR, "-lglsu", "-Wl,-rpath,$ORIGIN",
+                   "-L", os.path.join(CUDA_HOME, "lib64"), "-lcudart",
+                   "-Wl,-rpath," + os.path.join(CUDA_HOME, "lib64")]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError("C++ test driver build failed:\n%s\n%s" % (r.stdout, r.stderr))

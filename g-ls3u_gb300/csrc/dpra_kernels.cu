@@ -10,11 +10,18 @@
 // and dphi = atan2(-x3, x2); the kernel writes exp(j dphi).
 //
 // Numerics: x1 is eliminated (Schur complement) and the remaining 2x2 system
-// is formed from sums of values shifted by the centre pixel's c, s, I, which
-// removes the cancellation that makes the raw-sum normal matrix
-// ill-conditioned where phi_ref is locally flat.  The border quirk enters as
-// exact correction terms in rho = 1 - cnt/n0.  The shifted sums use Kahan
-// compensation in the FP32 form; the 2x2 solve runs in FP64 in both forms.
+// is formed from window sums of c, s, I shifted by reference values close to
+// the window mean, which removes the cancellation that makes the raw-sum
+// normal matrix ill-conditioned where phi_ref is locally smooth (for the
+// benchmark sequences the 3x3 condition number reaches 1e6-1e10).  The border
+// quirk enters as exact correction terms in rho = 1 - cnt/n0.  Because the
+// reduced 2x2 system itself has det/trace^2 ~ 1e-3 on most pixels, the sums
+// are formed in FP64 in both forms:
+//   FP32 form: c, s in FP64 from the FP32 phase; shift = the tile centre's
+//              values, so the sums stay separable (a horizontal then a
+//              vertical box pass over FP64 products in shared memory);
+//   FP64 form: shift = each pixel's own values (non-separable direct sums),
+//              the same evaluation the FP64 oracle uses.
 // exp(j dphi) is (X, -Y)/hypot(X, Y) with X ~ x2, Y ~ x3 -- the same value
 // as cos/sin of the atan2 without evaluating either.
 #include <cmath>
@@ -25,77 +32,22 @@ namespace glsu {
 
 constexpr int kDpraTX = 32, kDpraTY = 16;  // outputs per CTA (512 threads)
 
-template <typename T> struct Kahan {
-    T s = 0, c = 0;
-    __device__ __forceinline__ void add(T v)
-    {
-        const T y = v - c;
-        const T t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
-};
-
 template <typename T> __device__ __forceinline__ void sincos_t(T a, T *s, T *c);
 template <> __device__ __forceinline__ void sincos_t<float>(float a, float *s, float *c) { sincosf(a, s, c); }
 template <> __device__ __forceinline__ void sincos_t<double>(double a, double *s, double *c) { sincos(a, s, c); }
 
-template <typename IMG> __device__ __forceinline__ double load_img(const IMG *p, size_t i) { return (double)p[i]; }
-
-template <typename T, typename IMG, int R>
-__global__ void __launch_bounds__(kDpraTX *kDpraTY)
-    dpra_ls_kernel(const IMG *__restrict__ img, const T *__restrict__ phiref, C2<T> *__restrict__ z, int W, int H)
+// Shared tail: Schur-complement solve from sums shifted by (mc, ms, mi).
+template <typename T>
+__device__ __forceinline__ C2<T> dpra_solve(double Pc, double Ps, double Pi, double Pcc, double Pss, double Pcs,
+                                            double Pic, double Pis, double mc, double ms, double mi, double cnt,
+                                            double n0)
 {
-    constexpr int SW = kDpraTX + 2 * R, SH = kDpraTY + 2 * R;
-    __shared__ T sc[SH][SW + 1], ss[SH][SW + 1], si[SH][SW + 1];
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kDpraTX + tx;
-    const int x0 = blockIdx.x * kDpraTX, y0 = blockIdx.y * kDpraTY;
-    for (int e = tid; e < SW * SH; e += kDpraTX * kDpraTY) {
-        const int r = e / SW, c = e - r * SW;
-        const int gy = y0 - R + r, gx = x0 - R + c;
-        T cv = 0, sv = 0, iv = 0;
-        if (gy >= 0 && gy < H && gx >= 0 && gx < W) {
-            const size_t id = (size_t)gy * W + gx;
-            sincos_t<T>(phiref[id], &sv, &cv);
-            iv = (T)img[id];
-        }
-        sc[r][c] = cv;
-        ss[r][c] = sv;
-        si[r][c] = iv;
-    }
-    __syncthreads();
-    const int gx = x0 + tx, gy = y0 + ty;
-    if (gx >= W || gy >= H) return;
-
-    const int m0 = max(gy - R, 0), m1 = min(gy + R, H - 1);
-    const int n0 = max(gx - R, 0), n1 = min(gx + R, W - 1);
-    const T mc = sc[ty + R][tx + R], ms = ss[ty + R][tx + R], mi = si[ty + R][tx + R];
-    Kahan<T> pc, ps, pi, pcc, pss, pcs, pic, pis;
-    for (int m = m0; m <= m1; m++) {
-        const int r = m - y0 + R;
-        for (int n = n0; n <= n1; n++) {
-            const int c = n - x0 + R;
-            const T dc = sc[r][c] - mc, ds = ss[r][c] - ms, di = si[r][c] - mi;
-            pc.add(dc);
-            ps.add(ds);
-            pi.add(di);
-            pcc.add(dc * dc);
-            pss.add(ds * ds);
-            pcs.add(dc * ds);
-            pic.add(di * dc);
-            pis.add(di * ds);
-        }
-    }
-    const double cnt = (double)((m1 - m0 + 1) * (n1 - n0 + 1));
-    const double n0d = (double)((2 * R + 1) * (2 * R + 1));
-    const double rho = 1.0 - cnt / n0d;
-    const double Pc = pc.s, Ps = ps.s, Pi = pi.s;
-    const double Mc = mc, Ms = ms, Mi = mi;
-    const double a = (double)pcc.s - Pc * Pc / n0d + rho * (2 * Mc * Pc + cnt * Mc * Mc);
-    const double d = (double)pss.s - Ps * Ps / n0d + rho * (2 * Ms * Ps + cnt * Ms * Ms);
-    const double b = (double)pcs.s - Pc * Ps / n0d + rho * (Mc * Ps + Ms * Pc + cnt * Mc * Ms);
-    const double p = (double)pic.s - Pi * Pc / n0d + rho * (Mi * Pc + Mc * Pi + cnt * Mi * Mc);
-    const double q = (double)pis.s - Pi * Ps / n0d + rho * (Mi * Ps + Ms * Pi + cnt * Mi * Ms);
+    const double rho = 1.0 - cnt / n0;
+    const double a = Pcc - Pc * Pc / n0 + rho * (2 * mc * Pc + cnt * mc * mc);
+    const double d = Pss - Ps * Ps / n0 + rho * (2 * ms * Ps + cnt * ms * ms);
+    const double b = Pcs - Pc * Ps / n0 + rho * (mc * Ps + ms * Pc + cnt * mc * ms);
+    const double p = Pic - Pi * Pc / n0 + rho * (mi * Pc + mc * Pi + cnt * mi * mc);
+    const double q = Pis - Pi * Ps / n0 + rho * (mi * Ps + ms * Pi + cnt * mi * ms);
     double X = d * p - b * q;  // x2 * det
     double Y = a * q - b * p;  // x3 * det
     if (a * d - b * b < 0) {
@@ -111,42 +63,186 @@ __global__ void __launch_bounds__(kDpraTX *kDpraTY)
         out.x = 1;
         out.y = 0;
     }
-    z[(size_t)gy * W + gx] = out;
+    return out;
 }
 
-template <typename T, typename IMG>
-static int launch_ls_t(const void *d_img, const void *d_phiref, void *d_z, int W, int H, int r, cudaStream_t s)
+// FP32 form: FP64 products of tile-shifted values, separable box sums.
+template <typename IMG, int R> struct SepGeom {
+    static constexpr int SW = kDpraTX + 2 * R, SH = kDpraTY + 2 * R;
+    static constexpr size_t SMEM = sizeof(double) * 8 * ((size_t)SH * SW + (size_t)SH * kDpraTX);
+};
+
+template <typename IMG, int R>
+__global__ void __launch_bounds__(kDpraTX *kDpraTY)
+    dpra_ls_sep_kernel(const IMG *__restrict__ img, const float *__restrict__ phiref, float2 *__restrict__ z, int W,
+                       int H)
 {
-    dim3 blk(kDpraTX, kDpraTY), grd((W + kDpraTX - 1) / kDpraTX, (H + kDpraTY - 1) / kDpraTY);
-    const IMG *im = (const IMG *)d_img;
-    const T *ph = (const T *)d_phiref;
-    C2<T> *zz = (C2<T> *)d_z;
-    switch (r) {
-    case 1: dpra_ls_kernel<T, IMG, 1><<<grd, blk, 0, s>>>(im, ph, zz, W, H); break;
-    case 2: dpra_ls_kernel<T, IMG, 2><<<grd, blk, 0, s>>>(im, ph, zz, W, H); break;
-    case 3: dpra_ls_kernel<T, IMG, 3><<<grd, blk, 0, s>>>(im, ph, zz, W, H); break;
-    case 4: dpra_ls_kernel<T, IMG, 4><<<grd, blk, 0, s>>>(im, ph, zz, W, H); break;
-    case 5: dpra_ls_kernel<T, IMG, 5><<<grd, blk, 0, s>>>(im, ph, zz, W, H); break;
-    case 6: dpra_ls_kernel<T, IMG, 6><<<grd, blk, 0, s>>>(im, ph, zz, W, H); break;
-    case 7: dpra_ls_kernel<T, IMG, 7><<<grd, blk, 0, s>>>(im, ph, zz, W, H); break;
-    case 8: dpra_ls_kernel<T, IMG, 8><<<grd, blk, 0, s>>>(im, ph, zz, W, H); break;
-    default: return fail(GLSU_ERR_UNSUPPORTED, "DPRA window radius must be 1..8");
+    using G = SepGeom<IMG, R>;
+    constexpr int SW = G::SW, SH = G::SH, NE = SH * SW, NH = SH * kDpraTX;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *v = reinterpret_cast<double *>(smem_raw);  // [8][SH][SW]
+    double *hs = v + 8 * NE;                           // [8][SH][32]
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kDpraTX + tx;
+    const int x0 = blockIdx.x * kDpraTX, y0 = blockIdx.y * kDpraTY;
+    // shift: the values at the tile centre (clamped into the image)
+    const size_t cid = (size_t)min(y0 + kDpraTY / 2, H - 1) * W + min(x0 + kDpraTX / 2, W - 1);
+    double mc, ms;
+    sincos((double)phiref[cid], &ms, &mc);
+    const double mi = (double)img[cid];
+    for (int e = tid; e < NE; e += kDpraTX * kDpraTY) {
+        const int r = e / SW, c = e - r * SW;
+        const int gy = y0 - R + r, gx = x0 - R + c;
+        double dc = 0, ds = 0, di = 0;
+        if (gy >= 0 && gy < H && gx >= 0 && gx < W) {
+            const size_t id = (size_t)gy * W + gx;
+            double sv, cv;
+            sincos((double)phiref[id], &sv, &cv);
+            dc = cv - mc;
+            ds = sv - ms;
+            di = (double)img[id] - mi;
+        }
+        v[0 * NE + e] = dc;
+        v[1 * NE + e] = ds;
+        v[2 * NE + e] = di;
+        v[3 * NE + e] = dc * dc;
+        v[4 * NE + e] = ds * ds;
+        v[5 * NE + e] = dc * ds;
+        v[6 * NE + e] = di * dc;
+        v[7 * NE + e] = di * ds;
     }
+    __syncthreads();
+    for (int e = tid; e < 8 * NH; e += kDpraTX * kDpraTY) {
+        const int k = e / NH, rem = e - k * NH, r = rem / kDpraTX, c = rem - r * kDpraTX;
+        const double *src = v + k * NE + r * SW + c;
+        double acc = 0;
+#pragma unroll
+        for (int dx = 0; dx <= 2 * R; dx++) acc += src[dx];
+        hs[e] = acc;
+    }
+    __syncthreads();
+    const int gx = x0 + tx, gy = y0 + ty;
+    if (gx >= W || gy >= H) return;
+    double P[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const double *src = hs + k * NH + ty * kDpraTX + tx;
+        double acc = 0;
+#pragma unroll
+        for (int dy = 0; dy <= 2 * R; dy++) acc += src[dy * kDpraTX];
+        P[k] = acc;
+    }
+    const int m0 = max(gy - R, 0), m1 = min(gy + R, H - 1);
+    const int n0 = max(gx - R, 0), n1 = min(gx + R, W - 1);
+    const double cnt = (double)((m1 - m0 + 1) * (n1 - n0 + 1));
+    z[(size_t)gy * W + gx] = dpra_solve<float>(P[0], P[1], P[2], P[3], P[4], P[5], P[6], P[7], mc, ms, mi, cnt,
+                                               (double)((2 * R + 1) * (2 * R + 1)));
+}
+
+// FP64 form: sums shifted by each pixel's own values (direct, non-separable).
+template <typename IMG, int R>
+__global__ void __launch_bounds__(kDpraTX *kDpraTY)
+    dpra_ls_f64_kernel(const IMG *__restrict__ img, const double *__restrict__ phiref, double2 *__restrict__ z,
+                       int W, int H)
+{
+    constexpr int SW = kDpraTX + 2 * R, SH = kDpraTY + 2 * R;
+    __shared__ double sc[SH][SW + 1], ss[SH][SW + 1], si[SH][SW + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kDpraTX + tx;
+    const int x0 = blockIdx.x * kDpraTX, y0 = blockIdx.y * kDpraTY;
+    for (int e = tid; e < SW * SH; e += kDpraTX * kDpraTY) {
+        const int r = e / SW, c = e - r * SW;
+        const int gy = y0 - R + r, gx = x0 - R + c;
+        double cv = 0, sv = 0, iv = 0;
+        if (gy >= 0 && gy < H && gx >= 0 && gx < W) {
+            const size_t id = (size_t)gy * W + gx;
+            sincos(phiref[id], &sv, &cv);
+            iv = (double)img[id];
+        }
+        sc[r][c] = cv;
+        ss[r][c] = sv;
+        si[r][c] = iv;
+    }
+    __syncthreads();
+    const int gx = x0 + tx, gy = y0 + ty;
+    if (gx >= W || gy >= H) return;
+    const int m0 = max(gy - R, 0), m1 = min(gy + R, H - 1);
+    const int n0 = max(gx - R, 0), n1 = min(gx + R, W - 1);
+    const double mc = sc[ty + R][tx + R], ms = ss[ty + R][tx + R], mi = si[ty + R][tx + R];
+    double pc = 0, ps = 0, pi = 0, pcc = 0, pss = 0, pcs = 0, pic = 0, pis = 0;
+    for (int m = m0; m <= m1; m++) {
+        const int r = m - y0 + R;
+        for (int n = n0; n <= n1; n++) {
+            const int c = n - x0 + R;
+            const double dc = sc[r][c] - mc, ds = ss[r][c] - ms, di = si[r][c] - mi;
+            pc += dc;
+            ps += ds;
+            pi += di;
+            pcc += dc * dc;
+            pss += ds * ds;
+            pcs += dc * ds;
+            pic += di * dc;
+            pis += di * ds;
+        }
+    }
+    const double cnt = (double)((m1 - m0 + 1) * (n1 - n0 + 1));
+    z[(size_t)gy * W + gx] =
+        dpra_solve<double>(pc, ps, pi, pcc, pss, pcs, pic, pis, mc, ms, mi, cnt, (double)((2 * R + 1) * (2 * R + 1)));
+}
+
+template <typename IMG, int R>
+static int launch_sep(const void *d_img, const void *d_phiref, void *d_z, int W, int H, cudaStream_t s)
+{
+    using G = SepGeom<IMG, R>;
+    static bool attr = false;
+    if (!attr) {
+        GLSU_CUDA_TRY(cudaFuncSetAttribute(dpra_ls_sep_kernel<IMG, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)G::SMEM));
+        attr = true;
+    }
+    dim3 blk(kDpraTX, kDpraTY), grd((W + kDpraTX - 1) / kDpraTX, (H + kDpraTY - 1) / kDpraTY);
+    dpra_ls_sep_kernel<IMG, R><<<grd, blk, G::SMEM, s>>>((const IMG *)d_img, (const float *)d_phiref, (float2 *)d_z,
+                                                         W, H);
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
+}
+
+template <typename IMG, int R>
+static int launch_f64(const void *d_img, const void *d_phiref, void *d_z, int W, int H, cudaStream_t s)
+{
+    dim3 blk(kDpraTX, kDpraTY), grd((W + kDpraTX - 1) / kDpraTX, (H + kDpraTY - 1) / kDpraTY);
+    dpra_ls_f64_kernel<IMG, R><<<grd, blk, 0, s>>>((const IMG *)d_img, (const double *)d_phiref, (double2 *)d_z,
+                                                   W, H);
+    GLSU_CUDA_TRY(cudaGetLastError());
+    return GLSU_OK;
+}
+
+template <typename IMG>
+static int launch_ls_t(int prec, const void *d_img, const void *d_phiref, void *d_z, int W, int H, int r,
+                       cudaStream_t s)
+{
+#define GLSU_LS_CASE(RR)                                                                         \
+    case RR:                                                                                     \
+        return prec == GLSU_F32 ? launch_sep<IMG, RR>(d_img, d_phiref, d_z, W, H, s)             \
+                                : launch_f64<IMG, RR>(d_img, d_phiref, d_z, W, H, s);
+    switch (r) {
+        GLSU_LS_CASE(1)
+        GLSU_LS_CASE(2)
+        GLSU_LS_CASE(3)
+        GLSU_LS_CASE(4)
+        GLSU_LS_CASE(5)
+        GLSU_LS_CASE(6)
+        GLSU_LS_CASE(7)
+        GLSU_LS_CASE(8)
+    default: return fail(GLSU_ERR_UNSUPPORTED, "DPRA window radius must be 1..8");
+    }
+#undef GLSU_LS_CASE
 }
 
 int launch_dpra_ls(int prec, int img_type, const void *d_img, const void *d_phiref, void *d_z, int W, int H, int r,
                    cudaStream_t s)
 {
-    if (prec == GLSU_F32) {
-        if (img_type == GLSU_U8) return launch_ls_t<float, uint8_t>(d_img, d_phiref, d_z, W, H, r, s);
-        if (img_type == GLSU_F32) return launch_ls_t<float, float>(d_img, d_phiref, d_z, W, H, r, s);
-    } else {
-        if (img_type == GLSU_U8) return launch_ls_t<double, uint8_t>(d_img, d_phiref, d_z, W, H, r, s);
-        if (img_type == GLSU_F32) return launch_ls_t<double, float>(d_img, d_phiref, d_z, W, H, r, s);
-        if (img_type == GLSU_F64) return launch_ls_t<double, double>(d_img, d_phiref, d_z, W, H, r, s);
-    }
+    if (img_type == GLSU_U8) return launch_ls_t<uint8_t>(prec, d_img, d_phiref, d_z, W, H, r, s);
+    if (img_type == GLSU_F32) return launch_ls_t<float>(prec, d_img, d_phiref, d_z, W, H, r, s);
+    if (img_type == GLSU_F64 && prec == GLSU_F64) return launch_ls_t<double>(prec, d_img, d_phiref, d_z, W, H, r, s);
     return fail(GLSU_ERR_INVALID, "unsupported frame type for this precision");
 }
 

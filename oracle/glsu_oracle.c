@@ -17,6 +17,9 @@
  *
  * Documented deviations (all FP64 throughout):
  *   - DPRA/dpra_cpu.cpp:246 truncates atan2 of the filtered value to float; here it stays double.
+ *   - The DPRA normal equations are solved through the Schur complement
+ *     with centre-shifted window sums (or_dpra_ls); the literal raw-sum form
+ *     is kept as or_dpra_ls_raw.  See the comment above or_dpra_ls.
  *   - LAPACKE_dsysv (Bunch-Kaufman) is replaced by Gaussian elimination with
  *     partial pivoting and LAPACKE_dposv by a Cholesky solve; both give the
  *     same solution up to rounding for the matrices that arise.
@@ -504,8 +507,23 @@ static int chol3_solve(const double A[3][3], double *B, int nrhs)
  * img:    H*W intensities (double).
  * phiref: H*W reference phase.
  * z:      H*W complex output exp(j dphi).
+ *
+ * or_dpra_ls_raw follows DPRA/dpra_cpu.cpp:169-229 literally: raw window
+ * sums, the 3x3 system with A00 = (2r+1)^2, a pivoted solve.
+ *
+ * or_dpra_ls solves the same normal equations in a numerically stable way:
+ * x1 is eliminated (Schur complement) and the 2x2 system for (x2, x3) is
+ * built from window sums of c, s, I shifted by the centre pixel's values.
+ * In exact arithmetic both give the same dphi.  Where phi_ref is locally
+ * smooth the 3x3 raw-sum matrix has a condition number of 1e6-1e10 and the
+ * literal form loses that many digits (up to ~1e-3 rad at FP64 on the
+ * benchmark sequences); the shifted form does not, so it is the parity
+ * reference for the FP64 bar.  With rho = 1 - cnt/n0 (cnt = pixels inside
+ * the clipped window, n0 = (2r+1)^2) and P* the shifted sums:
+ *   a = Pcc - Pc^2/n0 + rho (2 mc Pc + cnt mc^2)      (and d, b, p, q alike)
+ *   x2 ~ d p - b q,  x3 ~ a q - b p,  dphi = atan2(-x3, x2)
  */
-void or_dpra_ls(int W, int H, int r, const double *img, const double *phiref, double *z, int nthreads)
+void or_dpra_ls_raw(int W, int H, int r, const double *img, const double *phiref, double *z, int nthreads)
 {
     const double a00 = (double)((2 * r + 1) * (2 * r + 1));
 #ifdef _OPENMP
@@ -531,6 +549,43 @@ void or_dpra_ls(int W, int H, int r, const double *img, const double *phiref, do
             size_t id = (size_t)i * W + j;
             z[2 * id] = cos(d);
             z[2 * id + 1] = sin(d);
+        }
+    }
+}
+
+void or_dpra_ls(int W, int H, int r, const double *img, const double *phiref, double *z, int nthreads)
+{
+    const double n0 = (double)((2 * r + 1) * (2 * r + 1));
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(static)
+#endif
+    for (int i = 0; i < H; i++) {
+        for (int j = 0; j < W; j++) {
+            const size_t id = (size_t)i * W + j;
+            const double mc = cos(phiref[id]), ms = sin(phiref[id]), mi = img[id];
+            double pc = 0, ps = 0, pi = 0, pcc = 0, pss = 0, pcs = 0, pic = 0, pis = 0;
+            int m0 = i - r < 0 ? 0 : i - r, m1 = i + r > H - 1 ? H - 1 : i + r;
+            int n0i = j - r < 0 ? 0 : j - r, n1 = j + r > W - 1 ? W - 1 : j + r;
+            for (int m = m0; m <= m1; m++)
+                for (int n = n0i; n <= n1; n++) {
+                    size_t q = (size_t)m * W + n;
+                    double dc = cos(phiref[q]) - mc, ds = sin(phiref[q]) - ms, di = img[q] - mi;
+                    pc += dc; ps += ds; pi += di;
+                    pcc += dc * dc; pss += ds * ds; pcs += dc * ds; pic += di * dc; pis += di * ds;
+                }
+            const double cnt = (double)((m1 - m0 + 1) * (n1 - n0i + 1));
+            const double rho = 1.0 - cnt / n0;
+            const double a = pcc - pc * pc / n0 + rho * (2 * mc * pc + cnt * mc * mc);
+            const double d = pss - ps * ps / n0 + rho * (2 * ms * ps + cnt * ms * ms);
+            const double b = pcs - pc * ps / n0 + rho * (mc * ps + ms * pc + cnt * mc * ms);
+            const double p = pic - pi * pc / n0 + rho * (mi * pc + mc * pi + cnt * mi * mc);
+            const double q = pis - pi * ps / n0 + rho * (mi * ps + ms * pi + cnt * mi * ms);
+            double X = d * p - b * q, Y = a * q - b * p;
+            if (a * d - b * b < 0) { X = -X; Y = -Y; }
+            const double h = hypot(X, Y);
+            z[2 * id] = h > 0 ? X / h : 1.0;
+            z[2 * id + 1] = h > 0 ? -Y / h : 0.0;
         }
     }
 }

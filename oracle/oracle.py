@@ -58,6 +58,7 @@ def lib():
                                   c_double, c_double, c_double, c_double, c_double, dp, dp,
                                   c_int, c_int, c_int]
             L.or_dpra_ls.argtypes = [c_int, c_int, c_int, dp, dp, dp, c_int]
+            L.or_dpra_ls_raw.argtypes = [c_int, c_int, c_int, dp, dp, dp, c_int]
             L.or_dpra_update.argtypes = [c_int, dp, dp, dp, dp, dp]
             L.or_aia_phi_solve.argtypes = [c_int, c_int, dp, dp, dp, dp]
             L.or_aia.argtypes = [c_int, c_int, dp, dp, c_int, c_double, dp, ip, dp]
@@ -137,12 +138,38 @@ def wff2(f, sigx, wxl, wxh, wxi, sigy, wyl, wyh, wyi, thr, nthreads=0, ky=None):
     return out, thr_used.value
 
 
-def dpra_ls(img, phiref, r=1, nthreads=0):
+def dpra_ls(img, phiref, r=1, nthreads=0, raw=False):
+    """exp(j dphi) of DPRA's windowed least squares.  raw=True: the literal
+    raw-sum 3x3 form of DPRA/dpra_cpu.cpp; default: the same normal
+    equations solved through the centre-shifted Schur complement."""
     img = _f64(img); phiref = _f64(phiref)
     H, W = img.shape
     z = np.zeros((H, W), np.complex128)
-    lib().or_dpra_ls(W, H, int(r), _dp(img), _dp(phiref), _dp(z.view(np.float64)), int(nthreads))
+    fn = lib().or_dpra_ls_raw if raw else lib().or_dpra_ls
+    fn(W, H, int(r), _dp(img), _dp(phiref), _dp(z.view(np.float64)), int(nthreads))
     return z
+
+
+def dpra_kappa(phiref, r=1):
+    """Conditioning of DPRA's reduced 2x2 normal matrix per pixel:
+    det / trace^2 of [[a, b], [b, d]] (<= 1/4; small = ill-conditioned)."""
+    phi = np.asarray(phiref, np.float64)
+    H, W = phi.shape
+    c, s = np.cos(phi), np.sin(phi)
+    n0 = (2 * r + 1) ** 2
+    ones = np.ones((H, W))
+    sums = {}
+    for name, v in (("c", c), ("s", s), ("cc", c * c), ("ss", s * s), ("cs", c * s), ("n", ones)):
+        p = np.pad(v, r)
+        acc = np.zeros((H, W))
+        for dy in range(2 * r + 1):
+            for dx in range(2 * r + 1):
+                acc += p[dy:dy + H, dx:dx + W]
+        sums[name] = acc
+    a = sums["cc"] - sums["c"] ** 2 / n0
+    d = sums["ss"] - sums["s"] ** 2 / n0
+    b = sums["cs"] - sums["c"] * sums["s"] / n0
+    return (a * d - b * b) / np.maximum((a + d) ** 2, 1e-300)
 
 
 def dpra_update(filtered, phiref, dphiref):

@@ -91,3 +91,11 @@ def test_no_silent_cpu_path_without_a_device(glsu):
     with pytest.raises(glsu.GlsuError) as e:
         glsu.WFF2(64, 64, "f32", glsu.WffParams())
     assert e.value.code == glsu.ERR_NO_DEVICE
+
+
+def test_frequency_count_float_and_double_can_differ(glsu):
+    """The reference counts frequencies in the class's precision, so the same
+    grid can hold a different number of frequencies in WFT2_CUDAF (float)
+    and WFT2_cpu / WFT2_CUDA (double): int(1.8 * (1/0.3)) + 1."""
+    assert glsu.wff_count(-0.9, 0.9, 0.3, glsu.F64) == 7
+    assert glsu.wff_count(-0.9, 0.9, 0.3, glsu.F32) == 6

@@ -52,7 +52,7 @@ WFF_CASES = [
     # (shape, params: sigx, wxl, wxh, wxi, sigy, wyl, wyh, wyi, thr)
     ((64, 80), (4.0, -1.0, 1.0, 0.25, 4.0, -1.0, 1.0, 0.25, 0.5)),         # half-size 12
     ((37, 44), (3.0, -1.0, 1.0, 0.25, 4.0, -0.8, 0.8, 0.2, 0.5)),          # odd size, sigx != sigy
-    ((96, 130), (6.5, -0.9, 0.9, 0.3, 6.5, -0.9, 0.9, 0.3, 1.0)),          # half-size 20
+    ((96, 130), (6.5, -0.8, 0.8, 0.4, 6.5, -0.8, 0.8, 0.4, 1.0)),          # half-size 20
     ((128, 128), (10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)),       # the 21x21 sweep, half 30
     ((140, 100), (15.0, -0.6, 0.6, 0.2, 15.0, -0.6, 0.6, 0.2, 0.3)),       # half-size 45
     ((150, 170), (20.0, -0.15, 0.15, 0.05, 20.0, -0.15, 0.15, 0.05, 15)),  # DPRA defaults, half 60
@@ -118,52 +118,73 @@ def test_dpra_least_squares_matches_oracle(glsu, oracle, synth, prec, r, img):
     z = d.get_lsq()
     zr = oracle.dpra_ls(fr.astype(np.float64), phi_in.astype(np.float64), r)
     err = np.abs(np.angle(z * np.conj(zr)))
-    print("dpra LS %s r=%d %s: max %.3g rad, 99.9%% %.3g rad" % (prec, r, img, err.max(), np.quantile(err, 0.999)))
+    kap = oracle.dpra_kappa(phi_in.astype(np.float64), r)
+    print("dpra LS %s r=%d %s: max %.3g rad, rms %.3g, min kappa %.2g" % (prec, r, img, err.max(),
+                                                                         np.sqrt(np.mean(err ** 2)), kap.min()))
     if prec == "f32":
-        assert np.quantile(err, 0.999) < 1e-3 and err.max() < 0.05
+        assert err.max() < 1e-4  # FP32 output rounding; the sums and the solve run in FP64
     else:
-        assert err.max() < 1e-8
+        assert err.max() < 1e-10
     d.close()
 
 
-def run_sequence(glsu, frames, phi0, r, wp, prec, rr=1):
-    d = glsu.DPRA(phi0, rr, r, prec, wp)
-    pcs, dps = [], []
+MASK_MAG = 0.1  # phase compared where |filtered| >= 0.1 (unit-modulus input; median ~0.9)
+
+
+def teacher_forced(glsu, oracle, frames, phi0, r, wp, prec, rr=1):
+    """Run the GPU sequence and, for every frame, the oracle on the GPU's own
+    reference state (teacher forcing).  Returns per-frame error stats."""
+    dt = np.float32 if prec == "f32" else np.float64
+    d = glsu.DPRA(phi0.astype(dt), rr, r, prec, wp)
+    stats = []
     for i, fr in enumerate(frames):
+        pref = d.get(glsu.PHI_REF).astype(np.float64)
+        dref = d.get(glsu.DPHI_REF).astype(np.float64)
         dphi, _ = d.per_frame(fr)
-        pcs.append(d.get(glsu.PHI_CURR))
-        dps.append(dphi)
+        pc = d.get(glsu.PHI_CURR)
+        opc, odp, _, ofilt = oracle.glsu_frame(fr.astype(np.float64), pref, dref, r, oracle.WffParams(*wp.tuple()))
+        m = np.abs(ofilt) >= MASK_MAG
+        e_pc = np.abs(np.angle(np.exp(1j * (pc.astype(np.float64) - opc))))
+        e_dp = np.abs(dphi.astype(np.float64) - odp)
+        stats.append({"frame": i, "kept": m.mean(), "pc_max": e_pc[m].max(), "dp_max": e_dp[m].max(),
+                      "pc_rms_all": np.sqrt(np.mean(e_pc ** 2)), "pc_max_all": e_pc.max()})
         if i % rr == 0:
             d.update_ref_phi()
     d.close()
-    return np.stack(pcs), np.stack(dps)
+    return stats
 
 
 @pytest.mark.parametrize("prec", ["f64", "f32"])
 def test_glsu_sequence_256_matches_oracle(glsu, oracle, synth, prec):
     """The FP64 reference path's workload: 256x256, DPRA 7x7, WFF2 sigma 10,
-    21x21 frequencies, threshold 0.2 (first 4 frames of the sequence)."""
+    21x21 frequencies, threshold 0.2; first 4 frames, teacher-forced."""
     frames, phi0, _ = synth.sequence(256, 256, 4, seed=0)
     wp = glsu.WffParams(10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)
     dt = np.float32 if prec == "f32" else np.float64
-    pcs, dps = run_sequence(glsu, frames.astype(dt), phi0.astype(dt), 3, wp, prec)
-    opc, odp = oracle.glsu_sequence(frames.astype(dt).astype(np.float64), phi0.astype(dt).astype(np.float64), 3,
-                                    oracle.WffParams(*wp.tuple()))
-    e_pc = np.abs(synth.phase_err(pcs, opc)).max()
-    e_dp = np.abs(dps - odp).max()
-    print("sequence %s: phi_curr max err %.3g rad, dphi max err %.3g rad" % (prec, e_pc, e_dp))
+    st = teacher_forced(glsu, oracle, frames.astype(dt), phi0, 3, wp, prec)
+    for s_ in st:
+        print("sequence %s frame %d: kept %.4f, phi max %.3g, dphi max %.3g, phi rms(all) %.3g, max(all) %.3g"
+              % (prec, s_["frame"], s_["kept"], s_["pc_max"], s_["dp_max"], s_["pc_rms_all"], s_["pc_max_all"]))
     tol = F32_PHASE_TOL if prec == "f32" else F64_PHASE_TOL
-    assert e_pc < tol and e_dp < tol
+    assert all(s_["pc_max"] < tol and s_["dp_max"] < tol and s_["pc_rms_all"] < tol for s_ in st)
 
 
 def test_reference_update_rate_semantics(glsu, oracle, synth):
     frames, phi0, _ = synth.sequence(48, 40, 5, seed=9)
     wp = glsu.WffParams(3.0, -0.5, 0.5, 0.25, 3.0, -0.5, 0.5, 0.25, 0.1)
+    st = teacher_forced(glsu, oracle, frames.astype(np.float64), phi0, 2, wp, "f64", rr=2)
+    assert all(s_["dp_max"] < F64_PHASE_TOL for s_ in st)
     d = glsu.DPRA(phi0, 2, 2, "f64", wp)
     dps, _ = d.sequence(frames.astype(np.float64))
-    _, odp = oracle.glsu_sequence(frames.astype(np.float64), phi0, 2, oracle.WffParams(*wp.tuple()), rr=2)
-    assert np.abs(dps - odp).max() < F64_PHASE_TOL
     d.close()
+    d = glsu.DPRA(phi0, 2, 2, "f64", wp)
+    ref = []
+    for i, fr in enumerate(frames.astype(np.float64)):
+        ref.append(d.per_frame(fr)[0])
+        if i % 2 == 0:
+            d.update_ref_phi()
+    d.close()
+    assert np.array_equal(dps, np.stack(ref))
 
 
 def test_aia_reference_bmp_frames(glsu, oracle):
@@ -217,13 +238,10 @@ def test_glsu_frame_1024_matches_oracle(glsu, oracle, synth):
     """One full-size frame (1024x1024, DPRA 7x7, 441 frequencies) against the oracle."""
     frames, phi0, _ = synth.sequence(1024, 1024, 2, seed=1)
     wp = glsu.WffParams(10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)
-    pcs, dps = run_sequence(glsu, frames[1:], phi0.astype(np.float32), 3, wp, "f32")
-    opc, odp, _, _ = oracle.glsu_frame(frames[1].astype(np.float64), phi0.astype(np.float32).astype(np.float64),
-                                       np.zeros((1024, 1024)), 3, oracle.WffParams(*wp.tuple()))
-    e_pc = np.abs(synth.phase_err(pcs[0], opc)).max()
-    rms = np.sqrt(np.mean(synth.phase_err(pcs[0], opc) ** 2))
-    print("1024 frame f32: max err %.3g rad, rms %.3g rad" % (e_pc, rms))
-    assert e_pc < F32_PHASE_TOL
+    st = teacher_forced(glsu, oracle, frames[1:], phi0, 3, wp, "f32")[0]
+    print("1024 frame f32: kept %.4f, phi max %.3g, dphi max %.3g, rms(all) %.3g, max(all) %.3g"
+          % (st["kept"], st["pc_max"], st["dp_max"], st["pc_rms_all"], st["pc_max_all"]))
+    assert st["pc_max"] < F32_PHASE_TOL and st["pc_rms_all"] < F32_PHASE_TOL
 
 
 def test_error_codes_on_device(glsu):
