@@ -52,6 +52,9 @@ constexpr int kPhasorPad = 2 * kMaxHalf;
 // kernel records GLSU_ERR_TIMEOUT in its error word and returns.
 constexpr long long kSpinLimit = 1ll << 26;
 
+// Blocks (and partial sums) of the automatic-threshold reduction.
+constexpr int kThrBlocks = 304;
+
 // ---------------------------------------------------------------------------
 // WFF2 plan: the frequency sweep on the device (see wff_kernels.cu)
 // ---------------------------------------------------------------------------

@@ -438,7 +438,6 @@ __global__ void __launch_bounds__(256) wff_rows_final_kernel(const C2<T> *__rest
 // ---------------------------------------------------------------------------
 // automatic threshold: thr = 6 sqrt(mean|f|^2 / 3)  (WFT/WFT2_CPU.cpp:977-1005)
 // ---------------------------------------------------------------------------
-constexpr int kThrBlocks = 304;
 
 template <typename T>
 __global__ void __launch_bounds__(256) wff_thr_partial_kernel(const C2<T> *__restrict__ f, size_t n,

@@ -108,6 +108,7 @@ def lib() -> ctypes.CDLL:
             "glsu_wff_run_async": ([c_void_p, c_void_p, c_void_p], c_int),
             "glsu_wff_threshold": ([c_void_p, dblp], c_int),
             "glsu_wff_padded_size": ([c_void_p, intp, intp], c_int),
+            "glsu_wff_run_noalloc": ([c_int, c_int, prm, c_void_p, c_void_p, c_void_p], c_int),
             "glsu_dpra_create": ([pp, c_int, c_void_p, c_int, c_int, c_int, c_int, prm], c_int),
             "glsu_dpra_destroy": ([c_void_p], c_int),
             "glsu_dpra_set_stream": ([c_void_p, c_void_p], c_int),

@@ -101,6 +101,31 @@ int glsu_wff_threshold(glsu_wff *h, double *thr);
 /* FFT-padded plane of the reference's formulation (kept for API parity). */
 int glsu_wff_padded_size(const glsu_wff *h, int *padded_width, int *padded_height);
 
+/* WFF2 in FP32 without allocating any device memory.  This entry point has
+ * no counterpart in the reference.  It is for callers that are not allowed
+ * to call cudaMalloc: a plugin living inside a host application whose
+ * device memory is handed out by that application's own pool, a real-time
+ * frame loop that must never stall in the allocator, or a deployment that
+ * fixes its whole device-memory budget when the library is loaded.
+ *
+ * The caller still passes the input d_f and the output d_filtered (device
+ * H*W complex64, as glsu_wff_run) and a stream (NULL: the legacy default
+ * stream); p == NULL selects the reference WFF defaults.  Scratch comes from
+ * one fixed 64 MiB array inside the library, which every GPU that loads the
+ * library holds until the process exits; problems whose scratch -- 2 x
+ * (number of x-frequencies) planes of H x round_up(W, 128) complex64 plus
+ * small tables -- exceeds 64 MiB are rejected with GLSU_ERR_INVALID and a
+ * message giving the size needed (256x256 with 21x21 frequencies uses 22 MiB).
+ *
+ * The first call on a device looks up that array's device address (once
+ * per device, with the device current); make that first call before any
+ * stream capture.  All calls share the array and each call overwrites it,
+ * so calls whose work overlaps on the GPU race: serialise them.  The call
+ * returns when the result is complete.  An automatic threshold (thr < 0) is
+ * recomputed on every call, since nothing is kept between calls. */
+int glsu_wff_run_noalloc(int width, int height, const glsu_wff_params *p, const void *d_f, void *d_filtered,
+                         void *cuda_stream);
+
 /* ---- DPRA: DPRA_CUDAF (F32) / DPRA_CUDA (F64) --------------------------- */
 /* h_phi0: HOST pointer to W*H initial phase in the handle's precision
  * (copied to the device, as DPRA_CUDAF's constructor does).
