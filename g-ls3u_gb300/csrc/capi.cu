@@ -196,6 +196,7 @@ extern "C" int glsu_wff_create(glsu_wff **out, int precision, int width, int hei
     if (rc == GLSU_OK) rc = h->plan.alloc_device();
     if (rc == GLSU_OK) rc = h->plan.upload_tables(h->stream);
     if (rc == GLSU_OK) rc = h->plan.make_tensor_map();
+    if (rc == GLSU_OK) rc = h->plan.init_colfft();
     if (rc == GLSU_OK && (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess))
         rc = fail(GLSU_ERR_CUDA, "cudaEventCreate failed");
     if (rc != GLSU_OK) {
@@ -273,6 +274,28 @@ extern "C" int glsu_wff_threshold(glsu_wff *h, double *thr)
     return GLSU_OK;
 }
 
+static int set_method(WffPlan &P, int method)
+{
+    if (method != GLSU_METHOD_AUTO && method != GLSU_METHOD_DIRECT && method != GLSU_METHOD_FFT)
+        return fail(GLSU_ERR_INVALID, "unknown column-sweep method");
+    if (method == GLSU_METHOD_FFT && P.fft_L == 0)
+        return fail(GLSU_ERR_UNSUPPORTED, "no shared-memory FFT plan for this handle (FP64, or no transform length)");
+    P.method = method;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_wff_set_method(glsu_wff *h, int method)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    return set_method(h->plan, method);
+}
+
+extern "C" int glsu_dpra_set_method(glsu_dpra *h, int method)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    return set_method(h->wff, method);
+}
+
 extern "C" int glsu_wff_padded_size(const glsu_wff *h, int *pw, int *ph)
 {
     if (!h) return fail(GLSU_ERR_INVALID, "null handle");
@@ -306,6 +329,7 @@ extern "C" int glsu_dpra_create(glsu_dpra **out, int precision, const void *h_ph
     if (rc == GLSU_OK) rc = h->wff.alloc_device();
     if (rc == GLSU_OK) rc = h->wff.upload_tables(h->stream);
     if (rc == GLSU_OK) rc = h->wff.make_tensor_map();
+    if (rc == GLSU_OK) rc = h->wff.init_colfft();
     const size_t N = (size_t)width * height;
     const size_t es = precision == GLSU_F32 ? 4 : 8;
     if (rc == GLSU_OK) {

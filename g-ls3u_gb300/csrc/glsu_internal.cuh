@@ -96,7 +96,21 @@ struct WffPlan {
     int enqueue(cudaStream_t s, const void *d_f, void *d_out, int final_mode, const void *phi_ref,
                 const void *dphi_ref, void *phi_curr, void *dphi, cudaEvent_t *stage_ev);
     int check_device_error(cudaStream_t s);
+
+    // Column sweep by shared-memory FFTs (FP32 form; see wff_colfft.cu).
+    int method = GLSU_METHOD_AUTO;  // GLSU_METHOD_AUTO / DIRECT / FFT
+    int fft_L = 0, fft_nst = 0;     // fft_L == 0: no FFT plan, the direct kernel runs
+    int fft_radix[12];
+    void *d_khat = nullptr;         // nfy x fft_L spectra of the modulated windows
+    void *d_tw = nullptr;           // fft_L twiddles e^{-2 pi i t / L}
+    int init_colfft();
+    void release_colfft();
+    // The FFT sweep runs when asked for: on GB300 the direct kernel is faster
+    // at the benchmark sizes (5.5 vs 9.1 ms at 1024^2 with 21x21 frequencies).
+    bool use_colfft() const { return fft_L > 0 && d_khat != nullptr && method == GLSU_METHOD_FFT; }
 };
+
+int launch_colfft(const WffPlan &P, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // kernel launchers

@@ -1,0 +1,399 @@
+// wff_colfft.cu -- WFF2 column sweep with shared-memory FFTs (FP32 form).
+//
+// Same mathematics as wff_cols_kernel, evaluated in the frequency domain of
+// each column.  For one x-frequency plane R_i and one column, with
+// h_k(m) = gy(m) e^{j wy_k m} (m in [-s, s]) the truncated, modulated
+// window and L >= H + 2s (so the circular convolutions below are the
+// linear, zero-boundary ones of the reference):
+//     U_k  = IFFT( FFT(R) . H_k )            (|U_k| / (L N) is |sf|)
+//     T_k  = U_k . [ |U_k| >= L N thr ],  rows >= H set to 0
+//     Ch  += FFT(T_k) . H_k                  (sum over wy_k in the spectrum)
+//     C    = IFFT(Ch) / (L^2 N)              (the C_i plane of the direct kernel)
+// H_k = FFT(h_k) is tabulated exactly (host, FP64), so the window is the
+// reference CPU path's truncated one.  Per column and plane: 1 + 2 nfy + 1
+// transforms of length L, all in shared memory / registers; FFT(R) and the
+// spectrum accumulator stay in registers for all nfy frequencies.
+//
+// Transforms: Stockham auto-sort, radix 8/4/2/5/3 stages, ping-pong between
+// two shared buffers laid out [L][NC] (NC columns per CTA, column index
+// fastest) with one float2 of padding per 16 elements against bank
+// conflicts on the strided writes of the early stages.
+#include <cmath>
+#include <vector>
+
+#include "glsu_internal.cuh"
+
+namespace glsu {
+
+constexpr int kFftThreads = 512;
+
+struct ColFftPlan {
+    int L;
+    int nst;
+    int radix[12];
+};
+
+__device__ __forceinline__ int pidx(int e) { return e + (e >> 4); }
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// In-register DFTs; INV selects the sign of the exponent (+ for the inverse).
+template <bool INV> __device__ __forceinline__ float2 mul_mi(float2 a)
+{
+    // forward: multiply by -i ; inverse: by +i
+    return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+template <bool INV> __device__ __forceinline__ void dft2(float2 *v)
+{
+    const float2 a = v[0], b = v[1];
+    v[0] = make_float2(a.x + b.x, a.y + b.y);
+    v[1] = make_float2(a.x - b.x, a.y - b.y);
+}
+
+template <bool INV> __device__ __forceinline__ void dft4(float2 *v)
+{
+    const float2 a0 = make_float2(v[0].x + v[2].x, v[0].y + v[2].y);
+    const float2 a1 = make_float2(v[0].x - v[2].x, v[0].y - v[2].y);
+    const float2 a2 = make_float2(v[1].x + v[3].x, v[1].y + v[3].y);
+    const float2 a3 = mul_mi<INV>(make_float2(v[1].x - v[3].x, v[1].y - v[3].y));
+    v[0] = make_float2(a0.x + a2.x, a0.y + a2.y);
+    v[2] = make_float2(a0.x - a2.x, a0.y - a2.y);
+    v[1] = make_float2(a1.x + a3.x, a1.y + a3.y);
+    v[3] = make_float2(a1.x - a3.x, a1.y - a3.y);
+}
+
+template <bool INV> __device__ __forceinline__ void dft8(float2 *v)
+{
+    // X[2q] = DFT4(v_r + v_{r+4}), X[2q+1] = DFT4((v_r - v_{r+4}) w8^r)
+    const float h = 0.70710678118654752f;
+    float2 b[4], c[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        b[r] = make_float2(v[r].x + v[r + 4].x, v[r].y + v[r + 4].y);
+        c[r] = make_float2(v[r].x - v[r + 4].x, v[r].y - v[r + 4].y);
+    }
+    // w8 = e^{-+ i pi/4}
+    c[1] = INV ? make_float2(h * (c[1].x - c[1].y), h * (c[1].x + c[1].y))
+               : make_float2(h * (c[1].x + c[1].y), h * (c[1].y - c[1].x));
+    c[2] = mul_mi<INV>(c[2]);
+    c[3] = INV ? make_float2(-h * (c[3].x + c[3].y), h * (c[3].x - c[3].y))
+               : make_float2(h * (c[3].y - c[3].x), -h * (c[3].x + c[3].y));
+    dft4<INV>(b);
+    dft4<INV>(c);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        v[2 * q] = b[q];
+        v[2 * q + 1] = c[q];
+    }
+}
+
+template <bool INV> __device__ __forceinline__ void dft3(float2 *v)
+{
+    const float s3 = 0.86602540378443865f;  // sin(2 pi / 3)
+    const float2 t1 = make_float2(v[1].x + v[2].x, v[1].y + v[2].y);
+    const float2 t2 = make_float2(v[1].x - v[2].x, v[1].y - v[2].y);
+    const float2 m = make_float2(v[0].x - 0.5f * t1.x, v[0].y - 0.5f * t1.y);
+    // forward: X1 = m - i s3 t2, X2 = m + i s3 t2
+    const float2 j = INV ? make_float2(-s3 * t2.y, s3 * t2.x) : make_float2(s3 * t2.y, -s3 * t2.x);
+    v[0] = make_float2(v[0].x + t1.x, v[0].y + t1.y);
+    v[1] = make_float2(m.x + j.x, m.y + j.y);
+    v[2] = make_float2(m.x - j.x, m.y - j.y);
+}
+
+template <bool INV> __device__ __forceinline__ void dft5(float2 *v)
+{
+    // X_q = sum_r v_r e^{-+ 2 pi i q r / 5}, via the two symmetric pairs
+    const float c1 = 0.30901699437494742f, c2 = -0.80901699437494742f;  // cos(2pi/5), cos(4pi/5)
+    const float s1 = 0.95105651629515357f, s2 = 0.58778525229247313f;   // sin(2pi/5), sin(4pi/5)
+    const float2 a1 = make_float2(v[1].x + v[4].x, v[1].y + v[4].y);
+    const float2 b1 = make_float2(v[1].x - v[4].x, v[1].y - v[4].y);
+    const float2 a2 = make_float2(v[2].x + v[3].x, v[2].y + v[3].y);
+    const float2 b2 = make_float2(v[2].x - v[3].x, v[2].y - v[3].y);
+    const float2 m1 = make_float2(v[0].x + c1 * a1.x + c2 * a2.x, v[0].y + c1 * a1.y + c2 * a2.y);
+    const float2 m2 = make_float2(v[0].x + c2 * a1.x + c1 * a2.x, v[0].y + c2 * a1.y + c1 * a2.y);
+    // n1 = s1 b1 + s2 b2, n2 = s2 b1 - s1 b2; X1 = m1 -+ i n1, X4 = m1 +- i n1, X2 = m2 -+ i n2, X3 = m2 +- i n2
+    const float2 n1 = make_float2(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y);
+    const float2 n2 = make_float2(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y);
+    const float2 j1 = INV ? make_float2(-n1.y, n1.x) : make_float2(n1.y, -n1.x);
+    const float2 j2 = INV ? make_float2(-n2.y, n2.x) : make_float2(n2.y, -n2.x);
+    v[0] = make_float2(v[0].x + a1.x + a2.x, v[0].y + a1.y + a2.y);
+    v[1] = make_float2(m1.x + j1.x, m1.y + j1.y);
+    v[4] = make_float2(m1.x - j1.x, m1.y - j1.y);
+    v[2] = make_float2(m2.x + j2.x, m2.y + j2.y);
+    v[3] = make_float2(m2.x - j2.x, m2.y - j2.y);
+}
+
+template <int R, bool INV> __device__ __forceinline__ void dft(float2 *v)
+{
+    if (R == 2) dft2<INV>(v);
+    else if (R == 4) dft4<INV>(v);
+    else if (R == 8) dft8<INV>(v);
+    else if (R == 3) dft3<INV>(v);
+    else dft5<INV>(v);
+}
+
+// One Stockham stage over all NC columns: in -> out.
+template <int R, bool INV, int NC>
+__device__ __forceinline__ void fft_stage(const float2 *__restrict__ in, float2 *__restrict__ out, int L, int Ns,
+                                          const float2 *__restrict__ tw)
+{
+    const int LR = L / R;
+    const int tstep = L / (Ns * R);
+    const int nb = LR * NC;
+    for (int b = threadIdx.x; b < nb; b += kFftThreads) {
+        const int c = b % NC, j = b / NC;
+        const int k = j % Ns;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) v[r] = in[pidx((j + r * LR) * NC + c)];
+        if (Ns > 1) {
+#pragma unroll
+            for (int r = 1; r < R; r++) {
+                float2 w = __ldg(tw + r * k * tstep);
+                if (INV) w.y = -w.y;
+                v[r] = cmulf(v[r], w);
+            }
+        }
+        dft<R, INV>(v);
+        const int idxD = (j / Ns) * Ns * R + k;
+#pragma unroll
+        for (int r = 0; r < R; r++) out[pidx((idxD + r * Ns) * NC + c)] = v[r];
+    }
+}
+
+// Full transform; returns the buffer holding the result (a or b).
+template <bool INV, int NC>
+__device__ float2 *fft_run(float2 *a, float2 *b, const ColFftPlan &P, const float2 *__restrict__ tw)
+{
+    int Ns = 1;
+    float2 *in = a, *out = b;
+    for (int s = 0; s < P.nst; s++) {
+        const int R = P.radix[s];
+        switch (R) {
+        case 8: fft_stage<8, INV, NC>(in, out, P.L, Ns, tw); break;
+        case 4: fft_stage<4, INV, NC>(in, out, P.L, Ns, tw); break;
+        case 2: fft_stage<2, INV, NC>(in, out, P.L, Ns, tw); break;
+        case 5: fft_stage<5, INV, NC>(in, out, P.L, Ns, tw); break;
+        default: fft_stage<3, INV, NC>(in, out, P.L, Ns, tw); break;
+        }
+        __syncthreads();
+        Ns *= R;
+        float2 *t = in;
+        in = out;
+        out = t;
+    }
+    return in;
+}
+
+// MAXE: elements (of the L x NC block) owned per thread, upper bound.
+template <int NC, int MAXE>
+__global__ void __launch_bounds__(kFftThreads, 1) wff_colfft_kernel(const float2 *__restrict__ R, float2 *__restrict__ Cout,
+                                                                 int H, int pitch, int nfy,
+                                                                 const float2 *__restrict__ khat,
+                                                                 const float2 *__restrict__ tw, ColFftPlan P,
+                                                                 const float *__restrict__ thr_ptr, float LN,
+                                                                 float out_scale)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int L = P.L;
+    const int nel = L * NC;
+    float2 *bufA = reinterpret_cast<float2 *>(smem_raw);
+    float2 *bufB = bufA + pidx(nel) + 1;
+    const int tid = threadIdx.x;
+    const int x0 = blockIdx.x * NC, i = blockIdx.y;
+    const size_t plane = (size_t)H * pitch;
+    const float2 *Ri = R + i * plane;
+
+    // load the NC columns (rows >= H are zero)
+    for (int e = tid; e < nel; e += kFftThreads) {
+        const int rho = e / NC, c = e - rho * NC;
+        float2 v = make_float2(0.f, 0.f);
+        if (rho < H) v = Ri[(size_t)rho * pitch + x0 + c];
+        bufA[pidx(e)] = v;
+    }
+    __syncthreads();
+    const float2 *res = fft_run<false, NC>(bufA, bufB, P, tw);
+    float2 rh[MAXE], ch[MAXE];
+#pragma unroll
+    for (int j = 0; j < MAXE; j++) {
+        const int e = tid + j * kFftThreads;
+        rh[j] = (e < nel) ? res[pidx(e)] : make_float2(0.f, 0.f);
+        ch[j] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const float T = LN * (*thr_ptr);
+    const float T2 = T * T;
+    for (int k = 0; k < nfy; k++) {
+        const float2 *hk = khat + (size_t)k * L;
+#pragma unroll
+        for (int j = 0; j < MAXE; j++) {
+            const int e = tid + j * kFftThreads;
+            if (e < nel) bufA[pidx(e)] = cmulf(rh[j], __ldg(hk + e / NC));
+        }
+        __syncthreads();
+        float2 *u = fft_run<true, NC>(bufA, bufB, P, tw);
+        // hard threshold in the spatial domain (own elements only)
+#pragma unroll
+        for (int j = 0; j < MAXE; j++) {
+            const int e = tid + j * kFftThreads;
+            if (e < nel) {
+                const float2 v = u[pidx(e)];
+                const bool keep = (e / NC < H) && (v.x * v.x + v.y * v.y >= T2);
+                if (!keep) u[pidx(e)] = make_float2(0.f, 0.f);
+            }
+        }
+        __syncthreads();
+        float2 *other = (u == bufA) ? bufB : bufA;
+        const float2 *sp = fft_run<false, NC>(u, other, P, tw);
+#pragma unroll
+        for (int j = 0; j < MAXE; j++) {
+            const int e = tid + j * kFftThreads;
+            if (e < nel) {
+                const float2 a = sp[pidx(e)], h = __ldg(hk + e / NC);
+                ch[j].x += a.x * h.x - a.y * h.y;
+                ch[j].y += a.x * h.y + a.y * h.x;
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < MAXE; j++) {
+        const int e = tid + j * kFftThreads;
+        if (e < nel) bufA[pidx(e)] = ch[j];
+    }
+    __syncthreads();
+    const float2 *cres = fft_run<true, NC>(bufA, bufB, P, tw);
+    float2 *Ci = Cout + i * plane;
+    for (int e = tid; e < nel; e += kFftThreads) {
+        const int rho = e / NC, c = e - rho * NC;
+        if (rho < H) {
+            const float2 v = cres[pidx(e)];
+            Ci[(size_t)rho * pitch + x0 + c] = make_float2(v.x * out_scale, v.y * out_scale);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static int factor(int n, int *rad)
+{
+    int ns = 0;
+    while (n % 8 == 0) { rad[ns++] = 8; n /= 8; }
+    while (n % 4 == 0) { rad[ns++] = 4; n /= 4; }
+    while (n % 2 == 0) { rad[ns++] = 2; n /= 2; }
+    while (n % 5 == 0) { rad[ns++] = 5; n /= 5; }
+    while (n % 3 == 0) { rad[ns++] = 3; n /= 3; }
+    return n == 1 ? ns : -1;
+}
+
+// Smallest-cost transform length >= need: cost = L x number of stages.
+static int choose_length(int need, ColFftPlan *out)
+{
+    long best_cost = -1;
+    for (int L = need; L <= 2 * need + 16; L++) {
+        ColFftPlan p;
+        const int ns = factor(L, p.radix);
+        if (ns < 1 || ns > 12) continue;
+        const long cost = (long)L * ns;
+        if (best_cost < 0 || cost < best_cost) {
+            best_cost = cost;
+            p.L = L;
+            p.nst = ns;
+            *out = p;
+        }
+    }
+    return best_cost < 0 ? -1 : 0;
+}
+
+static int colfft_nc(int L) { return L <= 1600 ? 4 : 2; }
+
+int WffPlan::init_colfft()
+{
+    if (prec != GLSU_F32) return GLSU_OK;
+    ColFftPlan p;
+    if (choose_length(H + 2 * sy, &p)) return GLSU_OK;  // no suitable length: direct kernel
+    const int nc = colfft_nc(p.L);
+    if ((size_t)p.L * nc > (size_t)kFftThreads * 13 || pitch % nc) return GLSU_OK;  // registers per thread
+    fft_L = p.L;
+    fft_nst = p.nst;
+    for (int s = 0; s < p.nst; s++) fft_radix[s] = p.radix[s];
+    // H_k = DFT of h_k(m) = gy(m) e^{j wy_k m}, m in [-sy, sy] placed circularly
+    std::vector<float> kh(2 * (size_t)nfy * p.L), tw(2 * (size_t)p.L);
+    for (int k = 0; k < nfy; k++) {
+        const double wy = this->p.wyl + (double)k * this->p.wyi;
+        for (int w = 0; w < p.L; w++) {
+            double re = 0, im = 0;
+            for (int m = -sy; m <= sy; m++) {
+                const double ang = wy * m - 2.0 * M_PI * (double)w * (double)m / (double)p.L;
+                re += gy[m + sy] * std::cos(ang);
+                im += gy[m + sy] * std::sin(ang);
+            }
+            kh[2 * ((size_t)k * p.L + w)] = (float)re;
+            kh[2 * ((size_t)k * p.L + w) + 1] = (float)im;
+        }
+    }
+    for (int t = 0; t < p.L; t++) {
+        tw[2 * t] = (float)std::cos(-2.0 * M_PI * t / p.L);
+        tw[2 * t + 1] = (float)std::sin(-2.0 * M_PI * t / p.L);
+    }
+    if (cudaMalloc(&d_khat, kh.size() * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&d_tw, tw.size() * sizeof(float)) != cudaSuccess)
+        return fail(GLSU_ERR_ALLOC, "cudaMalloc of the column FFT tables failed");
+    GLSU_CUDA_TRY(cudaMemcpy(d_khat, kh.data(), kh.size() * sizeof(float), cudaMemcpyHostToDevice));
+    GLSU_CUDA_TRY(cudaMemcpy(d_tw, tw.data(), tw.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return GLSU_OK;
+}
+
+void WffPlan::release_colfft()
+{
+    cudaFree(d_khat);
+    cudaFree(d_tw);
+    d_khat = d_tw = nullptr;
+    fft_L = 0;
+}
+
+template <int NC, int MAXE> static int launch_colfft_t(const WffPlan &P, cudaStream_t s)
+{
+    ColFftPlan cp;
+    cp.L = P.fft_L;
+    cp.nst = P.fft_nst;
+    for (int k = 0; k < 12; k++) cp.radix[k] = k < P.fft_nst ? P.fft_radix[k] : 0;
+    const int nel = cp.L * NC;
+    const size_t smem = sizeof(float2) * 2 * (size_t)(nel + (nel >> 4) + 1);
+    static bool attr = false;
+    if (!attr) {
+        GLSU_CUDA_TRY(cudaFuncSetAttribute(wff_colfft_kernel<NC, MAXE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           112 * 1024));
+        attr = true;
+    }
+    if (smem > 112 * 1024) return fail(GLSU_ERR_UNSUPPORTED, "column FFT length too large");
+    const double N = 1.0 / P.inv_norm;
+    dim3 grid(P.pitch / NC, P.nfx);
+    wff_colfft_kernel<NC, MAXE><<<grid, kFftThreads, smem, s>>>(
+        (const float2 *)P.d_R, (float2 *)P.d_C, P.H, P.pitch, P.nfy, (const float2 *)P.d_khat,
+        (const float2 *)P.d_tw, cp, (const float *)P.d_thr, (float)(cp.L * N),
+        (float)(1.0 / ((double)cp.L * cp.L * N)));
+    GLSU_CUDA_TRY(cudaGetLastError());
+    return GLSU_OK;
+}
+
+int launch_colfft(const WffPlan &P, cudaStream_t s)
+{
+    const int nc = colfft_nc(P.fft_L);
+    const int per = (P.fft_L * nc + kFftThreads - 1) / kFftThreads;  // elements owned per thread
+    if (nc == 4) {
+        if (per <= 3) return launch_colfft_t<4, 3>(P, s);
+        if (per <= 5) return launch_colfft_t<4, 5>(P, s);
+        if (per <= 10) return launch_colfft_t<4, 10>(P, s);
+        return launch_colfft_t<4, 13>(P, s);
+    }
+    if (per <= 10) return launch_colfft_t<2, 10>(P, s);
+    return launch_colfft_t<2, 13>(P, s);
+}
+
+}  // namespace glsu

@@ -634,6 +634,7 @@ int WffPlan::make_tensor_map()
 
 void WffPlan::release()
 {
+    release_colfft();
     cudaFree(d_ex);
     cudaFree(d_ey);
     d_ex = d_ey = nullptr;
@@ -750,12 +751,16 @@ static int enqueue_t(WffPlan &P, cudaStream_t s, const void *d_f, void *d_out, i
     }
     if (rc) return rc;
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[1], s));
-    switch (P.syi) {
-    case 12: rc = launch_cols<T, 12>(P, s); break;
-    case 20: rc = launch_cols<T, 20>(P, s); break;
-    case 30: rc = launch_cols<T, 30>(P, s); break;
-    case 45: rc = launch_cols<T, 45>(P, s); break;
-    default: rc = launch_cols<T, 60>(P, s); break;
+    if (sizeof(T) == 4 && P.use_colfft()) {
+        rc = launch_colfft(P, s);
+    } else {
+        switch (P.syi) {
+        case 12: rc = launch_cols<T, 12>(P, s); break;
+        case 20: rc = launch_cols<T, 20>(P, s); break;
+        case 30: rc = launch_cols<T, 30>(P, s); break;
+        case 45: rc = launch_cols<T, 45>(P, s); break;
+        default: rc = launch_cols<T, 60>(P, s); break;
+        }
     }
     if (rc) return rc;
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[2], s));

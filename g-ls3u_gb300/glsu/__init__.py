@@ -36,6 +36,7 @@ ERR_UNSUPPORTED, ERR_NOT_POSDEF, ERR_TIMEOUT, ERR_NO_DEVICE = -5, -6, -7, -8
 F32, F64, U8 = 0, 1, 2
 PHI_REF, PHI_CURR, DPHI_REF, DPHI = 0, 1, 2, 3
 WFT_WFF, WFT_WFR = 0, 1
+METHOD_AUTO, METHOD_DIRECT, METHOD_FFT = 0, 1, 2
 
 _lock = threading.Lock()
 _lib = None
@@ -107,6 +108,8 @@ def lib() -> ctypes.CDLL:
             "glsu_wff_run": ([c_void_p, c_void_p, c_void_p, dblp], c_int),
             "glsu_wff_run_async": ([c_void_p, c_void_p, c_void_p], c_int),
             "glsu_wff_threshold": ([c_void_p, dblp], c_int),
+            "glsu_wff_set_method": ([c_void_p, c_int], c_int),
+            "glsu_dpra_set_method": ([c_void_p, c_int], c_int),
             "glsu_wff_padded_size": ([c_void_p, intp, intp], c_int),
             "glsu_wff_run_noalloc": ([c_int, c_int, prm, c_void_p, c_void_p, c_void_p], c_int),
             "glsu_dpra_create": ([pp, c_int, c_void_p, c_int, c_int, c_int, c_int, prm], c_int),
@@ -225,6 +228,10 @@ class WFF2:
     def run_async(self, d_f: int, d_out: int):
         check(lib().glsu_wff_run_async(self._h, ctypes.c_void_p(d_f), ctypes.c_void_p(d_out)))
 
+    def set_method(self, method: int):
+        """Column-sweep method: METHOD_AUTO, METHOD_DIRECT or METHOD_FFT."""
+        check(lib().glsu_wff_set_method(self._h, method))
+
     @property
     def threshold(self) -> float:
         t = ctypes.c_double(0)
@@ -309,6 +316,10 @@ class DPRA:
         p = ctypes.c_void_p()
         check(lib().glsu_dpra_device_ptr(self._h, which, ctypes.byref(p)))
         return p.value
+
+    def set_method(self, method: int):
+        """Column-sweep method of the WFF2: METHOD_AUTO, METHOD_DIRECT or METHOD_FFT."""
+        check(lib().glsu_dpra_set_method(self._h, method))
 
     def stage_timing(self, enable: bool = True):
         check(lib().glsu_dpra_stage_timing(self._h, int(enable)))

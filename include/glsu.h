@@ -50,6 +50,15 @@ extern "C" {
 #define GLSU_DPHI_REF 2
 #define GLSU_DPHI 3
 
+/* Column-sweep method of the WFF2 (glsu_wff_set_method / glsu_dpra_set_method):
+ * DIRECT convolves the columns with the truncated window; FFT (FP32 form
+ * only) does the same in the frequency domain of each column with
+ * shared-memory transforms; AUTO picks DIRECT, the faster of the two on
+ * GB300 at the sizes measured. */
+#define GLSU_METHOD_AUTO 0
+#define GLSU_METHOD_DIRECT 1
+#define GLSU_METHOD_FFT 2
+
 /* WFT_TYPE of the reference (WFT-FPA.h enum WFT_TYPE) */
 #define GLSU_WFT_WFF 0
 #define GLSU_WFT_WFR 1
@@ -98,6 +107,10 @@ int glsu_wff_run(glsu_wff *h, const void *d_f, void *d_filtered, double *time_ms
 int glsu_wff_run_async(glsu_wff *h, const void *d_f, void *d_filtered);
 /* Threshold in use (after the first call when automatic). */
 int glsu_wff_threshold(glsu_wff *h, double *thr);
+/* Choose the column-sweep method (GLSU_METHOD_*); results agree to FP32
+ * rounding.  GLSU_METHOD_FFT fails with GLSU_ERR_UNSUPPORTED where no
+ * transform plan exists (FP64 handles). */
+int glsu_wff_set_method(glsu_wff *h, int method);
 /* FFT-padded plane of the reference's formulation (kept for API parity). */
 int glsu_wff_padded_size(const glsu_wff *h, int *padded_width, int *padded_height);
 
@@ -158,6 +171,8 @@ int glsu_dpra_get(glsu_dpra *h, int which, void *h_out);
 int glsu_dpra_get_lsq(glsu_dpra *h, void *h_out);
 /* Device address of a state plane (valid until the next call on h). */
 int glsu_dpra_device_ptr(glsu_dpra *h, int which, void **d_ptr);
+/* Column-sweep method of the handle's WFF2 (GLSU_METHOD_*). */
+int glsu_dpra_set_method(glsu_dpra *h, int method);
 /* Record CUDA events between the stages of each frame (off by default). */
 int glsu_dpra_stage_timing(glsu_dpra *h, int enable);
 /* Device times (ms) of the stages of the last frame: [0] LS solve, [1] WFF

@@ -19,12 +19,14 @@ def _torch():
     return torch
 
 
-def wff_gpu(glsu, f, prec, params):
+def wff_gpu(glsu, f, prec, params, method=None):
     torch = _torch()
     dt = np.complex64 if prec == "f32" else np.complex128
     t = torch.from_numpy(np.ascontiguousarray(f, dt)).cuda()
     out = torch.empty_like(t)
     w = glsu.WFF2(f.shape[1], f.shape[0], prec, params)
+    if method is not None:
+        w.set_method(method)
     ms = w.run(t.data_ptr(), out.data_ptr())
     thr = w.threshold
     w.close()
@@ -62,14 +64,17 @@ WFF_CASES = [
 ]
 
 
+@pytest.mark.parametrize("method", ["direct", "fft"])
 @pytest.mark.parametrize("case", range(len(WFF_CASES)))
-def test_wff_f32_matches_oracle(glsu, oracle, case):
+def test_wff_f32_matches_oracle(glsu, oracle, case, method):
+    """Both column-sweep methods (direct convolution, shared-memory FFT)."""
     shape, p = WFF_CASES[case]
     f = field(shape, case)
     ref, rthr = oracle.wff2(f.astype(np.complex64).astype(np.complex128), *p)
-    out, thr, _ = wff_gpu(glsu, f, "f32", glsu.WffParams(*p))
+    m = glsu.METHOD_DIRECT if method == "direct" else glsu.METHOD_FFT
+    out, thr, _ = wff_gpu(glsu, f, "f32", glsu.WffParams(*p), m)
     perr, rel = compare(out, ref)
-    print("wff f32 case %d: phase err %.3g rad, rel err %.3g" % (case, perr, rel))
+    print("wff f32 %s case %d: phase err %.3g rad, rel err %.3g" % (method, case, perr, rel))
     assert abs(thr - rthr) <= 1e-5 * rthr
     assert perr < F32_PHASE_TOL and rel < 1e-4
 
@@ -84,6 +89,17 @@ def test_wff_f64_matches_oracle(glsu, oracle, case):
     print("wff f64 case %d: phase err %.3g rad, rel err %.3g" % (case, perr, rel))
     assert abs(thr - rthr) <= 1e-12 * rthr
     assert perr < F64_PHASE_TOL and rel < 1e-11
+
+
+def test_column_method_switch(glsu):
+    w = glsu.WFF2(64, 64, "f64", glsu.WffParams(4.0, -1, 1, 0.5, 4.0, -1, 1, 0.5, 0.1))
+    with pytest.raises(glsu.GlsuError) as e:
+        w.set_method(glsu.METHOD_FFT)
+    assert e.value.code == glsu.ERR_UNSUPPORTED
+    w.set_method(glsu.METHOD_DIRECT)
+    with pytest.raises(glsu.GlsuError):
+        w.set_method(7)
+    w.close()
 
 
 def test_wff_threshold_is_kept_after_first_call(glsu, oracle):
