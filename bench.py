@@ -66,6 +66,9 @@ def workload_config(size):
         "dpra_window": 2 * RADIUS + 1,
         "wff": {"sigma": WFF[0], "wl": WFF[1], "wh": WFF[2], "wi": WFF[3], "thr": WFF[8], "n_freq": NFX * NFY},
         "l2": "flushed before every timed step (256 MiB device write outside the timed events)",
+        "e2e_path": "glsu_dpra_sequence over K pinned host frames (H2D, D2H on their own streams, overlapped "
+                    "with neighbouring frames); L2 flushed once before, and each frame streams 352 MB of WFF2 "
+                    "planes, more than the 129 MB L2",
     }
 
 
@@ -259,22 +262,19 @@ def run_ours(args, rank, world, local):
     max_ms = reduce_max(dev_ms, world)
     value = world * args.steps / (max_ms / 1e3)
 
-    # ---- end to end through the public API with pinned host buffers
-    hfr = torch.from_numpy(frames).pin_memory()
-    hout = torch.empty((size, size), dtype=torch.float32).pin_memory()
-    for k in range(2):
-        d.per_frame_ptr(hfr[k].data_ptr(), glsu.F32, hout.data_ptr())
-        d.update_ref_phi()
-    e2e_s = 0.0
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        stream.synchronize()
-        t0 = time.perf_counter()
-        d.per_frame_ptr(hfr[k % nfr].data_ptr(), glsu.F32, hout.data_ptr())
-        d.update_ref_phi()
-        e2e_s += time.perf_counter() - t0
-    e2e_s = reduce_max(e2e_s, world)
+    # ---- end to end through the public API (glsu_dpra_sequence, the C-ABI of
+    # DPRA_CUDAF::operator()) with pinned host buffers: K frames uploaded,
+    # processed and downloaded; copies overlap neighbouring frames' compute
+    hseq = torch.from_numpy(np.ascontiguousarray(frames[np.arange(args.steps) % nfr])).pin_memory()
+    hout = torch.empty((args.steps, size, size), dtype=torch.float32).pin_memory()
+    d.sequence_ptr(min(2, args.steps), hseq.data_ptr(), glsu.F32, hout.data_ptr())  # warm the copy streams
+    with torch.cuda.stream(stream):
+        flush.zero_()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    d.sequence_ptr(args.steps, hseq.data_ptr(), glsu.F32, hout.data_ptr())
+    e2e_s = reduce_max(time.perf_counter() - t0, world)
     e2e = world * args.steps / e2e_s
     d.close()
 

@@ -72,9 +72,16 @@ struct glsu_dpra {
     void *h_in = nullptr, *h_out = nullptr;                 // pinned staging
     bool synced = true;  // phi_curr/dphi equal phi_ref/dphi_ref (after an update)
     bool timing = false;
+    bool unwrap = false;  // MATLAB fp_ls3u semantics: dphi = dphi_ref + unwrap(t)
+    int unwrap_row = -1, unwrap_col = -1;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     int frames_done = 0;
+    // pipelined sequence over pinned host buffers: frame slot s uses
+    // d_seq_img[s] (slot 0 is d_img) and output ring d_ring[s]
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    void *d_seq_img1 = nullptr, *d_ring[2] = {nullptr, nullptr};
+    cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
 };
 
 struct glsu_aia {
@@ -371,6 +378,17 @@ extern "C" int glsu_dpra_destroy(glsu_dpra *h)
         if (h->ev[k]) cudaEventDestroy(h->ev[k]);
     if (h->t0) cudaEventDestroy(h->t0);
     if (h->t1) cudaEventDestroy(h->t1);
+    if (h->s_in) cudaStreamSynchronize(h->s_in);
+    if (h->s_out) cudaStreamSynchronize(h->s_out);
+    cudaFree(h->d_seq_img1);
+    for (int s = 0; s < 2; s++) {
+        cudaFree(h->d_ring[s]);
+        if (h->ev_in[s]) cudaEventDestroy(h->ev_in[s]);
+        if (h->ev_comp[s]) cudaEventDestroy(h->ev_comp[s]);
+        if (h->ev_out[s]) cudaEventDestroy(h->ev_out[s]);
+    }
+    if (h->s_in) cudaStreamDestroy(h->s_in);
+    if (h->s_out) cudaStreamDestroy(h->s_out);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return GLSU_OK;
@@ -402,8 +420,11 @@ extern "C" int glsu_dpra_per_frame_device(glsu_dpra *h, const void *d_img, int i
     cudaEvent_t *ev = h->timing ? h->ev : nullptr;
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[4], h->stream));
     GLSU_TRY(launch_dpra_ls(h->prec, img_type, d_img, h->d_phi[GLSU_PHI_REF], h->d_z, h->W, h->H, h->r, h->stream));
-    GLSU_TRY(h->wff.enqueue(h->stream, h->d_z, nullptr, 1, h->d_phi[GLSU_PHI_REF], h->d_phi[GLSU_DPHI_REF],
-                            h->d_phi[GLSU_PHI_CURR], h->d_phi[GLSU_DPHI], ev));
+    GLSU_TRY(h->wff.enqueue(h->stream, h->d_z, nullptr, h->unwrap ? 2 : 1, h->d_phi[GLSU_PHI_REF],
+                            h->d_phi[GLSU_DPHI_REF], h->d_phi[GLSU_PHI_CURR], h->d_phi[GLSU_DPHI], ev));
+    if (h->unwrap)
+        GLSU_TRY(launch_unwrap(h->prec, h->d_phi[GLSU_DPHI], h->d_phi[GLSU_DPHI_REF], h->W, h->H, h->unwrap_row,
+                               h->unwrap_col, h->stream));
     h->synced = false;
     h->frames_done++;
     if (d_dphi) {
@@ -487,12 +508,75 @@ extern "C" int glsu_dpra_device_ptr(glsu_dpra *h, int which, void **d_ptr)
     return dpra_plane(h, which, d_ptr);
 }
 
+static int dpra_pipeline_init(glsu_dpra *h)
+{
+    if (h->s_in) return GLSU_OK;
+    const size_t N = (size_t)h->W * h->H;
+    const size_t es = h->prec == GLSU_F32 ? 4 : 8;
+    GLSU_CUDA_TRY(cudaMalloc(&h->d_seq_img1, 8 * N));
+    for (int s = 0; s < 2; s++) {
+        GLSU_CUDA_TRY(cudaMalloc(&h->d_ring[s], es * N));
+        GLSU_CUDA_TRY(cudaEventCreateWithFlags(&h->ev_in[s], cudaEventDisableTiming));
+        GLSU_CUDA_TRY(cudaEventCreateWithFlags(&h->ev_comp[s], cudaEventDisableTiming));
+        GLSU_CUDA_TRY(cudaEventCreateWithFlags(&h->ev_out[s], cudaEventDisableTiming));
+    }
+    GLSU_CUDA_TRY(cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking));
+    GLSU_CUDA_TRY(cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking));  // set last: marks init done
+    return GLSU_OK;
+}
+
+// Frame loop of DPRA_CPU::operator() (DPRA/dpra_cpu.cpp:58-89) with the
+// host<->device copies taken off the compute stream: frame i is uploaded on
+// s_in into slot i%2 while frame i-1 computes, and its phase change is copied
+// (device to device, on the compute stream) into ring slot i%2 and downloaded
+// on s_out while frame i+1 computes.  Slot reuse waits on frame i-2's events.
+static int dpra_sequence_pipelined(glsu_dpra *h, int nframes, const char *h_frames, size_t in_bytes,
+                                   int img_type, char *h_out, double *time_ms)
+{
+    GLSU_TRY(dpra_pipeline_init(h));
+    const size_t out_bytes = (h->prec == GLSU_F32 ? 4 : 8) * (size_t)h->W * h->H;
+    void *d_slot[2] = {h->d_img, h->d_seq_img1};
+    GLSU_CUDA_TRY(cudaEventRecord(h->t0, h->stream));
+    GLSU_CUDA_TRY(cudaStreamWaitEvent(h->s_in, h->t0, 0));  // earlier work on the compute stream first
+    for (int i = 0; i < nframes; i++) {
+        const int s = i & 1;
+        if (i >= 2) GLSU_CUDA_TRY(cudaStreamWaitEvent(h->s_in, h->ev_comp[s], 0));
+        GLSU_CUDA_TRY(cudaMemcpyAsync(d_slot[s], h_frames + in_bytes * i, in_bytes, cudaMemcpyHostToDevice, h->s_in));
+        GLSU_CUDA_TRY(cudaEventRecord(h->ev_in[s], h->s_in));
+        GLSU_CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_in[s], 0));
+        if (i >= 2) GLSU_CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_out[s], 0));
+        GLSU_TRY(glsu_dpra_per_frame_device(h, d_slot[s], img_type, h->d_ring[s]));
+        GLSU_CUDA_TRY(cudaEventRecord(h->ev_comp[s], h->stream));
+        GLSU_CUDA_TRY(cudaStreamWaitEvent(h->s_out, h->ev_comp[s], 0));
+        GLSU_CUDA_TRY(cudaMemcpyAsync(h_out + out_bytes * i, h->d_ring[s], out_bytes, cudaMemcpyDeviceToHost, h->s_out));
+        GLSU_CUDA_TRY(cudaEventRecord(h->ev_out[s], h->s_out));
+        if (i % h->rr == 0) GLSU_TRY(glsu_dpra_update_ref_phi(h));
+    }
+    // the compute stream is done with the last frame once s_out has its copy
+    GLSU_CUDA_TRY(cudaEventRecord(h->t1, h->s_out));
+    GLSU_CUDA_TRY(cudaStreamWaitEvent(h->stream, h->t1, 0));
+    GLSU_TRY(h->wff.check_device_error(h->stream));
+    GLSU_CUDA_TRY(cudaEventSynchronize(h->t1));
+    if (time_ms) {
+        float ms = 0;
+        GLSU_CUDA_TRY(cudaEventElapsedTime(&ms, h->t0, h->t1));
+        *time_ms = ms;
+    }
+    return GLSU_OK;
+}
+
 extern "C" int glsu_dpra_sequence(glsu_dpra *h, int nframes, const void *h_frames, int img_type, void *h_dphi_all,
                                   double *time_ms)
 {
     if (!h || !h_frames || !h_dphi_all || nframes < 0) return fail(GLSU_ERR_INVALID, "bad argument");
+    GLSU_TRY(dpra_check_type(h, img_type));
     const size_t N = (size_t)h->W * h->H;
     const size_t es = h->prec == GLSU_F32 ? 4 : 8;
+    if (nframes > 0 && is_pinned(h_frames) && is_pinned(h_dphi_all) &&
+        is_pinned((const char *)h_frames + elem_size(img_type) * N * nframes - 1) &&
+        is_pinned((const char *)h_dphi_all + es * N * nframes - 1))
+        return dpra_sequence_pipelined(h, nframes, (const char *)h_frames, elem_size(img_type) * N, img_type,
+                                       (char *)h_dphi_all, time_ms);
     double total = 0;
     for (int i = 0; i < nframes; i++) {
         double t = 0;
@@ -503,6 +587,24 @@ extern "C" int glsu_dpra_sequence(glsu_dpra *h, int nframes, const void *h_frame
     }
     if (time_ms) *time_ms = total;
     return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_set_unwrap(glsu_dpra *h, int enable, int start_row, int start_col)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    if (start_row >= h->H || start_col >= h->W) return fail(GLSU_ERR_INVALID, "unwrap start outside the image");
+    if (h->W > 4096 || h->H > 4096) return fail(GLSU_ERR_UNSUPPORTED, "unwrap supports sides up to 4096");
+    h->unwrap = enable != 0;
+    h->unwrap_row = start_row;
+    h->unwrap_col = start_col;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_unwrap2_device(int precision, void *d_p, int width, int height, int start_row, int start_col,
+                                   void *cuda_stream)
+{
+    if (!d_p) return fail(GLSU_ERR_INVALID, "null argument");
+    return launch_unwrap(precision, d_p, nullptr, width, height, start_row, start_col, (cudaStream_t)cuda_stream);
 }
 
 extern "C" int glsu_dpra_stage_timing(glsu_dpra *h, int enable)

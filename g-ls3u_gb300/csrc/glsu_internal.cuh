@@ -119,6 +119,9 @@ int launch_dpra_ls(int prec, int img_type, const void *d_img, const void *d_phir
                    int r, cudaStream_t s);
 int launch_dpra_update(int prec, const void *d_filtered, const void *phiref, const void *dphiref,
                        void *phicurr, void *dphi, int n, cudaStream_t s);
+// Line-scanning unwrapping in place; d_add (optional) is added to every
+// element; negative starts select MATLAB's default (the image centre).
+int launch_unwrap(int prec, void *d_p, const void *d_add, int W, int H, int row0, int col0, cudaStream_t s);
 
 // AIA
 struct AiaDev {

@@ -104,6 +104,21 @@ template <typename T> __device__ __forceinline__ C2<T> mk(T x, T y)
     return r;
 }
 
+// acc += g * v for a real tap g and a complex v: two scalar FMAs, whose tap
+// operand comes straight from the kernel-parameter bank.  (The packed
+// __ffma2_rn needs {g, g} in a register pair; with 2S+1 = 61 taps that cost a
+// move per FMA and made the 1024^2 column sweep 2.9x slower, 16.2 vs 5.5 ms.)
+__device__ __forceinline__ void cfma(float2 &acc, float g, float2 v)
+{
+    acc.x = fmaf(g, v.x, acc.x);
+    acc.y = fmaf(g, v.y, acc.y);
+}
+__device__ __forceinline__ void cfma(double2 &acc, double g, double2 v)
+{
+    acc.x = fma(g, v.x, acc.x);
+    acc.y = fma(g, v.y, acc.y);
+}
+
 // ---------------------------------------------------------------------------
 // geometry
 // ---------------------------------------------------------------------------
@@ -121,19 +136,24 @@ template <typename T, int S> struct RowGeom {
 };
 
 template <typename T, int S> struct ColGeom {
+    // 8 warps; FP32 tiles of 128 output rows (the first filter recomputes a
+    // 2S-row halo, 1.47x at S = 30).  A 16-warp, 256-row variant cut that to
+    // 1.23x but ran no faster: at 128 registers per thread it spills.
+    static constexpr int WARPS = 8;
+    static constexpr int THREADS = 32 * WARPS;
     static constexpr int TY = (sizeof(T) == 4) ? 128 : (S <= 30 ? 64 : 32);  // output rows per CTA
     static constexpr int ROWS_U = TY + 2 * S;                                // rows of u / t
-    static constexpr int KU = (ROWS_U + 7) / 8;                              // u rows per warp
-    static constexpr int KC = TY / 8;                                        // output rows per warp
+    static constexpr int KU = (ROWS_U + WARPS - 1) / WARPS;                  // u rows per warp
+    static constexpr int KC = TY / WARPS;                                    // output rows per warp
     static constexpr int ROWS_R = TY + 4 * S;                                // rows of R needed
     static constexpr int BOX = (sizeof(T) == 4) ? 64 : 16;                   // rows per TMA box
     static constexpr int NBOX = (ROWS_R + BOX - 1) / BOX;
-    static constexpr int RT = (NBOX * BOX > 8 * KU + 2 * S) ? NBOX * BOX : 8 * KU + 2 * S;
-    static constexpr int TT = 8 * KU;
+    static constexpr int RT = (NBOX * BOX > WARPS * KU + 2 * S) ? NBOX * BOX : WARPS * KU + 2 * S;
+    static constexpr int TT = WARPS * KU;
     static constexpr int FPC = (int)(sizeof(C2<T>) / 4);  // floats per complex element
     static constexpr uint32_t TX_BYTES = (uint32_t)(NBOX * BOX * 32 * sizeof(C2<T>));
     static constexpr size_t SMEM = sizeof(C2<T>) * (size_t)(RT + TT) * 32 + 16;
-    static constexpr int MINB = 1;
+    static_assert(SMEM <= 227 * 1024, "column tile exceeds shared memory");
 };
 
 // ---------------------------------------------------------------------------
@@ -206,7 +226,7 @@ __global__ void __launch_bounds__(256) wff_rows_demod_kernel(const C2<T> *__rest
 // B: column sweep over all wy for one wx and one 32-column tile
 // ---------------------------------------------------------------------------
 template <typename T, int S>
-__global__ void __launch_bounds__(256, ColGeom<T, S>::MINB)
+__global__ void __launch_bounds__(ColGeom<T, S>::THREADS, 1)
     wff_cols_kernel(const __grid_constant__ CUtensorMap tmR, C2<T> *__restrict__ Cout,
                     const C2<T> *__restrict__ ey, int nfy, int H, int pitch, const T *__restrict__ thr_ptr,
                     Taps<T, S> gA, Taps<T, S> gB, int *__restrict__ err)
@@ -230,7 +250,7 @@ __global__ void __launch_bounds__(256, ColGeom<T, S>::MINB)
         for (int b = 0; b < G::NBOX; b++)
             tma_load_3d(Rt + b * G::BOX * 32, &tmR, bar, x0 * G::FPC, y0 - 2 * S + b * G::BOX, i);
     }
-    for (int e = G::NBOX * G::BOX * 32 + tid; e < G::RT * 32; e += 256) Rt[e] = mk<T>(0, 0);
+    for (int e = G::NBOX * G::BOX * 32 + tid; e < G::RT * 32; e += G::THREADS) Rt[e] = mk<T>(0, 0);
     const bool late = !mbar_wait_bounded(bar, 0);
     if (__syncthreads_or(late)) {
         if (tid == 0) {
@@ -256,12 +276,9 @@ __global__ void __launch_bounds__(256, ColGeom<T, S>::MINB)
         // ---- pass 1: u over rows y0-S .. y0+TY+S-1, threshold into tt ----
         {
             const int q0 = w * G::KU;
-            T ar[G::KU], ai[G::KU];
+            C2<T> a[G::KU];
 #pragma unroll
-            for (int kk = 0; kk < G::KU; kk++) {
-                ar[kk] = 0;
-                ai[kk] = 0;
-            }
+            for (int kk = 0; kk < G::KU; kk++) a[kk] = mk<T>(0, 0);
 #pragma unroll
             for (int j = 0; j < G::KU + 2 * S; j++) {
                 const int q = q0 + j;
@@ -269,15 +286,11 @@ __global__ void __launch_bounds__(256, ColGeom<T, S>::MINB)
                 int gr = y0 - 2 * S + q;
                 gr = min(max(gr, -kPhasorPad), H - 1 + kPhasorPad);
                 const C2<T> p = __ldg(eyk + gr);
-                const T dx = r.x * p.x - r.y * p.y;
-                const T dy = r.x * p.y + r.y * p.x;
+                const C2<T> d = mk<T>(r.x * p.x - r.y * p.y, r.x * p.y + r.y * p.x);
 #pragma unroll
                 for (int kk = 0; kk < G::KU; kk++) {
                     const int m = j - kk;
-                    if (m >= 0 && m <= 2 * S) {
-                        ar[kk] = fma(gA.g[m], dx, ar[kk]);
-                        ai[kk] = fma(gA.g[m], dy, ai[kk]);
-                    }
+                    if (m >= 0 && m <= 2 * S) cfma(a[kk], gA.g[m], d);
                 }
             }
 #pragma unroll
@@ -287,10 +300,10 @@ __global__ void __launch_bounds__(256, ColGeom<T, S>::MINB)
                     const int gr = y0 - S + lr;
                     bool keep = (gr >= 0) && (gr < H);
                     if (sizeof(T) == 8)
-                        keep = keep && (sqrt(ar[kk] * ar[kk] + ai[kk] * ai[kk]) >= thr);
+                        keep = keep && (sqrt(a[kk].x * a[kk].x + a[kk].y * a[kk].y) >= thr);
                     else
-                        keep = keep && (ar[kk] * ar[kk] + ai[kk] * ai[kk] >= thr2);
-                    tt[lr * 32 + lane] = keep ? mk<T>(ar[kk], ai[kk]) : mk<T>(0, 0);
+                        keep = keep && (a[kk].x * a[kk].x + a[kk].y * a[kk].y >= thr2);
+                    tt[lr * 32 + lane] = keep ? a[kk] : mk<T>(0, 0);
                 }
             }
         }
@@ -298,30 +311,24 @@ __global__ void __launch_bounds__(256, ColGeom<T, S>::MINB)
         // ---- pass 2: c = t (*)_y gy, C += e^{+j wy y} c ----
         {
             const int o0 = w * G::KC;
-            T cr[G::KC], ci[G::KC];
+            C2<T> c[G::KC];
 #pragma unroll
-            for (int kk = 0; kk < G::KC; kk++) {
-                cr[kk] = 0;
-                ci[kk] = 0;
-            }
+            for (int kk = 0; kk < G::KC; kk++) c[kk] = mk<T>(0, 0);
 #pragma unroll
             for (int j = 0; j < G::KC + 2 * S; j++) {
                 const C2<T> t = tt[(o0 + j) * 32 + lane];
 #pragma unroll
                 for (int kk = 0; kk < G::KC; kk++) {
                     const int m = j - kk;
-                    if (m >= 0 && m <= 2 * S) {
-                        cr[kk] = fma(gB.g[m], t.x, cr[kk]);
-                        ci[kk] = fma(gB.g[m], t.y, ci[kk]);
-                    }
+                    if (m >= 0 && m <= 2 * S) cfma(c[kk], gB.g[m], t);
                 }
             }
 #pragma unroll
             for (int kk = 0; kk < G::KC; kk++) {
                 const int gr = min(y0 + o0 + kk, H - 1);
                 const C2<T> p = __ldg(eyk + gr);  // e^{-j wy y}; multiply by its conjugate
-                cr_acc[kk] += p.x * cr[kk] + p.y * ci[kk];
-                ci_acc[kk] += p.x * ci[kk] - p.y * cr[kk];
+                cr_acc[kk] += p.x * c[kk].x + p.y * c[kk].y;
+                ci_acc[kk] += p.x * c[kk].y - p.y * c[kk].x;
             }
         }
         __syncthreads();
@@ -430,7 +437,9 @@ __global__ void __launch_bounds__(256) wff_rows_final_kernel(const C2<T> *__rest
             const T t = atan2(v.y, v.x);
             const T pr = phiref[id];
             phicurr[id] = wrap_atan2<T>(t + pr);
-            dphi[id] = dphiref[id] + t;
+            // MODE 2 leaves the wrapped change t for the spatial unwrapping,
+            // which adds dphi_ref afterwards (MatLab/fp_ls3u.m:104)
+            dphi[id] = (MODE == 1) ? dphiref[id] + t : t;
         }
     }
 }
@@ -701,7 +710,7 @@ template <typename T, int S> static int launch_cols(const WffPlan &P, cudaStream
         attr = true;
     }
     dim3 grid(P.pitch / 32, (P.H + G::TY - 1) / G::TY, P.nfx);
-    wff_cols_kernel<T, S><<<grid, 256, G::SMEM, s>>>(P.tmR, (C2<T> *)P.d_C, (const C2<T> *)P.d_ey, P.nfy, P.H,
+    wff_cols_kernel<T, S><<<grid, G::THREADS, G::SMEM, s>>>(P.tmR, (C2<T> *)P.d_C, (const C2<T> *)P.d_ey, P.nfy, P.H,
                                                        P.pitch, (const T *)P.d_thr,
                                                        make_taps<T, S>(P.gy, P.sy, P.inv_norm),
                                                        make_taps<T, S>(P.gy, P.sy, 1.0), P.d_err);
@@ -765,8 +774,9 @@ static int enqueue_t(WffPlan &P, cudaStream_t s, const void *d_f, void *d_out, i
     if (rc) return rc;
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[2], s));
 #define GLSU_FINAL(SS)                                                                              \
-    rc = mode == 0 ? launch_final<T, SS, 0>(P, d_out, phiref, dphiref, phicurr, dphi, s)            \
-                   : launch_final<T, SS, 1>(P, d_out, phiref, dphiref, phicurr, dphi, s);
+    rc = mode == 0   ? launch_final<T, SS, 0>(P, d_out, phiref, dphiref, phicurr, dphi, s)          \
+         : mode == 1 ? launch_final<T, SS, 1>(P, d_out, phiref, dphiref, phicurr, dphi, s)          \
+                     : launch_final<T, SS, 2>(P, d_out, phiref, dphiref, phicurr, dphi, s);
     switch (P.sxi) {
     case 12: GLSU_FINAL(12) break;
     case 20: GLSU_FINAL(20) break;

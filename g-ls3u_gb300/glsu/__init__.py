@@ -110,6 +110,8 @@ def lib() -> ctypes.CDLL:
             "glsu_wff_threshold": ([c_void_p, dblp], c_int),
             "glsu_wff_set_method": ([c_void_p, c_int], c_int),
             "glsu_dpra_set_method": ([c_void_p, c_int], c_int),
+            "glsu_dpra_set_unwrap": ([c_void_p, c_int, c_int, c_int], c_int),
+            "glsu_unwrap2_device": ([c_int, c_void_p, c_int, c_int, c_int, c_int, c_void_p], c_int),
             "glsu_wff_padded_size": ([c_void_p, intp, intp], c_int),
             "glsu_wff_run_noalloc": ([c_int, c_int, prm, c_void_p, c_void_p, c_void_p], c_int),
             "glsu_dpra_create": ([pp, c_int, c_void_p, c_int, c_int, c_int, c_int, prm], c_int),
@@ -174,6 +176,13 @@ def random_deltas(M: int, seed: int) -> np.ndarray:
     d = np.zeros(M, np.float32)
     check(lib().glsu_aia_random_deltas(M, ctypes.c_uint64(seed), d.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
     return d
+
+
+def unwrap2_device(precision, d_p: int, width: int, height: int, start_row: int = -1, start_col: int = -1,
+                   stream: int = 0):
+    """Line-scanning unwrapping (MatLab/fp_unwrapping.m) of a device phase map, in place."""
+    check(lib().glsu_unwrap2_device(_prec(precision), ctypes.c_void_p(d_p), width, height, start_row, start_col,
+                                    ctypes.c_void_p(stream) if stream else None))
 
 
 def _prec(p) -> int:
@@ -301,6 +310,16 @@ class DPRA:
                                        ctypes.byref(t)))
         return out, t.value
 
+    def sequence_ptr(self, nframes: int, h_frames_ptr: int, img_type: int, h_out_ptr: int) -> float:
+        """Sequence over raw host pointers.  When both buffers are page-locked
+        (e.g. ``torch.empty(..., pin_memory=True)``) the uploads and downloads
+        overlap the compute of neighbouring frames; the returned time is then
+        the device time from the first upload to the last download."""
+        t = ctypes.c_double(0)
+        check(lib().glsu_dpra_sequence(self._h, nframes, ctypes.c_void_p(h_frames_ptr), img_type,
+                                       ctypes.c_void_p(h_out_ptr), ctypes.byref(t)))
+        return t.value
+
     def get(self, which: int) -> np.ndarray:
         out = np.empty((self.height, self.width), self.dtype)
         check(lib().glsu_dpra_get(self._h, which, _ptr(out)))
@@ -320,6 +339,10 @@ class DPRA:
     def set_method(self, method: int):
         """Column-sweep method of the WFF2: METHOD_AUTO, METHOD_DIRECT or METHOD_FFT."""
         check(lib().glsu_dpra_set_method(self._h, method))
+
+    def set_unwrap(self, enable: bool = True, start_row: int = -1, start_col: int = -1):
+        """dphi = dphi_ref + unwrap(t) (MatLab/fp_ls3u.m:104) instead of dphi_ref + t."""
+        check(lib().glsu_dpra_set_unwrap(self._h, int(enable), start_row, start_col))
 
     def stage_timing(self, enable: bool = True):
         check(lib().glsu_dpra_stage_timing(self._h, int(enable)))

@@ -161,7 +161,13 @@ int glsu_dpra_update_ref_phi(glsu_dpra *h);
  * per_frame, store its dphi, update the reference when i % rr == 0
  * (DPRA/dpra_cpu.cpp:58-89; the CUDA reference's overloads are empty,
  * DPRA/dpra_cudaf.cu:193-205).  h_frames: nframes*W*H host frames;
- * h_dphi_all: nframes*W*H host output. */
+ * h_dphi_all: nframes*W*H host output.  When both buffers are page-locked
+ * (cudaHostAlloc / cudaHostRegister / pinned tensors) the uploads and
+ * downloads run on two copy streams of the handle, overlapped with the
+ * compute of neighbouring frames, and *time_ms is the device time from the
+ * first upload to the last download; otherwise frames go one by one through
+ * glsu_dpra_per_frame and *time_ms is the sum of their times.  Results are
+ * the same either way.  Returns when every output is on the host. */
 int glsu_dpra_sequence(glsu_dpra *h, int nframes, const void *h_frames, int img_type, void *h_dphi_all,
                        double *time_ms);
 /* Copy a state plane (GLSU_PHI_*) to the host. */
@@ -171,6 +177,12 @@ int glsu_dpra_get(glsu_dpra *h, int which, void *h_out);
 int glsu_dpra_get_lsq(glsu_dpra *h, void *h_out);
 /* Device address of a state plane (valid until the next call on h). */
 int glsu_dpra_device_ptr(glsu_dpra *h, int which, void **d_ptr);
+/* Spatially unwrap each frame's phase change before adding it to dphi_ref,
+ * dphi = dphi_ref + unwrap(t), as MatLab/fp_ls3u.m:104 does; off by default
+ * (the C++ reference adds the wrapped t, DPRA/dpra_cpu.cpp:248).  Starts are
+ * 0-based; negative selects MATLAB's default (the image centre).  Sides up
+ * to 4096. */
+int glsu_dpra_set_unwrap(glsu_dpra *h, int enable, int start_row, int start_col);
 /* Column-sweep method of the handle's WFF2 (GLSU_METHOD_*). */
 int glsu_dpra_set_method(glsu_dpra *h, int method);
 /* Record CUDA events between the stages of each frame (off by default). */
@@ -179,6 +191,15 @@ int glsu_dpra_stage_timing(glsu_dpra *h, int enable);
  * row pass, [2] WFF column sweep, [3] WFF final row pass + phase update.
  * Returns the number of stages written. */
 int glsu_dpra_stage_times(glsu_dpra *h, float *ms, int n);
+
+/* ---- spatial unwrapping: MatLab/fp_unwrapping.m ------------------------- */
+/* Line-scanning unwrapping of a device H*W phase map (precision GLSU_F32 or
+ * GLSU_F64) in place: the column start_col is unwrapped from start_row, then
+ * every row from start_col (fp_unwrapping.m:59-71).  0-based starts;
+ * negative selects MATLAB's default round(m/2), round(n/2).  Sides up to
+ * 4096.  Enqueued on the stream (NULL: legacy default stream). */
+int glsu_unwrap2_device(int precision, void *d_p, int width, int height, int start_row, int start_col,
+                        void *cuda_stream);
 
 /* ---- AIA: AIA_CUDAF ----------------------------------------------------- */
 /* M frames of cols x rows pixels. */

@@ -14,6 +14,7 @@
  *   - DPRA phase update:                              DPRA/dpra_cpu.cpp:243-258
  *   - AIA alternating least squares:                  AIA/aia_cpu.cpp:16-263
  *   - ifftshift-ed integer frequency grid:            Test/xfyf_2D_1D_Test.cu:48-108 (golden Test/xfyf.csv)
+ *   - line-scanning spatial unwrapping:               MatLab/fp_unwrapping.m:41-71
  *
  * Documented deviations (all FP64 throughout):
  *   - DPRA/dpra_cpu.cpp:246 truncates atan2 of the filtered value to float; here it stays double.
@@ -702,4 +703,26 @@ int or_aia(int M, int N, const double *f, double *delta, int max_iter, double ma
     free(x);
     free(old);
     return info;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Line-scanning spatial unwrapping -- MatLab/fp_unwrapping.m:41-71 (the    */
+/* MATLAB spec; the C++ reference omits it).  p: H*W row-major, in place;   */
+/* start_row/start_col are 0-based.  round() is MATLAB's (half away from 0). */
+/* ------------------------------------------------------------------------ */
+static void unwrap1(double *p, int n, size_t stride, int s)
+{
+    const double tp = 2.0 * M_PI;
+    for (int i = s + 1; i < n; i++)
+        p[i * stride] += round((p[(i - 1) * stride] - p[i * stride]) / tp) * tp;
+    for (int i = s - 1; i >= 0; i--)
+        p[i * stride] += round((p[(i + 1) * stride] - p[i * stride]) / tp) * tp;
+}
+
+void or_unwrap2(int W, int H, double *p, int start_row, int start_col)
+{
+    /* seed column, from start_row (fp_unwrapping.m:66) */
+    unwrap1(p + start_col, H, (size_t)W, start_row);
+    /* every row from start_col (fp_unwrapping.m:68-70) */
+    for (int i = 0; i < H; i++) unwrap1(p + (size_t)i * W, W, 1, start_col);
 }

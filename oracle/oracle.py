@@ -62,6 +62,7 @@ def lib():
             L.or_dpra_update.argtypes = [c_int, dp, dp, dp, dp, dp]
             L.or_aia_phi_solve.argtypes = [c_int, c_int, dp, dp, dp, dp]
             L.or_aia.argtypes = [c_int, c_int, dp, dp, c_int, c_double, dp, ip, dp]
+            L.or_unwrap2.argtypes = [c_int, c_int, dp, c_int, c_int]
             _lib = L
     return _lib
 
@@ -204,6 +205,19 @@ def aia(frames, deltas, max_iter=20, max_err=1e-4):
     if info:
         raise ValueError("matrix not positive definite")
     return phi.reshape(f.shape[1:]), d, it.value, err.value
+
+
+def unwrap2(p, start_row=None, start_col=None):
+    """Line-scanning unwrapping of MatLab/fp_unwrapping.m (0-based starts;
+    default: MATLAB's round(m/2), round(n/2) converted to 0-based)."""
+    a = _f64(p).copy()
+    H, W = a.shape
+    if start_row is None:
+        start_row = int(np.floor(H / 2 + 0.5)) - 1
+    if start_col is None:
+        start_col = int(np.floor(W / 2 + 0.5)) - 1
+    lib().or_unwrap2(W, H, _dp(a), int(start_row), int(start_col))
+    return a
 
 
 class WffParams:

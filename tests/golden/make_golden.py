@@ -10,6 +10,10 @@ script writes:
 - ``fft_lut.json``: the FFT size table of ``WFT/WFT.h:18-32``.
 - ``xfyf.npz``: the ifftshift-ed integer frequency grid printed by the
   reference's GPU test into ``Test/xfyf.csv`` (64 x 50 plane).
+- ``phi_1.bin``: the reference's phase map ``Experiments/imgs/1/1_phi.bin``,
+  byte for byte: the ``matrixIO`` binary format (int32 rows, int32 cols,
+  row-major float32), which pins the readers in ``glsu/io.py`` and
+  ``include/glsu_io.hpp``.
 - ``aia_bmp.npz``: the three 256x256 fringe frames ``Test/{1,2,3}.bmp``
   (decoded top-down, as OpenCV's imread + BGR2GRAY does for these 8-bit
   grey-palette files), the initial deltas used by the reference's AIA tests
@@ -95,6 +99,9 @@ def main(ref: str) -> None:
     np.savez_compressed(os.path.join(HERE, "aia_bmp.npz"), frames=frames,
                         deltas0=np.array([0.8622, 0.3188, -1.3077], np.float32),
                         pix=idx.astype(np.int32), x=x[idx])
+    # 4. matrixIO phase map, copied as is
+    raw = open(os.path.join(ref, "Experiments", "imgs", "1", "1_phi.bin"), "rb").read()
+    open(os.path.join(HERE, "phi_1.bin"), "wb").write(raw)
     print("wrote fixtures to", HERE)
 
 

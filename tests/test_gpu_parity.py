@@ -203,6 +203,46 @@ def test_reference_update_rate_semantics(glsu, oracle, synth):
     assert np.array_equal(dps, np.stack(ref))
 
 
+@pytest.mark.parametrize("prec,rr,img", [("f32", 1, "f32"), ("f32", 3, "u8"), ("f64", 2, "f64")])
+def test_pipelined_sequence_equals_frame_loop(glsu, synth, prec, rr, img):
+    """Pinned host buffers take the copy-overlapped sequence path; it must give
+    the per-frame loop's results bit for bit (same kernels, same order)."""
+    torch = _torch()
+    frames, phi0, _ = synth.sequence(96, 128, 7, seed=5)
+    wp = glsu.WffParams(6.0, -1.0, 1.0, 0.25, 6.0, -1.0, 1.0, 0.25, -1)
+    dt = np.float32 if prec == "f32" else np.float64
+    if img == "u8":
+        fr = np.clip(np.round(frames * 255), 0, 255).astype(np.uint8)
+    else:
+        fr = frames.astype(np.float32 if img == "f32" else np.float64)
+    d = glsu.DPRA(phi0.astype(dt), rr, 3, prec, wp)
+    ref = []
+    for i, f in enumerate(fr):
+        ref.append(d.per_frame(f)[0])
+        if i % rr == 0:
+            d.update_ref_phi()
+    ref_state = d.get(glsu.PHI_REF)
+    d.close()
+    tf = torch.from_numpy(fr).pin_memory()
+    out = torch.empty((fr.shape[0],) + fr.shape[1:], dtype=torch.float32 if prec == "f32" else torch.float64)
+    out = out.pin_memory()
+    d = glsu.DPRA(phi0.astype(dt), rr, 3, prec, wp)
+    itype = {"u8": glsu.U8, "f32": glsu.F32, "f64": glsu.F64}[img]
+    ms = d.sequence_ptr(fr.shape[0], tf.data_ptr(), itype, out.data_ptr())
+    assert ms > 0
+    assert np.array_equal(out.numpy(), np.stack(ref))
+    assert np.array_equal(d.get(glsu.PHI_REF), ref_state)
+    # a second sequence on the same handle continues from the updated state
+    ms2 = d.sequence_ptr(2, tf.data_ptr(), itype, out.data_ptr())
+    d.close()
+    d = glsu.DPRA(phi0.astype(dt), rr, 3, prec, wp)
+    seq_np, _ = d.sequence(fr)
+    more, _ = d.sequence(np.ascontiguousarray(fr[:2]))
+    d.close()
+    assert ms2 > 0 and np.array_equal(out.numpy()[:2], more)
+    assert np.array_equal(seq_np, np.stack(ref))
+
+
 def test_aia_reference_bmp_frames(glsu, oracle):
     """AIA on the reference's own test frames Test/{1,2,3}.bmp with the
     deltas of its tests (uint8 path, as AIA_CUDAF receives cv::Mat CV_8UC1)."""
@@ -270,4 +310,44 @@ def test_error_codes_on_device(glsu):
     d = glsu.DPRA(np.zeros((16, 16), np.float32), 1, 1, "f32", glsu.WffParams(2.0, -1, 1, 1, 2.0, -1, 1, 1, 0.1))
     with pytest.raises((TypeError, glsu.GlsuError)):
         d.per_frame(np.zeros((16, 16), np.int16))
+    d.close()
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("shape,start", [((64, 80), (-1, -1)), ((37, 300), (19, 19)), ((1, 50), (0, 49)),
+                                         ((200, 1), (5, 0)), ((512, 384), (0, 383))])
+def test_unwrap_matches_oracle(glsu, oracle, prec, shape, start):
+    torch = _torch()
+    rng = np.random.default_rng(shape[0] * 7 + shape[1])
+    y, x = np.mgrid[0:shape[0], 0:shape[1]]
+    true = 0.5 * x - 0.35 * y + 3 * np.sin(x / 11.0) * np.cos(y / 13.0) + 0.3 * rng.standard_normal(shape)
+    w = np.angle(np.exp(1j * true))
+    dt = np.float32 if prec == "f32" else np.float64
+    t = torch.from_numpy(w.astype(dt)).cuda()
+    glsu.unwrap2_device(prec, t.data_ptr(), shape[1], shape[0], *start)
+    torch.cuda.synchronize()
+    got = t.cpu().numpy().astype(np.float64)
+    sr, sc = start
+    ref = oracle.unwrap2(w.astype(dt).astype(np.float64), None if sr < 0 else sr, None if sc < 0 else sc)
+    k = np.round((got - ref) / (2 * np.pi))
+    print("unwrap %s %s: 2pi-count mismatches %d, max diff %.3g" % (prec, shape, int((k != 0).sum()),
+                                                                   np.abs(got - ref).max()))
+    assert (k == 0).all()
+    assert np.abs(got - ref).max() < (1e-4 if prec == "f32" else 1e-10) * max(1, np.abs(ref).max())
+
+
+def test_dpra_with_unwrapping_matches_matlab_semantics(glsu, oracle, synth):
+    """dphi = dphi_ref + unwrap(angle(filtered)) (MatLab/fp_ls3u.m:104)."""
+    frames, phi0, _ = synth.sequence(64, 72, 3, seed=8)
+    wp = glsu.WffParams(4.0, -1.0, 1.0, 0.5, 4.0, -1.0, 1.0, 0.5, 0.3)
+    d = glsu.DPRA(phi0, 1, 2, "f64", wp)
+    d.set_unwrap(True, 19, 19)
+    for fr in frames[1:]:
+        pref = d.get(glsu.PHI_REF)
+        dref = d.get(glsu.DPHI_REF)
+        dphi, _ = d.per_frame(fr.astype(np.float64))
+        _, _, _, filt = oracle.glsu_frame(fr.astype(np.float64), pref, dref, 2, oracle.WffParams(*wp.tuple()))
+        ref = dref + oracle.unwrap2(np.angle(filt), 19, 19)
+        assert np.abs(dphi - ref).max() < 1e-9
+        d.update_ref_phi()
     d.close()

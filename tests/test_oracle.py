@@ -182,3 +182,38 @@ def test_dpra_stable_and_literal_forms_agree_where_well_posed(oracle, synth):
         good = kap > 1e-3
         assert good.mean() > 0.2
         assert e[good].max() < 1e-9, (r, e[good].max())
+
+
+def unwrap_matlab(p, sx, sy):
+    """Loop restatement of MatLab/fp_unwrapping.m:41-71 (0-based starts)."""
+    p = np.array(p, np.float64)
+    m, n = p.shape
+
+    def u1(v, s):
+        v = v.copy()
+        for i in range(s + 1, len(v)):
+            v[i] += np.trunc((v[i - 1] - v[i]) / 2 / np.pi + np.copysign(0.5, (v[i - 1] - v[i]))) * 2 * np.pi
+        for i in range(s - 1, -1, -1):
+            v[i] += np.trunc((v[i + 1] - v[i]) / 2 / np.pi + np.copysign(0.5, (v[i + 1] - v[i]))) * 2 * np.pi
+        return v
+    p[:, sy] = u1(p[:, sy], sx)
+    for i in range(m):
+        p[i, :] = u1(p[i, :], sy)
+    return p
+
+
+@pytest.mark.parametrize("shape,start", [((40, 50), (10, 20)), ((33, 17), (0, 0)), ((1, 30), (0, 29)),
+                                         ((25, 1), (12, 0))])
+def test_unwrap_matches_matlab_loops(oracle, shape, start):
+    rng = np.random.default_rng(sum(shape))
+    y, x = np.mgrid[0:shape[0], 0:shape[1]]
+    true = 0.4 * x - 0.3 * y + 2 * np.sin(x / 7.0) + 0.2 * rng.standard_normal(shape)
+    w = np.angle(np.exp(1j * true))
+    a = oracle.unwrap2(w, *start)
+    b = unwrap_matlab(w, *start)
+    assert np.array_equal(a, b)
+    # a smooth field is recovered up to one 2pi offset
+    smooth = np.angle(np.exp(1j * (0.4 * x - 0.3 * y)))
+    u = oracle.unwrap2(smooth, *start)
+    d = u - (0.4 * x - 0.3 * y)
+    assert np.allclose(d, d[start], atol=1e-12)
