@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "glsu_internal.cuh"
+#include "sur_net.cuh"
 
 namespace glsu {
 
@@ -82,7 +83,15 @@ struct glsu_dpra {
     cudaStream_t s_in = nullptr, s_out = nullptr;
     void *d_seq_img1 = nullptr, *d_ring[2] = {nullptr, nullptr};
     cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
+    // surrogate form: network output, probes, per-tile fallback
+    SurNet *sur = nullptr;
+    void *d_filt = nullptr;  // complex H*W: the filtered field (surrogate, then fallback tiles)
+    int sur_tile = 0, sur_patch = 0, sur_ntx = 0, sur_nty = 0;
+    double sur_tol = 0;
+    ProbeOut probe;
 };
+
+static void dpra_surrogate_release(glsu_dpra *h);
 
 struct glsu_aia {
     int M = 0, cols = 0, rows = 0, N = 0;
@@ -389,6 +398,7 @@ extern "C" int glsu_dpra_destroy(glsu_dpra *h)
     }
     if (h->s_in) cudaStreamDestroy(h->s_in);
     if (h->s_out) cudaStreamDestroy(h->s_out);
+    dpra_surrogate_release(h);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return GLSU_OK;
@@ -413,6 +423,111 @@ static int dpra_check_type(glsu_dpra *h, int img_type)
     return fail(GLSU_ERR_INVALID, "frame type must be GLSU_U8, GLSU_F32 or (FP64 handles) GLSU_F64");
 }
 
+static void dpra_surrogate_release(glsu_dpra *h)
+{
+    if (h->sur) {
+        h->sur->release();
+        delete h->sur;
+        h->sur = nullptr;
+    }
+    cudaFree(h->d_filt);
+    cudaFree(h->probe.partial);
+    cudaFree(h->probe.sites);
+    cudaFree(h->probe.resid);
+    cudaFree(h->probe.flags);
+    cudaFree(h->probe.counts);
+    h->d_filt = nullptr;
+    h->probe = ProbeOut();
+}
+
+// Surrogate form of one frame after the LS stage (d_z): network -> probes ->
+// plain WFF2 on flagged tiles -> phase update.  Stage events: after the
+// network, after the probes, after fallback and update.
+static int dpra_surrogate_frame(glsu_dpra *h, cudaEvent_t *ev)
+{
+    if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[0], h->stream));
+    h->sur->stream = h->stream;
+    GLSU_TRY(h->sur->forward(h->d_z, h->d_filt));
+    if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[1], h->stream));
+    if (h->sur_tol > 0) {
+        GLSU_TRY(h->wff.enqueue_probe(h->stream, h->d_z, h->d_filt, h->sur_tile, h->sur_patch,
+                                      (uint32_t)h->frames_done, h->sur_tol, h->probe));
+        if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[2], h->stream));
+        TileMask m;
+        m.flags = h->probe.flags;
+        m.tile = h->sur_tile;
+        m.ntx = h->sur_ntx;
+        m.nty = h->sur_nty;
+        h->wff.mask = m;
+        const int rc = h->wff.enqueue(h->stream, h->d_z, h->d_filt, 0, nullptr, nullptr, nullptr, nullptr, nullptr);
+        h->wff.mask = TileMask();
+        GLSU_TRY(rc);
+    } else if (ev) {
+        GLSU_CUDA_TRY(cudaEventRecord(ev[2], h->stream));
+    }
+    GLSU_TRY(launch_dpra_update(h->prec, h->d_filt, h->d_phi[GLSU_PHI_REF], h->unwrap ? nullptr : h->d_phi[GLSU_DPHI_REF],
+                                h->d_phi[GLSU_PHI_CURR], h->d_phi[GLSU_DPHI], h->W * h->H, h->stream));
+    if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[3], h->stream));
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_set_surrogate(glsu_dpra *h, const float *h_params, const int *dilations, int tile,
+                                       int patch, double tol)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    dpra_surrogate_release(h);
+    if (!h_params) return GLSU_OK;
+    if (h->prec != GLSU_F32) return fail(GLSU_ERR_UNSUPPORTED, "the surrogate form is FP32");
+    if (tol > 0 && (tile < 1 || patch < 1 || patch > kProbeMaxP || patch > tile))
+        return fail(GLSU_ERR_INVALID, "probe patch must be 1..8 and not above the tile size");
+    const size_t N = (size_t)h->W * h->H;
+    h->sur = new SurNet();
+    h->sur->stream = h->stream;
+    int rc = h->sur->init(1, h->W, h->H, dilations, false);
+    if (rc == GLSU_OK) rc = h->sur->set_params(h_params);
+    if (rc == GLSU_OK && cudaMalloc(&h->d_filt, 8 * N) != cudaSuccess) rc = fail(GLSU_ERR_ALLOC, "allocation failed");
+    h->sur_tol = tol;
+    if (rc == GLSU_OK && tol > 0) {
+        h->sur_tile = tile;
+        h->sur_patch = patch;
+        h->sur_ntx = (h->W + tile - 1) / tile;
+        h->sur_nty = (h->H + tile - 1) / tile;
+        const size_t nt = (size_t)h->sur_ntx * h->sur_nty;
+        if (cudaMalloc(&h->probe.partial, nt * h->wff.nfx * patch * patch * sizeof(float2)) != cudaSuccess ||
+            cudaMalloc(&h->probe.sites, nt * sizeof(int2)) != cudaSuccess ||
+            cudaMalloc(&h->probe.resid, nt * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&h->probe.flags, nt * sizeof(int)) != cudaSuccess ||
+            cudaMalloc(&h->probe.counts, 2 * sizeof(int)) != cudaSuccess)
+            rc = fail(GLSU_ERR_ALLOC, "allocation failed");
+        if (rc == GLSU_OK && (cudaMemset(h->probe.counts, 0, 2 * sizeof(int)) != cudaSuccess ||
+                              cudaMemset(h->probe.resid, 0, nt * sizeof(float)) != cudaSuccess))
+            rc = fail(GLSU_ERR_CUDA, "memset failed");
+    }
+    if (rc != GLSU_OK) dpra_surrogate_release(h);
+    return rc;
+}
+
+extern "C" int glsu_dpra_surrogate_stats(glsu_dpra *h, long long *tiles_probed, long long *tiles_flagged,
+                                         float *h_resid, int *h_sites)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    int c[2] = {0, 0};
+    GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (h->sur && h->probe.counts) {
+        GLSU_CUDA_TRY(cudaMemcpy(c, h->probe.counts, sizeof(c), cudaMemcpyDeviceToHost));
+        if (h_resid)
+            GLSU_CUDA_TRY(cudaMemcpy(h_resid, h->probe.resid, sizeof(float) * h->sur_ntx * h->sur_nty,
+                                     cudaMemcpyDeviceToHost));
+        if (h_sites)
+            GLSU_CUDA_TRY(cudaMemcpy(h_sites, h->probe.sites, sizeof(int2) * h->sur_ntx * h->sur_nty,
+                                     cudaMemcpyDeviceToHost));
+    }
+    if (tiles_probed) *tiles_probed = c[0];
+    if (tiles_flagged) *tiles_flagged = c[1];
+    return GLSU_OK;
+}
+
 extern "C" int glsu_dpra_per_frame_device(glsu_dpra *h, const void *d_img, int img_type, void *d_dphi)
 {
     if (!h || !d_img) return fail(GLSU_ERR_INVALID, "null argument");
@@ -420,8 +535,11 @@ extern "C" int glsu_dpra_per_frame_device(glsu_dpra *h, const void *d_img, int i
     cudaEvent_t *ev = h->timing ? h->ev : nullptr;
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[4], h->stream));
     GLSU_TRY(launch_dpra_ls(h->prec, img_type, d_img, h->d_phi[GLSU_PHI_REF], h->d_z, h->W, h->H, h->r, h->stream));
-    GLSU_TRY(h->wff.enqueue(h->stream, h->d_z, nullptr, h->unwrap ? 2 : 1, h->d_phi[GLSU_PHI_REF],
-                            h->d_phi[GLSU_DPHI_REF], h->d_phi[GLSU_PHI_CURR], h->d_phi[GLSU_DPHI], ev));
+    if (h->sur)
+        GLSU_TRY(dpra_surrogate_frame(h, ev));
+    else
+        GLSU_TRY(h->wff.enqueue(h->stream, h->d_z, nullptr, h->unwrap ? 2 : 1, h->d_phi[GLSU_PHI_REF],
+                                h->d_phi[GLSU_DPHI_REF], h->d_phi[GLSU_PHI_CURR], h->d_phi[GLSU_DPHI], ev));
     if (h->unwrap)
         GLSU_TRY(launch_unwrap(h->prec, h->d_phi[GLSU_DPHI], h->d_phi[GLSU_DPHI_REF], h->W, h->H, h->unwrap_row,
                                h->unwrap_col, h->stream));
@@ -451,6 +569,7 @@ extern "C" int glsu_dpra_per_frame(glsu_dpra *h, const void *h_img, int img_type
                                   h->stream));
     GLSU_CUDA_TRY(cudaEventRecord(h->t1, h->stream));
     GLSU_TRY(h->wff.check_device_error(h->stream));
+    if (h->sur) GLSU_TRY(h->sur->check_error());
     if (!pin_out) std::memcpy(h_dphi, h->h_out, es * N);
     if (time_ms) {
         float ms = 0;
@@ -490,6 +609,15 @@ extern "C" int glsu_dpra_get(glsu_dpra *h, int which, void *h_out)
     const size_t es = h->prec == GLSU_F32 ? 4 : 8;
     GLSU_CUDA_TRY(cudaMemcpyAsync(h_out, p, es * (size_t)h->W * h->H, cudaMemcpyDeviceToHost, h->stream));
     GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_lsq_device(glsu_dpra *h, void *d_out)
+{
+    if (!h || !d_out) return fail(GLSU_ERR_INVALID, "null argument");
+    const size_t es = h->prec == GLSU_F32 ? 4 : 8;
+    GLSU_CUDA_TRY(
+        cudaMemcpyAsync(d_out, h->d_z, 2 * es * (size_t)h->W * h->H, cudaMemcpyDeviceToDevice, h->stream));
     return GLSU_OK;
 }
 
@@ -556,6 +684,7 @@ static int dpra_sequence_pipelined(glsu_dpra *h, int nframes, const char *h_fram
     GLSU_CUDA_TRY(cudaEventRecord(h->t1, h->s_out));
     GLSU_CUDA_TRY(cudaStreamWaitEvent(h->stream, h->t1, 0));
     GLSU_TRY(h->wff.check_device_error(h->stream));
+    if (h->sur) GLSU_TRY(h->sur->check_error());
     GLSU_CUDA_TRY(cudaEventSynchronize(h->t1));
     if (time_ms) {
         float ms = 0;

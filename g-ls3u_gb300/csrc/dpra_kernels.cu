@@ -258,7 +258,7 @@ __global__ void dpra_update_kernel(const C2<T> *__restrict__ f, const T *__restr
         T s, c;
         sincos_t<T>(t + pr[i], &s, &c);
         pc[i] = atan2(s, c);
-        dp[i] = dpr[i] + t;
+        dp[i] = dpr ? dpr[i] + t : t;  // null dphi_ref: the wrapped change alone (unwrapping adds it later)
     }
 }
 

@@ -55,6 +55,36 @@ constexpr long long kSpinLimit = 1ll << 26;
 // Blocks (and partial sums) of the automatic-threshold reduction.
 constexpr int kThrBlocks = 304;
 
+// Tiles of a frame that the plain WFF2 recomputes (surrogate fallback).
+// With flags set, each WFF2 kernel CTA runs only when its output rectangle,
+// grown by (my, mx), meets a flagged tile, and the final pass writes only
+// pixels of flagged tiles.  The image border (crop) stays the full frame's.
+struct TileMask {
+    const int *flags = nullptr;  // [nty][ntx], nonzero = recompute
+    int tile = 0, ntx = 0, nty = 0;
+    int my = 0, mx = 0;  // margins of the kernel being launched
+    __device__ __forceinline__ bool any(int y0, int y1, int x0, int x1) const
+    {
+        const int ty0 = max(0, y0 - my) / tile, ty1 = min(nty - 1, (y1 - 1 + my) / tile);
+        const int tx0 = max(0, x0 - mx) / tile, tx1 = min(ntx - 1, (x1 - 1 + mx) / tile);
+        for (int ty = ty0; ty <= ty1; ty++)
+            for (int tx = tx0; tx <= tx1; tx++)
+                if (flags[ty * ntx + tx]) return true;
+        return false;
+    }
+    __device__ __forceinline__ bool at(int y, int x) const { return flags[(y / tile) * ntx + x / tile] != 0; }
+};
+
+// Exact sparse WFF2 probe: per tile one P x P patch (P <= kProbeMaxP).
+constexpr int kProbeMaxP = 8;
+struct ProbeOut {
+    float2 *partial = nullptr;  // [ntiles][nfx][P*P] per-wx partial sums
+    int2 *sites = nullptr;      // [ntiles] (row, col) of each patch
+    float *resid = nullptr;     // [ntiles] RMS phase residual of the surrogate
+    int *flags = nullptr;       // [ntiles] residual > tolerance
+    int *counts = nullptr;      // [2] cumulative: tiles probed, tiles flagged
+};
+
 // ---------------------------------------------------------------------------
 // WFF2 plan: the frequency sweep on the device (see wff_kernels.cu)
 // ---------------------------------------------------------------------------
@@ -97,6 +127,17 @@ struct WffPlan {
                 const void *dphi_ref, void *phi_curr, void *dphi, cudaEvent_t *stage_ev);
     int check_device_error(cudaStream_t s);
 
+    // Tile mask of the next enqueue (flags == nullptr: whole frame).
+    TileMask mask;
+    // Ensure the threshold on the device (automatic: from d_f, once).
+    int ensure_threshold(cudaStream_t s, const void *d_f);
+    // FP32 only: exact WFF2 of d_f on one P x P patch per tile (patch
+    // position hashed from seed and the tile), compared with d_cmp (complex,
+    // the surrogate's output): RMS phase residual over patch pixels with
+    // |WFF2| >= 0.1, flag when above tol.
+    int enqueue_probe(cudaStream_t s, const void *d_f, const void *d_cmp, int tile, int P, uint32_t seed,
+                      double tol, const ProbeOut &o);
+
     // Column sweep by shared-memory FFTs (FP32 form; see wff_colfft.cu).
     int method = GLSU_METHOD_AUTO;  // GLSU_METHOD_AUTO / DIRECT / FFT
     int fft_L = 0, fft_nst = 0;     // fft_L == 0: no FFT plan, the direct kernel runs
@@ -122,6 +163,28 @@ int launch_dpra_update(int prec, const void *d_filtered, const void *phiref, con
 // Line-scanning unwrapping in place; d_add (optional) is added to every
 // element; negative starts select MATLAB's default (the image centre).
 int launch_unwrap(int prec, void *d_p, const void *d_add, int W, int H, int row0, int col0, cudaStream_t s);
+
+// Surrogate network (sur_kernels.cu).  FP32 master parameters, per layer
+// W[co][ci][3][3] then b[co]: layer 0 (2 -> 32), layers 1..6 (32 -> 32),
+// layer 7 (32 -> 2).
+constexpr int kSurLayers = 8;
+constexpr int kSurL0Params = 32 * 2 * 9 + 32;
+constexpr int kSurL32Params = 32 * 32 * 9 + 32;
+constexpr int kSurL7Params = 2 * 32 * 9 + 2;
+constexpr int kSurParams = kSurL0Params + 6 * kSurL32Params + kSurL7Params;
+inline int sur_layer_offset(int l) { return l == 0 ? 0 : kSurL0Params + (l - 1) * kSurL32Params; }
+
+struct SurConvArgs {
+    int B = 0, H = 0, W = 0, dil = 1;
+    const uint16_t *wpack = nullptr;  // [9][4][32][8] BF16 B-operand image of the layer
+    const float *bias = nullptr;      // [32] or null
+    const uint16_t *mask = nullptr;   // [B][H][W][32]: output zeroed where mask <= 0 (null: none)
+    uint16_t *out = nullptr;          // [B][H][W][32] BF16
+    int relu = 1;
+    int *err = nullptr;
+};
+int sur_make_map(CUtensorMap *tm, const void *act, int B, int H, int W, int dil);
+int launch_sur_conv(const CUtensorMap &tm, const SurConvArgs &a, cudaStream_t s);
 
 // AIA
 struct AiaDev {

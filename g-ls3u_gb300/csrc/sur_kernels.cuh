@@ -1,0 +1,622 @@
+// sur_kernels.cuh -- kernels of the learned WFF2 surrogate on sm_103a
+// (compiled in sur_host.cu).
+//
+// Network: 8 layers of 3x3 convolutions with per-layer dilation, 32 hidden
+// channels, ReLU after layers 0..6; input and output 2 channels (re, im):
+//     x   = (Re z, Im z)                 z = exp(j dphi) of the DPRA LS stage
+//     a0  = relu(conv0(x))               2 -> 32   CUDA cores, FP32 math
+//     a_l = relu(conv_l(a_{l-1}))        32 -> 32  tcgen05, l = 1..6
+//     y   = x + conv7(a6)                32 -> 2   CUDA cores
+//     out = y / |y|                      the stand-in for WFF2(z) / |WFF2(z)|
+// Weights and activations are BF16, accumulation FP32 (TMEM for the
+// tensor-core layers).  Activations are NHWC [B][H][W][32] BF16, 64 bytes a
+// pixel.
+//
+// Tensor-core layer (sur_conv_tc_kernel): one MMA tile is 128 consecutive
+// pixels of one output row (M = 128) x 32 output channels (N = 32), and
+// K = 9 taps x 32 input channels, issued as 18 tcgen05.mma of K = 16.  The
+// input rows are loaded by TMA through a 5-D tensor map whose box is
+// {8 channels, 128 + 2d pixels, 4 channel chunks} -- in shared memory that
+// is "chunk-planar": chunk c at c * (128 + 2d) * 16 bytes, pixel p at p * 16
+// within it, i.e. the K-major no-swizzle operand layout with 8-row groups
+// 128 B apart.  A tap's horizontal offset dx * d is then just a shift of the
+// descriptor start by 16 * dx * d bytes, so the 9 taps read the same three
+// input rows without any im2col copy, and TMA zero-fills the image border.
+// A CTA walks one chain of output rows y = r, r + d, r + 2d, ... (the rows a
+// dilated tap pair shares) through a ring of input-row slots; the
+// accumulator is double-buffered in TMEM so the epilogue of row k overlaps
+// the MMAs of row k + 1.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include <cmath>
+
+#include "glsu_internal.cuh"
+#include "ptx_sm103.cuh"
+
+namespace glsu {
+
+constexpr int kSurSlots = 6;     // input-row ring of the tensor-core conv
+constexpr int kSurRows = 16;     // output rows per CTA (one chain segment)
+constexpr int kSurWBytes = 9 * 4 * 32 * 16;  // packed B operand of one layer
+
+__device__ __forceinline__ float bf2f(uint16_t v) { return __uint_as_float((uint32_t)v << 16); }
+
+__device__ __forceinline__ uint32_t pack_bf2(float lo, float hi)
+{
+    const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+__device__ __forceinline__ void unpack8(const uint4 u, float *f)
+{
+    const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        f[2 * i] = __uint_as_float(w[i] << 16);
+        f[2 * i + 1] = __uint_as_float(w[i] & 0xFFFF0000u);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// tensor-core 32 -> 32 conv (forward, or backward-data with flipped weights)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256, 2) sur_conv_tc_kernel(const __grid_constant__ CUtensorMap tm, SurConvArgs a)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const int BW = 128 + 2 * a.dil;
+    const int slot_bytes = (BW * 64 + 1023) & ~1023;
+    unsigned char *wsm = sm;
+    unsigned char *slots = sm + kSurWBytes;
+    uint64_t *full = reinterpret_cast<uint64_t *>(slots + kSurSlots * slot_bytes);
+    uint64_t *sfree = full + kSurSlots;
+    uint64_t *accf = sfree + kSurSlots;
+    uint64_t *acce = accf + 2;
+    uint64_t *drain = acce + 2;
+    float *bias_s = reinterpret_cast<float *>(drain + 1);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bias_s + 32);
+
+    // work item: (image b, 128-pixel segment sx, residue r mod d, chain chunk)
+    const int nsx = (a.W + 127) / 128;
+    const int nch = ((a.H + a.dil - 1) / a.dil + kSurRows - 1) / kSurRows;
+    int item = blockIdx.x;
+    const int ch = item % nch;
+    item /= nch;
+    const int r = item % a.dil;
+    item /= a.dil;
+    const int sxi = item % nsx;
+    const int b = item / nsx;
+    const int x0 = sxi * 128;
+    const int kbeg = ch * kSurRows;
+    const int chain_len = (a.H - r + a.dil - 1) / a.dil;  // rows r, r+d, ... below H
+    const int nout = min(kSurRows, chain_len - kbeg);
+    if (b >= a.B || nout <= 0) return;  // uniform over the CTA, before any barrier or TMEM use
+    const int nin = nout + 2;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int e = tid; e < kSurWBytes / 16; e += 256)
+        reinterpret_cast<uint4 *>(wsm)[e] = reinterpret_cast<const uint4 *>(a.wpack)[e];
+    if (tid < 32) bias_s[tid] = a.bias ? a.bias[tid] : 0.f;
+    if (tid == 0) {
+        for (int s = 0; s < kSurSlots; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&sfree[s], 1);
+        }
+        mbar_init(&accf[0], 1);
+        mbar_init(&accf[1], 1);
+        mbar_init(&acce[0], 128);
+        mbar_init(&acce[1], 128);
+        mbar_init(drain, 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) tmem_alloc(tslot, 64);
+    fence_proxy_async_smem();  // the weight image was written by generic stores
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    if (tid == 0) {
+        // ---- producer (TMA) and MMA issuer ----
+        const uint32_t idesc = umma_idesc_bf16(128, 32);
+        const uint32_t wbase = smem_u32(wsm), sbase = smem_u32(slots);
+        const uint32_t lbo_a = (uint32_t)BW * 16;
+        int issued = 0;
+        bool ok = true;
+        for (int k = 0; k < nout && ok; k++) {
+            while (issued < nin && issued <= k + kSurSlots - 2) {
+                const int s = issued % kSurSlots;
+                if (issued >= kSurSlots && !mbar_wait_bounded(&sfree[s], ((issued / kSurSlots) - 1) & 1)) {
+                    ok = false;
+                    break;
+                }
+                mbar_expect_tx(&full[s], (uint32_t)BW * 64);
+                tma_load_5d(slots + s * slot_bytes, &tm, &full[s], 0, x0 - a.dil, 0, r + (kbeg + issued - 1) * a.dil,
+                            b);
+                issued++;
+            }
+            if (!ok) break;
+            for (int j = (k == 0 ? 0 : k + 2); j <= k + 2; j++)
+                if (!mbar_wait_bounded(&full[j % kSurSlots], (j / kSurSlots) & 1)) ok = false;
+            if (ok && k >= 2 && !mbar_wait_bounded(&acce[k & 1], ((k >> 1) - 1) & 1)) ok = false;
+            if (!ok) break;
+            tc_fence_after();
+            const uint32_t d = tmem + (uint32_t)(k & 1) * 32;
+#pragma unroll
+            for (int dy = 0; dy < 3; dy++) {
+                const uint32_t srow = sbase + (uint32_t)(((k + dy) % kSurSlots) * slot_bytes);
+#pragma unroll
+                for (int dx = 0; dx < 3; dx++) {
+#pragma unroll
+                    for (int kc = 0; kc < 2; kc++) {
+                        const uint64_t ad = umma_desc(srow + kc * 2 * lbo_a + (uint32_t)(dx * a.dil * 16), lbo_a, 128);
+                        const uint64_t bd = umma_desc(wbase + (uint32_t)((dy * 3 + dx) * 2048 + kc * 1024), 512, 128);
+                        umma_bf16(d, ad, bd, idesc, (dy | dx | kc) ? 1u : 0u);
+                    }
+                }
+            }
+            umma_commit(&accf[k & 1]);
+            umma_commit(&sfree[k % kSurSlots]);  // input row k is not read again
+        }
+        if (!ok) atomicExch(a.err, GLSU_ERR_TIMEOUT);
+        // drain: the last load of every slot has landed, every MMA has completed
+        for (int j = max(0, issued - kSurSlots); j < issued; j++)
+            mbar_wait_bounded(&full[j % kSurSlots], (j / kSurSlots) & 1);
+        umma_commit(drain);
+        mbar_wait_bounded(drain, 0);
+    } else if (warp >= 4) {
+        // ---- epilogue: TMEM -> bias, ReLU, mask -> BF16 NHWC ----
+        const int q = warp - 4;
+        const int x = x0 + q * 32 + lane;
+        for (int k = 0; k < nout; k++) {
+            if (!mbar_wait_bounded(&accf[k & 1], (k >> 1) & 1)) {
+                if (lane == 0) atomicExch(a.err, GLSU_ERR_TIMEOUT);
+                break;
+            }
+            tc_fence_after();
+            float v[32];
+            tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(k & 1) * 32, v);
+            tc_fence_before();
+            mbar_arrive(&acce[k & 1]);
+            const int y = r + (kbeg + k) * a.dil;
+            if (x < a.W) {
+                const size_t off = (((size_t)b * a.H + y) * a.W + x) * 32;
+#pragma unroll
+                for (int c = 0; c < 32; c++) {
+                    v[c] += bias_s[c];
+                    if (a.relu) v[c] = fmaxf(v[c], 0.f);
+                }
+                if (a.mask) {
+                    const uint4 *mp = reinterpret_cast<const uint4 *>(a.mask + off);
+#pragma unroll
+                    for (int g = 0; g < 4; g++) {
+                        float mv[8];
+                        unpack8(mp[g], mv);
+#pragma unroll
+                        for (int i = 0; i < 8; i++)
+                            if (!(mv[i] > 0.f)) v[8 * g + i] = 0.f;
+                    }
+                }
+                uint4 *op = reinterpret_cast<uint4 *>(a.out + off);
+#pragma unroll
+                for (int g = 0; g < 4; g++)
+                    op[g] = make_uint4(pack_bf2(v[8 * g], v[8 * g + 1]), pack_bf2(v[8 * g + 2], v[8 * g + 3]),
+                                       pack_bf2(v[8 * g + 4], v[8 * g + 5]), pack_bf2(v[8 * g + 6], v[8 * g + 7]));
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 64);
+}
+
+int sur_conv_smem_bytes(int dil)
+{
+    const int BW = 128 + 2 * dil;
+    const int slot_bytes = (BW * 64 + 1023) & ~1023;
+    return kSurWBytes + kSurSlots * slot_bytes + (2 * kSurSlots + 5) * 8 + 32 * 4 + 16;
+}
+
+int sur_conv_grid(int B, int H, int W, int dil)
+{
+    const int nsx = (W + 127) / 128;
+    const int nch = ((H + dil - 1) / dil + kSurRows - 1) / kSurRows;
+    return B * nsx * dil * nch;
+}
+
+// 5-D map of a [B][H][W][32] BF16 activation tensor: {8 channels, W, 4
+// chunks, H, B} with strides {64 B, 16 B, W*64 B, H*W*64 B}; box
+// {8, 128 + 2d, 4, 1, 1}.
+int sur_make_map(CUtensorMap *tm, const void *act, int B, int H, int W, int dil)
+{
+    auto enc = get_encode_fn();
+    if (!enc) return fail(GLSU_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    if (dil < 1 || 128 + 2 * dil > 256) return fail(GLSU_ERR_INVALID, "surrogate dilation must be 1..64");
+    cuuint64_t dims[5] = {8, (cuuint64_t)W, 4, (cuuint64_t)H, (cuuint64_t)B};
+    cuuint64_t strides[4] = {64, 16, (cuuint64_t)W * 64, (cuuint64_t)H * W * 64};
+    cuuint32_t box[5] = {8, (cuuint32_t)(128 + 2 * dil), 4, 1, 1};
+    cuuint32_t es[5] = {1, 1, 1, 1, 1};
+    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(act), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(GLSU_ERR_CUDA, "cuTensorMapEncodeTiled failed for an activation map");
+    return GLSU_OK;
+}
+
+int launch_sur_conv(const CUtensorMap &tm, const SurConvArgs &a, cudaStream_t s)
+{
+    static int attr_bytes = 0;
+    const int smem = sur_conv_smem_bytes(a.dil);
+    if (smem > attr_bytes) {
+        GLSU_CUDA_TRY(cudaFuncSetAttribute(sur_conv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           sur_conv_smem_bytes(64)));
+        attr_bytes = sur_conv_smem_bytes(64);
+    }
+    sur_conv_tc_kernel<<<sur_conv_grid(a.B, a.H, a.W, a.dil), 256, smem, s>>>(tm, a);
+    GLSU_CUDA_TRY(cudaGetLastError());
+    return GLSU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// layer 0 (2 -> 32) and layer 7 (32 -> 2) on CUDA cores
+// ---------------------------------------------------------------------------
+// w0: [32][2][9] (BF16-rounded FP32), b0[32]; z: complex [B][H][W]
+__global__ void __launch_bounds__(256) sur_l0_kernel(const float2 *__restrict__ z, int B, int H, int W, int dil,
+                                                     const float *__restrict__ w0, const float *__restrict__ b0,
+                                                     uint16_t *__restrict__ out)
+{
+    __shared__ float ws[32 * 18 + 32];
+    for (int e = threadIdx.x; e < 32 * 18; e += 256) ws[e] = w0[e];
+    if (threadIdx.x < 32) ws[576 + threadIdx.x] = b0[threadIdx.x];
+    __syncthreads();
+    const size_t n = (size_t)B * H * W;
+    for (size_t p = (size_t)blockIdx.x * 256 + threadIdx.x; p < n; p += (size_t)gridDim.x * 256) {
+        const int x = (int)(p % W);
+        const int y = (int)((p / W) % H);
+        const size_t img = p - (size_t)y * W - x;
+        float in[18];
+#pragma unroll
+        for (int t = 0; t < 9; t++) {
+            const int yy = y + (t / 3 - 1) * dil, xx = x + (t % 3 - 1) * dil;
+            float2 v = make_float2(0.f, 0.f);
+            if (yy >= 0 && yy < H && xx >= 0 && xx < W) v = z[img + (size_t)yy * W + xx];
+            in[t] = v.x;
+            in[9 + t] = v.y;
+        }
+        float acc[32];
+#pragma unroll
+        for (int c = 0; c < 32; c++) {
+            float s = ws[576 + c];
+#pragma unroll
+            for (int k = 0; k < 18; k++) s = fmaf(ws[c * 18 + k], in[k], s);
+            acc[c] = fmaxf(s, 0.f);
+        }
+        uint4 *op = reinterpret_cast<uint4 *>(out + p * 32);
+#pragma unroll
+        for (int g = 0; g < 4; g++)
+            op[g] = make_uint4(pack_bf2(acc[8 * g], acc[8 * g + 1]), pack_bf2(acc[8 * g + 2], acc[8 * g + 3]),
+                               pack_bf2(acc[8 * g + 4], acc[8 * g + 5]), pack_bf2(acc[8 * g + 6], acc[8 * g + 7]));
+    }
+}
+
+// Last layer, residual, renormalisation.  w7: [2][32][9], b7[2].
+// Writes out = y/|y| (complex).  With a target (training): per pixel loss
+// wgt |out - t|^2, wgt = min(|target|, 1), t = target/|target|, and the
+// gradient dL/dh7 of the mean loss into dh; per-block loss sums into part.
+__global__ void __launch_bounds__(256) sur_l7_kernel(const uint16_t *__restrict__ a6, const float2 *__restrict__ z,
+                                                     int B, int H, int W, int dil, const float *__restrict__ w7,
+                                                     const float *__restrict__ b7, float2 *__restrict__ out,
+                                                     const float2 *__restrict__ target, float2 *__restrict__ dh,
+                                                     double *__restrict__ part)
+{
+    __shared__ float ws[2 * 32 * 9 + 2];
+    __shared__ double red[256];
+    for (int e = threadIdx.x; e < 576; e += 256) ws[e] = w7[e];
+    if (threadIdx.x < 2) ws[576 + threadIdx.x] = b7[threadIdx.x];
+    __syncthreads();
+    const size_t n = (size_t)B * H * W;
+    const double inv_n = 1.0 / (double)n;
+    double lsum = 0;
+    for (size_t p = (size_t)blockIdx.x * 256 + threadIdx.x; p < n; p += (size_t)gridDim.x * 256) {
+        const int x = (int)(p % W);
+        const int y = (int)((p / W) % H);
+        const size_t img = p - (size_t)y * W - x;
+        float h0 = ws[576], h1 = ws[577];
+#pragma unroll
+        for (int t = 0; t < 9; t++) {
+            const int yy = y + (t / 3 - 1) * dil, xx = x + (t % 3 - 1) * dil;
+            if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
+            const uint4 *ap = reinterpret_cast<const uint4 *>(a6 + (img + (size_t)yy * W + xx) * 32);
+#pragma unroll
+            for (int g = 0; g < 4; g++) {
+                float av[8];
+                unpack8(ap[g], av);
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    h0 = fmaf(ws[(8 * g + i) * 9 + t], av[i], h0);
+                    h1 = fmaf(ws[288 + (8 * g + i) * 9 + t], av[i], h1);
+                }
+            }
+        }
+        const float2 xv = z[p];
+        const float yr = xv.x + h0, yi = xv.y + h1;
+        const float nrm = sqrtf(yr * yr + yi * yi);
+        const float inv = nrm > 1e-20f ? 1.f / nrm : 0.f;
+        const float orr = yr * inv, oii = yi * inv;
+        out[p] = make_float2(orr, oii);
+        if (target) {
+            const float2 tv = target[p];
+            const float tn = sqrtf(tv.x * tv.x + tv.y * tv.y);
+            const float wgt = fminf(tn, 1.f);
+            const float ti = tn > 1e-20f ? 1.f / tn : 0.f;
+            const float er = orr - tv.x * ti, ei = oii - tv.y * ti;
+            lsum += (double)(wgt * (er * er + ei * ei));
+            // d out: 2 wgt e / n; through out = y/|y|: (g - out (out.g)) / |y|
+            const float gr = (float)(2.0 * inv_n) * wgt * er, gi = (float)(2.0 * inv_n) * wgt * ei;
+            const float dot = orr * gr + oii * gi;
+            dh[p] = make_float2((gr - orr * dot) * inv, (gi - oii * dot) * inv);
+        }
+    }
+    if (target) {
+        red[threadIdx.x] = lsum;
+        __syncthreads();
+        for (int s = 128; s > 0; s >>= 1) {
+            if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) part[blockIdx.x] = red[0] * inv_n;
+    }
+}
+
+// dL/da6 through layer 7, masked by ReLU'(a6): g6[p][ci] = [a6 > 0] *
+// sum_t sum_co w7[co][ci][t] dh[p - off_t][co]
+__global__ void __launch_bounds__(256) sur_l7_bwd_kernel(const float2 *__restrict__ dh,
+                                                         const uint16_t *__restrict__ a6, int B, int H, int W,
+                                                         int dil, const float *__restrict__ w7,
+                                                         uint16_t *__restrict__ g6)
+{
+    __shared__ float ws[576];
+    for (int e = threadIdx.x; e < 576; e += 256) ws[e] = w7[e];
+    __syncthreads();
+    const size_t n = (size_t)B * H * W;
+    for (size_t p = (size_t)blockIdx.x * 256 + threadIdx.x; p < n; p += (size_t)gridDim.x * 256) {
+        const int x = (int)(p % W);
+        const int y = (int)((p / W) % H);
+        const size_t img = p - (size_t)y * W - x;
+        float acc[32];
+#pragma unroll
+        for (int c = 0; c < 32; c++) acc[c] = 0.f;
+#pragma unroll
+        for (int t = 0; t < 9; t++) {
+            const int yy = y - (t / 3 - 1) * dil, xx = x - (t % 3 - 1) * dil;
+            if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
+            const float2 d = dh[img + (size_t)yy * W + xx];
+#pragma unroll
+            for (int c = 0; c < 32; c++) acc[c] = fmaf(ws[c * 9 + t], d.x, fmaf(ws[288 + c * 9 + t], d.y, acc[c]));
+        }
+        const uint4 *ap = reinterpret_cast<const uint4 *>(a6 + p * 32);
+        uint4 *op = reinterpret_cast<uint4 *>(g6 + p * 32);
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            float av[8];
+            unpack8(ap[g], av);
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+                if (!(av[i] > 0.f)) acc[8 * g + i] = 0.f;
+            op[g] = make_uint4(pack_bf2(acc[8 * g], acc[8 * g + 1]), pack_bf2(acc[8 * g + 2], acc[8 * g + 3]),
+                               pack_bf2(acc[8 * g + 4], acc[8 * g + 5]), pack_bf2(acc[8 * g + 6], acc[8 * g + 7]));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// weight gradients (CUDA cores, FP32), per-block partials
+// ---------------------------------------------------------------------------
+// 32 -> 32 layer: part[blk][co][ci][t] (+ part[blk][9216 + co] for the bias)
+// = sum over the block's pixels of g[p][co] * a[p + off_t][ci].  A block
+// takes output rows of one 64-pixel segment.
+constexpr int kDwSeg = 64;
+constexpr int kDwRowsPerBlock = 8;
+
+__global__ void __launch_bounds__(256) sur_dw32_kernel(const uint16_t *__restrict__ g, const uint16_t *__restrict__ a,
+                                                       int B, int H, int W, int dil, float *__restrict__ part)
+{
+    extern __shared__ __align__(16) float dsm[];
+    const int SW = kDwSeg + 2 * dil;
+    float *gs = dsm;                  // [64][32]
+    float *as = gs + kDwSeg * 32;     // [3][SW][32]
+    const int nsx = (W + kDwSeg - 1) / kDwSeg;
+    const int nby = (H + kDwRowsPerBlock - 1) / kDwRowsPerBlock;
+    int item = blockIdx.x;
+    const int sx = item % nsx;
+    item /= nsx;
+    const int by = item % nby;
+    const int b = item / nby;
+    const int x0 = sx * kDwSeg;
+    const int tid = threadIdx.x, co = tid >> 3, ci0 = (tid & 7) * 4;
+    float acc[9][4];
+    float bacc = 0.f;
+#pragma unroll
+    for (int t = 0; t < 9; t++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) acc[t][i] = 0.f;
+    for (int yy = 0; yy < kDwRowsPerBlock; yy++) {
+        const int y = by * kDwRowsPerBlock + yy;
+        if (y >= H) break;
+        __syncthreads();
+        for (int e = tid; e < kDwSeg * 4; e += 256) {  // 16-byte groups of g
+            const int px = e >> 2, grp = e & 3, x = x0 + px;
+            float v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (x < W) unpack8(reinterpret_cast<const uint4 *>(g + (((size_t)b * H + y) * W + x) * 32)[grp], v);
+#pragma unroll
+            for (int i = 0; i < 8; i++) gs[px * 32 + grp * 8 + i] = v[i];
+        }
+        for (int e = tid; e < 3 * SW * 4; e += 256) {
+            const int grp = e & 3, rest = e >> 2, px = rest % SW, ky = rest / SW;
+            const int ys = y + (ky - 1) * dil, xs = x0 - dil + px;
+            float v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (ys >= 0 && ys < H && xs >= 0 && xs < W)
+                unpack8(reinterpret_cast<const uint4 *>(a + (((size_t)b * H + ys) * W + xs) * 32)[grp], v);
+#pragma unroll
+            for (int i = 0; i < 8; i++) as[(ky * SW + px) * 32 + grp * 8 + i] = v[i];
+        }
+        __syncthreads();
+        for (int px = 0; px < kDwSeg; px++) {
+            const float gv = gs[px * 32 + co];
+            bacc += gv;
+#pragma unroll
+            for (int t = 0; t < 9; t++) {
+                const float4 av =
+                    *reinterpret_cast<const float4 *>(&as[((t / 3) * SW + px + (t % 3) * dil) * 32 + ci0]);
+                acc[t][0] = fmaf(gv, av.x, acc[t][0]);
+                acc[t][1] = fmaf(gv, av.y, acc[t][1]);
+                acc[t][2] = fmaf(gv, av.z, acc[t][2]);
+                acc[t][3] = fmaf(gv, av.w, acc[t][3]);
+            }
+        }
+    }
+    float *pp = part + (size_t)blockIdx.x * (9216 + 32);
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int t = 0; t < 9; t++) pp[(co * 32 + ci0 + i) * 9 + t] = acc[t][i];
+    if ((tid & 7) == 0) pp[9216 + co] = bacc;
+}
+
+int sur_dw32_blocks(int B, int H, int W)
+{
+    return B * ((H + kDwRowsPerBlock - 1) / kDwRowsPerBlock) * ((W + kDwSeg - 1) / kDwSeg);
+}
+int sur_dw32_smem(int dil) { return (kDwSeg * 32 + 3 * (kDwSeg + 2 * dil) * 32) * 4; }
+
+// Layer 0 (g0 BF16 32 ch, input x = z 2 ch) and layer 7 (g = dh 2 ch FP32,
+// input a6 32 ch): part[blk][co][ci][t] + bias, one combination per thread
+// stride.  COUT x CIN = 32 x 2 or 2 x 32.
+template <int COUT, int CIN>
+__global__ void __launch_bounds__(256) sur_dw_small_kernel(const void *__restrict__ gptr,
+                                                           const void *__restrict__ inptr, int B, int H, int W,
+                                                           int dil, int pix_per_block, float *__restrict__ part)
+{
+    constexpr int NW = COUT * CIN * 9, NT = NW + COUT;
+    constexpr int PER = (NT + 255) / 256;
+    float acc[PER];
+#pragma unroll
+    for (int i = 0; i < PER; i++) acc[i] = 0.f;
+    const size_t n = (size_t)B * H * W;
+    const size_t p0 = (size_t)blockIdx.x * pix_per_block;
+    for (size_t p = p0; p < p0 + pix_per_block && p < n; p++) {
+        const int x = (int)(p % W);
+        const int y = (int)((p / W) % H);
+        const size_t img = p - (size_t)y * W - x;
+#pragma unroll
+        for (int i = 0; i < PER; i++) {
+            const int c = threadIdx.x + 256 * i;
+            if (c >= NT) continue;
+            const int co = c < NW ? c / (CIN * 9) : c - NW;
+            float gv;
+            if (COUT == 32) gv = bf2f(reinterpret_cast<const uint16_t *>(gptr)[p * 32 + co]);
+            else gv = co == 0 ? reinterpret_cast<const float2 *>(gptr)[p].x : reinterpret_cast<const float2 *>(gptr)[p].y;
+            if (c >= NW) {
+                acc[i] += gv;
+                continue;
+            }
+            const int ci = (c / 9) % CIN, t = c % 9;
+            const int yy = y + (t / 3 - 1) * dil, xx = x + (t % 3 - 1) * dil;
+            if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
+            const size_t q = img + (size_t)yy * W + xx;
+            float iv;
+            if (CIN == 2) {
+                const float2 zv = reinterpret_cast<const float2 *>(inptr)[q];
+                iv = ci == 0 ? zv.x : zv.y;
+            } else {
+                iv = bf2f(reinterpret_cast<const uint16_t *>(inptr)[q * 32 + ci]);
+            }
+            acc[i] = fmaf(gv, iv, acc[i]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        const int c = threadIdx.x + 256 * i;
+        if (c < NT) part[(size_t)blockIdx.x * NT + c] = acc[i];
+    }
+}
+
+// Deterministic column sums of per-block partials: out[c] = sum_b part[b][c].
+__global__ void sur_reduce_kernel(const float *__restrict__ part, int nblocks, int ncols, float *__restrict__ out)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncols) return;
+    double s = 0;
+    for (int b = 0; b < nblocks; b++) s += part[(size_t)b * ncols + c];
+    out[c] = (float)s;
+}
+
+__global__ void sur_sum_kernel(const double *__restrict__ part, int n, double *__restrict__ out)
+{
+    double s = 0;
+    for (int i = threadIdx.x; i < n; i += 32) s += part[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) *out = s;
+}
+
+// ---------------------------------------------------------------------------
+// Adam and weight packing
+// ---------------------------------------------------------------------------
+__global__ void sur_adam_kernel(float *__restrict__ w, const float *__restrict__ grad, float *__restrict__ m,
+                                float *__restrict__ v, int n, float lr, float b1, float b2, float eps, float c1,
+                                float c2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = grad[i];
+    const float mi = b1 * m[i] + (1 - b1) * gi;
+    const float vi = b2 * v[i] + (1 - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    w[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+}
+
+__device__ __forceinline__ float bf16_round(float f) { return __bfloat162float(__float2bfloat16_rn(f)); }
+
+// From the FP32 master parameters (per layer W[co][ci][3][3] then b[co]):
+//   pk_fwd[l][t][chunk][n=co][8 ci] and pk_bwd[l][t'][chunk][n=ci][8 co]
+//   (t' = 8 - t: the transposed, flipped kernel of the backward-data pass)
+//   for the six tensor-core layers; BF16-rounded FP32 copies of layers 0, 7.
+__global__ void sur_pack_kernel(const float *__restrict__ master, uint16_t *__restrict__ pk_fwd,
+                                uint16_t *__restrict__ pk_bwd, float *__restrict__ w0r, float *__restrict__ w7r)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 576) w0r[i] = bf16_round(master[i]);
+    const int off7 = kSurL0Params + 6 * kSurL32Params;
+    if (i < 576) w7r[i] = bf16_round(master[off7 + i]);
+    if (i >= 6 * 9216) return;
+    const int l = i / 9216, e = i % 9216;
+    const int co = e / 288, ci = (e / 9) % 32, t = e % 9;
+    const float wv = master[kSurL0Params + l * kSurL32Params + e];
+    const __nv_bfloat16 h = __float2bfloat16_rn(wv);
+    const uint16_t bits = *reinterpret_cast<const uint16_t *>(&h);
+    // forward: B[n = co][k = ci] of tap t
+    pk_fwd[(size_t)l * 9216 + ((t * 4 + ci / 8) * 32 + co) * 8 + (ci % 8)] = bits;
+    // backward data: B[n = ci][k = co] of tap 8 - t
+    pk_bwd[(size_t)l * 9216 + (((8 - t) * 4 + co / 8) * 32 + ci) * 8 + (co % 8)] = bits;
+}
+
+// Gather training crops: x[b] = pool_x[idx[b]][oy:oy+h, ox:ox+w] (complex),
+// same for the target.
+__global__ void sur_gather_kernel(const float2 *__restrict__ px, const float2 *__restrict__ pt, int PH, int PW,
+                                  const int4 *__restrict__ crops, int B, int h, int w, float2 *__restrict__ x,
+                                  float2 *__restrict__ t)
+{
+    const size_t n = (size_t)B * h * w;
+    for (size_t p = (size_t)blockIdx.x * 256 + threadIdx.x; p < n; p += (size_t)gridDim.x * 256) {
+        const int xx = (int)(p % w), yy = (int)((p / w) % h), b = (int)(p / ((size_t)w * h));
+        const int4 c = crops[b];  // (pool index, oy, ox, unused)
+        const size_t src = ((size_t)c.x * PH + c.y + yy) * PW + c.z + xx;
+        x[p] = px[src];
+        t[p] = pt[src];
+    }
+}
+
+}  // namespace glsu

@@ -1,0 +1,45 @@
+// sur_net.cuh -- the surrogate network object shared by the C ABI and the
+// DPRA handle (see sur_kernels.cu for the network and its kernels).
+#pragma once
+
+#include "glsu_internal.cuh"
+
+namespace glsu {
+
+struct SurNet {
+    int B = 0, H = 0, W = 0;
+    int dil[kSurLayers] = {1, 1, 1, 1, 1, 1, 1, 1};
+    bool training = false;
+    cudaStream_t stream = nullptr;
+    // parameters: FP32 master, BF16 operand images of layers 1..6 (forward and
+    // transposed/flipped for backward-data), BF16-rounded layers 0 and 7
+    float *d_master = nullptr;
+    uint16_t *d_pk_fwd = nullptr, *d_pk_bwd = nullptr;
+    float *d_w0r = nullptr, *d_w7r = nullptr;
+    // activations [B][H][W][32] BF16: training keeps a0..a6, inference ping-pongs two
+    uint16_t *d_act[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    // training
+    uint16_t *d_g[2] = {nullptr, nullptr};  // gradients w.r.t. pre-activations
+    float2 *d_dh = nullptr, *d_out = nullptr;
+    float *d_grad = nullptr, *d_m = nullptr, *d_v = nullptr, *d_part = nullptr;
+    double *d_lpart = nullptr, *d_loss = nullptr;
+    int nb32 = 0, nbs = 0, adam_t = 0;
+    int *d_err = nullptr;
+    CUtensorMap map_fwd[7], map_bwd[7];
+
+    int init(int batch, int width, int height, const int *dilations, bool train);
+    void release();
+    int pack();
+    int set_params(const float *h);
+    int get_params(float *h);
+    int hidden(const float2 *z);
+    const uint16_t *a6() const;
+    // out = y / |y| of the network on z (complex [B][H][W]), enqueued on stream
+    int forward(const void *d_z, void *d_out);
+    // forward with loss and all parameter gradients into d_grad / d_loss
+    int backward(const void *d_z, const void *d_target);
+    int adam(float lr, float b1, float b2, float eps);
+    int check_error();
+};
+
+}  // namespace glsu

@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "glsu_internal.cuh"
+#include "ptx_sm103.cuh"
 
 namespace glsu {
 
@@ -41,60 +42,6 @@ namespace glsu {
 template <typename T, int S> struct Taps {
     T g[2 * S + 1];
 };
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void fence_mbar_init()
-{
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait: gives up after ~2^31 SM cycles (about a second).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
-{
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > (1ll << 31)) return false;
-    }
-    return true;
-}
-
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, uint64_t *bar, int c0, int c1,
-                                            int c2)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
-        : "memory");
-}
 
 template <typename T> __device__ __forceinline__ C2<T> mk(T x, T y)
 {
@@ -162,7 +109,7 @@ template <typename T, int S> struct ColGeom {
 template <typename T, int S>
 __global__ void __launch_bounds__(256) wff_rows_demod_kernel(const C2<T> *__restrict__ f, int W, int H,
                                                              int pitch, const C2<T> *__restrict__ ex, int nfx,
-                                                             C2<T> *__restrict__ R, Taps<T, S> gx)
+                                                             C2<T> *__restrict__ R, Taps<T, S> gx, TileMask tm)
 {
     using G = RowGeom<T, S>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -170,6 +117,7 @@ __global__ void __launch_bounds__(256) wff_rows_demod_kernel(const C2<T> *__rest
     C2<T> *ot = ft + kRowTileRows * G::IN_STRIDE;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int x0 = blockIdx.x * kRowTileCols, y0 = blockIdx.y * kRowTileRows;
+    if (tm.flags && !tm.any(y0, y0 + kRowTileRows, x0, x0 + kRowTileCols)) return;
 
     for (int e = tid; e < kRowTileRows * G::IN_W; e += 256) {
         const int r = e / G::IN_W, c = e - r * G::IN_W;
@@ -229,7 +177,7 @@ template <typename T, int S>
 __global__ void __launch_bounds__(ColGeom<T, S>::THREADS, 1)
     wff_cols_kernel(const __grid_constant__ CUtensorMap tmR, C2<T> *__restrict__ Cout,
                     const C2<T> *__restrict__ ey, int nfy, int H, int pitch, const T *__restrict__ thr_ptr,
-                    Taps<T, S> gA, Taps<T, S> gB, int *__restrict__ err)
+                    Taps<T, S> gA, Taps<T, S> gB, int *__restrict__ err, TileMask tm)
 {
     using G = ColGeom<T, S>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -238,6 +186,7 @@ __global__ void __launch_bounds__(ColGeom<T, S>::THREADS, 1)
     uint64_t *bar = reinterpret_cast<uint64_t *>(tt + G::TT * 32);
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int x0 = blockIdx.x * 32, y0 = blockIdx.y * G::TY, i = blockIdx.z;
+    if (tm.flags && !tm.any(y0, y0 + G::TY, x0, x0 + 32)) return;  // before any barrier or copy
 
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -365,7 +314,8 @@ __global__ void __launch_bounds__(256) wff_rows_final_kernel(const C2<T> *__rest
                                                              Taps<T, S> gx, C2<T> *__restrict__ out,
                                                              const T *__restrict__ phiref,
                                                              const T *__restrict__ dphiref,
-                                                             T *__restrict__ phicurr, T *__restrict__ dphi)
+                                                             T *__restrict__ phicurr, T *__restrict__ dphi,
+                                                             TileMask tm)
 {
     using G = RowGeom<T, S>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -373,6 +323,7 @@ __global__ void __launch_bounds__(256) wff_rows_final_kernel(const C2<T> *__rest
     C2<T> *ot = ft + kRowTileRows * G::IN_STRIDE;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int x0 = blockIdx.x * kRowTileCols, y0 = blockIdx.y * kRowTileRows;
+    if (tm.flags && !tm.any(y0, y0 + kRowTileRows, x0, x0 + kRowTileCols)) return;
     const size_t exs = (size_t)pitch + 2 * kPhasorPad;
     const size_t plane = (size_t)H * pitch;
 
@@ -428,6 +379,7 @@ __global__ void __launch_bounds__(256) wff_rows_final_kernel(const C2<T> *__rest
         const int r = e / kRowTileCols, c = e - r * kRowTileCols;
         const int gy = y0 + r, gxx = x0 + c;
         if (gy >= H || gxx >= W) continue;
+        if (tm.flags && !tm.at(gy, gxx)) continue;
         const size_t id = (size_t)gy * W + gxx;
         const C2<T> v = ot[r * G::OUT_STRIDE + c];
         if (MODE == 0) {
@@ -564,6 +516,9 @@ int WffPlan::alloc_device()
         if (cudaMalloc(&d_R, (size_t)nfx * plane_bytes()) != cudaSuccess ||
             cudaMalloc(&d_C, (size_t)nfx * plane_bytes()) != cudaSuccess)
             return fail(GLSU_ERR_ALLOC, "cudaMalloc of WFF2 planes failed");
+        // defined contents: a tile-masked run reads planes it did not write
+        GLSU_CUDA_TRY(cudaMemset(d_R, 0, (size_t)nfx * plane_bytes()));
+        GLSU_CUDA_TRY(cudaMemset(d_C, 0, (size_t)nfx * plane_bytes()));
         if (cudaMalloc(&d_thr, sizeof(double)) != cudaSuccess ||
             cudaMalloc((void **)&d_part, sizeof(double) * kThrBlocks) != cudaSuccess ||
             cudaMalloc((void **)&d_err, sizeof(int)) != cudaSuccess)
@@ -610,7 +565,7 @@ int WffPlan::upload_tables(cudaStream_t s)
     return GLSU_OK;
 }
 
-static PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn()
+PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn()
 {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     if (!fn) {
@@ -672,6 +627,13 @@ int WffPlan::check_device_error(cudaStream_t s)
 }
 
 // ---- launch dispatch ------------------------------------------------------
+static TileMask with_margins(TileMask m, int my, int mx)
+{
+    m.my = my;
+    m.mx = mx;
+    return m;
+}
+
 template <typename T, int S> static Taps<T, S> make_taps(const double *g, int strue, double mul)
 {
     Taps<T, S> t;
@@ -695,7 +657,7 @@ static int launch_rows_demod(const WffPlan &P, const void *d_f, cudaStream_t s)
     dim3 grid(P.pitch / kRowTileCols, (P.H + kRowTileRows - 1) / kRowTileRows);
     wff_rows_demod_kernel<T, S><<<grid, 256, G::SMEM, s>>>(
         (const C2<T> *)d_f, P.W, P.H, P.pitch, (const C2<T> *)P.d_ex, P.nfx, (C2<T> *)P.d_R,
-        make_taps<T, S>(P.gx, P.sx, 1.0));
+        make_taps<T, S>(P.gx, P.sx, 1.0), with_margins(P.mask, 2 * P.sy, P.sx));
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
 }
@@ -713,7 +675,8 @@ template <typename T, int S> static int launch_cols(const WffPlan &P, cudaStream
     wff_cols_kernel<T, S><<<grid, G::THREADS, G::SMEM, s>>>(P.tmR, (C2<T> *)P.d_C, (const C2<T> *)P.d_ey, P.nfy, P.H,
                                                        P.pitch, (const T *)P.d_thr,
                                                        make_taps<T, S>(P.gy, P.sy, P.inv_norm),
-                                                       make_taps<T, S>(P.gy, P.sy, 1.0), P.d_err);
+                                                       make_taps<T, S>(P.gy, P.sy, 1.0), P.d_err,
+                                                       with_margins(P.mask, 0, P.sx));
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
 }
@@ -733,7 +696,7 @@ static int launch_final(const WffPlan &P, void *d_out, const void *phiref, const
     wff_rows_final_kernel<T, S, MODE><<<grid, 256, G::SMEM, s>>>(
         (const C2<T> *)P.d_C, P.W, P.H, P.pitch, (const C2<T> *)P.d_ex, P.nfx,
         make_taps<T, S>(P.gx, P.sx, P.scale * P.inv_norm), (C2<T> *)d_out, (const T *)phiref, (const T *)dphiref,
-        (T *)phicurr, (T *)dphi);
+        (T *)phicurr, (T *)dphi, with_margins(P.mask, 0, 0));
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
 }
@@ -742,13 +705,7 @@ template <typename T>
 static int enqueue_t(WffPlan &P, cudaStream_t s, const void *d_f, void *d_out, int mode, const void *phiref,
                      const void *dphiref, void *phicurr, void *dphi, cudaEvent_t *ev)
 {
-    if (P.p.thr < 0 && !P.thr_ready) {
-        const size_t n = (size_t)P.W * P.H;
-        wff_thr_partial_kernel<T><<<kThrBlocks, 256, 0, s>>>((const C2<T> *)d_f, n, P.d_part);
-        wff_thr_final_kernel<T><<<1, 32, 0, s>>>(P.d_part, kThrBlocks, n, (T *)P.d_thr);
-        GLSU_CUDA_TRY(cudaGetLastError());
-        P.thr_ready = true;
-    }
+    GLSU_TRY(P.ensure_threshold(s, d_f));
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[0], s));
     int rc = GLSU_OK;
     switch (P.sxi) {
@@ -760,7 +717,7 @@ static int enqueue_t(WffPlan &P, cudaStream_t s, const void *d_f, void *d_out, i
     }
     if (rc) return rc;
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[1], s));
-    if (sizeof(T) == 4 && P.use_colfft()) {
+    if (sizeof(T) == 4 && P.use_colfft() && !P.mask.flags) {
         rc = launch_colfft(P, s);
     } else {
         switch (P.syi) {
@@ -787,6 +744,22 @@ static int enqueue_t(WffPlan &P, cudaStream_t s, const void *d_f, void *d_out, i
 #undef GLSU_FINAL
     if (rc) return rc;
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[3], s));
+    return GLSU_OK;
+}
+
+int WffPlan::ensure_threshold(cudaStream_t s, const void *d_f)
+{
+    if (p.thr >= 0 || thr_ready) return GLSU_OK;
+    const size_t n = (size_t)W * H;
+    if (prec == GLSU_F32) {
+        wff_thr_partial_kernel<float><<<kThrBlocks, 256, 0, s>>>((const float2 *)d_f, n, d_part);
+        wff_thr_final_kernel<float><<<1, 32, 0, s>>>(d_part, kThrBlocks, n, (float *)d_thr);
+    } else {
+        wff_thr_partial_kernel<double><<<kThrBlocks, 256, 0, s>>>((const double2 *)d_f, n, d_part);
+        wff_thr_final_kernel<double><<<1, 32, 0, s>>>(d_part, kThrBlocks, n, (double *)d_thr);
+    }
+    GLSU_CUDA_TRY(cudaGetLastError());
+    thr_ready = true;
     return GLSU_OK;
 }
 

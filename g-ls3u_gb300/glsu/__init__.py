@@ -133,6 +133,24 @@ def lib() -> ctypes.CDLL:
                               ctypes.c_uint64], c_int),
             "glsu_aia_run_device": ([c_void_p, c_void_p, c_int, fltp, fltp, c_int, intp, fltp, c_int, c_float,
                                      ctypes.c_uint64], c_int),
+            "glsu_sur_param_count": ([], c_int),
+            "glsu_sur_create": ([pp, c_int, c_int, c_int, intp, c_int], c_int),
+            "glsu_sur_destroy": ([c_void_p], c_int),
+            "glsu_sur_set_stream": ([c_void_p, c_void_p], c_int),
+            "glsu_sur_set_params": ([c_void_p, fltp], c_int),
+            "glsu_sur_get_params": ([c_void_p, fltp], c_int),
+            "glsu_sur_forward": ([c_void_p, c_void_p, c_void_p], c_int),
+            "glsu_sur_backward": ([c_void_p, c_void_p, c_void_p, dblp, fltp], c_int),
+            "glsu_sur_adam": ([c_void_p, c_float, c_float, c_float, c_float], c_int),
+            "glsu_sur_output": ([c_void_p, c_void_p], c_int),
+            "glsu_sur_gather": ([c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, intp, c_void_p, c_void_p],
+                                c_int),
+            "glsu_sur_conv32": ([c_void_p, c_void_p, c_int, c_int, c_int, c_int, fltp, fltp, c_int, c_void_p,
+                                 c_void_p], c_int),
+            "glsu_dpra_set_surrogate": ([c_void_p, fltp, intp, c_int, c_int, c_double], c_int),
+            "glsu_dpra_surrogate_stats": ([c_void_p, ctypes.POINTER(ctypes.c_longlong),
+                                           ctypes.POINTER(ctypes.c_longlong), fltp, intp], c_int),
+            "glsu_dpra_lsq_device": ([c_void_p, c_void_p], c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -344,6 +362,35 @@ class DPRA:
         """dphi = dphi_ref + unwrap(t) (MatLab/fp_ls3u.m:104) instead of dphi_ref + t."""
         check(lib().glsu_dpra_set_unwrap(self._h, int(enable), start_row, start_col))
 
+    def set_surrogate(self, params, dilations, tile: int = 256, patch: int = 8, tol: float = 0.05):
+        """Surrogate form (FP32): the learned network replaces WFF2, one exact
+        WFF2 patch per tile judges it, tiles above ``tol`` rad fall back to the
+        plain WFF2.  ``params=None`` restores the plain form."""
+        if params is None:
+            check(lib().glsu_dpra_set_surrogate(self._h, None, None, 0, 0, 0.0))
+            return
+        p = np.ascontiguousarray(params, np.float32)
+        d = np.ascontiguousarray(dilations, np.int32)
+        check(lib().glsu_dpra_set_surrogate(self._h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                            d.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), tile, patch,
+                                            float(tol)))
+
+    def surrogate_stats(self, ntiles: int = 0):
+        """(tiles probed, tiles recomputed by the plain WFF2[, last residuals,
+        last probe sites (row, col)]) -- the last two when ntiles > 0."""
+        a, b = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        r = np.zeros(max(ntiles, 1), np.float32)
+        st = np.zeros((max(ntiles, 1), 2), np.int32)
+        check(lib().glsu_dpra_surrogate_stats(
+            self._h, ctypes.byref(a), ctypes.byref(b),
+            r.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) if ntiles else None,
+            st.ctypes.data_as(ctypes.POINTER(ctypes.c_int)) if ntiles else None))
+        return (a.value, b.value, r, st) if ntiles else (a.value, b.value)
+
+    def lsq_device(self, d_out: int):
+        """Device copy of the last least-squares output (enqueued on the handle's stream)."""
+        check(lib().glsu_dpra_lsq_device(self._h, ctypes.c_void_p(d_out)))
+
     def stage_timing(self, enable: bool = True):
         check(lib().glsu_dpra_stage_timing(self._h, int(enable)))
 
@@ -385,3 +432,86 @@ class AIA:
                                  ctypes.byref(t), ctypes.byref(iters), ctypes.byref(err), max_iter,
                                  ctypes.c_float(max_err), ctypes.c_uint64(seed)))
         return phi, d, t.value, iters.value, err.value
+
+
+# ---------------------------------------------------------------------------
+# learned WFF2 surrogate
+# ---------------------------------------------------------------------------
+def sur_param_count() -> int:
+    return lib().glsu_sur_param_count()
+
+
+def conv32(d_in: int, d_out: int, batch: int, width: int, height: int, dilation: int, w: np.ndarray, b=None,
+           relu: bool = True, d_mask: int = 0, stream: int = 0):
+    """One 32 -> 32 tensor-core layer on BF16 NHWC device buffers (synchronous)."""
+    fp = ctypes.POINTER(ctypes.c_float)
+    w = np.ascontiguousarray(w, np.float32)
+    bb = None if b is None else np.ascontiguousarray(b, np.float32)
+    check(lib().glsu_sur_conv32(ctypes.c_void_p(d_in), ctypes.c_void_p(d_out), batch, width, height, dilation,
+                                w.ctypes.data_as(fp), None if bb is None else bb.ctypes.data_as(fp), int(relu),
+                                ctypes.c_void_p(d_mask) if d_mask else None,
+                                ctypes.c_void_p(stream) if stream else None))
+
+
+class Surrogate:
+    """The residual CNN that stands in for WFF2 (see ``include/glsu.h``)."""
+
+    def __init__(self, batch: int, width: int, height: int, dilations, training: bool = False):
+        self.batch, self.width, self.height = batch, width, height
+        self.dilations = list(dilations)
+        d = np.ascontiguousarray(dilations, np.int32)
+        h = ctypes.c_void_p()
+        check(lib().glsu_sur_create(ctypes.byref(h), batch, width, height,
+                                    d.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), int(training)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().glsu_sur_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def set_stream(self, stream: int):
+        check(lib().glsu_sur_set_stream(self._h, ctypes.c_void_p(stream)))
+
+    @property
+    def params(self) -> np.ndarray:
+        p = np.empty(sur_param_count(), np.float32)
+        check(lib().glsu_sur_get_params(self._h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return p
+
+    @params.setter
+    def params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        if p.size != sur_param_count():
+            raise ValueError("expected %d parameters" % sur_param_count())
+        check(lib().glsu_sur_set_params(self._h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
+    def forward(self, d_z: int, d_out: int):
+        check(lib().glsu_sur_forward(self._h, ctypes.c_void_p(d_z), ctypes.c_void_p(d_out)))
+
+    def backward(self, d_z: int, d_target: int, want_grad: bool = False, want_loss: bool = True):
+        loss = ctypes.c_double(0)
+        g = np.empty(sur_param_count(), np.float32) if want_grad else None
+        check(lib().glsu_sur_backward(self._h, ctypes.c_void_p(d_z), ctypes.c_void_p(d_target),
+                                      ctypes.byref(loss) if want_loss else None,
+                                      g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) if want_grad else None))
+        return (loss.value if want_loss else None), g
+
+    def adam(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8):
+        check(lib().glsu_sur_adam(self._h, lr, beta1, beta2, eps))
+
+    def output(self) -> np.ndarray:
+        o = np.empty((self.batch, self.height, self.width), np.complex64)
+        check(lib().glsu_sur_output(self._h, _ptr(o)))
+        return o
+
+    def gather(self, d_pool_x: int, d_pool_t: int, pool_n: int, pool_h: int, pool_w: int, crops, d_x: int,
+               d_t: int):
+        """crops: rows (pool index, row, col) of the batch's windows."""
+        c = np.ascontiguousarray(crops, np.int32).reshape(-1)
+        check(lib().glsu_sur_gather(self._h, ctypes.c_void_p(d_pool_x), ctypes.c_void_p(d_pool_t), pool_n,
+                                    pool_h, pool_w,
+                                    c.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), ctypes.c_void_p(d_x),
+                                    ctypes.c_void_p(d_t)))

@@ -170,6 +170,9 @@ int glsu_dpra_update_ref_phi(glsu_dpra *h);
  * the same either way.  Returns when every output is on the host. */
 int glsu_dpra_sequence(glsu_dpra *h, int nframes, const void *h_frames, int img_type, void *h_dphi_all,
                        double *time_ms);
+/* Copy the last frame's least-squares output exp(j dphi) (complex, W*H) to a
+ * device buffer, enqueued on the handle's stream. */
+int glsu_dpra_lsq_device(glsu_dpra *h, void *d_out);
 /* Copy a state plane (GLSU_PHI_*) to the host. */
 int glsu_dpra_get(glsu_dpra *h, int which, void *h_out);
 /* Copy exp(j dphi) of the last frame's least-squares stage (W*H complex,
@@ -220,6 +223,61 @@ int glsu_aia_run(glsu_aia *h, const void *const *h_frames, int img_type, float *
 int glsu_aia_run_device(glsu_aia *h, const void *d_frames, int img_type, float *d_phi, float *h_deltas,
                         int n_deltas_in, int *iters, float *err, int max_iter, float max_err,
                         uint64_t seed);
+
+/* ---- learned WFF2 surrogate ----------------------------------------------
+ * A residual CNN that stands in for WFF2 on DPRA's least-squares output:
+ * 8 layers of 3x3 convolutions (per-layer dilations), 32 hidden channels,
+ * ReLU; input and output 2 channels (re, im); out = y/|y| with
+ * y = z + net(z).  BF16 weights and activations, FP32 accumulation; the
+ * 32 -> 32 layers run on the tensor cores (tcgen05).  No reference
+ * counterpart: the reference has only the plain WFF2.
+ * Parameters (FP32, glsu_sur_param_count() of them): per layer
+ * W[co][ci][3][3] then b[co]; layer 0 is 2 -> 32, layers 1..6 32 -> 32,
+ * layer 7 32 -> 2.  All device buffers are complex64 [batch][height][width]. */
+typedef struct glsu_sur glsu_sur;
+int glsu_sur_param_count(void);
+/* dilations: 8 values in 1..64.  training != 0 keeps the activations,
+ * gradients and Adam state. */
+int glsu_sur_create(glsu_sur **out, int batch, int width, int height, const int *dilations, int training);
+int glsu_sur_destroy(glsu_sur *h);
+int glsu_sur_set_stream(glsu_sur *h, void *cuda_stream);
+int glsu_sur_set_params(glsu_sur *h, const float *h_params); /* resets the Adam state */
+int glsu_sur_get_params(glsu_sur *h, float *h_params);
+/* out = surrogate(d_z), enqueued on the handle's stream. */
+int glsu_sur_forward(glsu_sur *h, const void *d_z, void *d_out);
+/* Training handles: forward, loss = mean over pixels of
+ * min(|t|,1) |out - t/|t||^2 and its gradient for every parameter.  *loss
+ * and h_grad (param_count floats) are optional; when given, the call
+ * synchronises. */
+int glsu_sur_backward(glsu_sur *h, const void *d_z, const void *d_target, double *loss, float *h_grad);
+/* One Adam step with the gradient of the last glsu_sur_backward. */
+int glsu_sur_adam(glsu_sur *h, float lr, float beta1, float beta2, float eps);
+/* Training handles: the output of the last glsu_sur_backward (synchronous). */
+int glsu_sur_output(glsu_sur *h, void *h_out);
+/* Training crops: for b < batch, copy the width x height window at
+ * (row h_crops[3b+1], col h_crops[3b+2]) of pool image h_crops[3b] (pool:
+ * complex [pool_n][pool_h][pool_w], input and target) into d_x / d_t. */
+int glsu_sur_gather(glsu_sur *h, const void *d_pool_x, const void *d_pool_t, int pool_n, int pool_h, int pool_w,
+                    const int *h_crops, void *d_x, void *d_t);
+/* One 32 -> 32 tensor-core layer on caller BF16 NHWC buffers (synchronous):
+ * out = relu?(conv_dilation(in, w) + b), zeroed where d_mask <= 0 (d_mask
+ * may be NULL).  h_w: W[co][ci][3][3] (rounded to BF16), h_b: [32] or NULL. */
+int glsu_sur_conv32(const void *d_in, void *d_out, int batch, int width, int height, int dilation,
+                    const float *h_w, const float *h_b, int relu, const void *d_mask, void *cuda_stream);
+
+/* ---- DPRA surrogate form ---------------------------------------------------
+ * FP32 DPRA handles: replace WFF2 by the surrogate (h_params, dilations as
+ * above; NULL h_params switches back to the plain WFF2).  Every frame, one
+ * patch x patch patch per tile x tile tile gets the exact WFF2 (the sparse
+ * probe); tiles whose RMS phase residual exceeds tol (radians) are
+ * recomputed by the plain WFF2.  tol <= 0 turns the probes off. */
+int glsu_dpra_set_surrogate(glsu_dpra *h, const float *h_params, const int *dilations, int tile, int patch,
+                            double tol);
+/* Cumulative probe counts; h_resid (optional, one float per tile, tiles
+ * row-major) gets the last frame's residuals and h_sites (optional, two ints
+ * per tile) the (row, col) of the last frame's probe patches.  Synchronous. */
+int glsu_dpra_surrogate_stats(glsu_dpra *h, long long *tiles_probed, long long *tiles_flagged, float *h_resid,
+                              int *h_sites);
 
 #ifdef __cplusplus
 }
