@@ -122,9 +122,11 @@ def one_cycle(step: int, steps: int, peak: float, warm: float = 0.25) -> float:
 
 
 def train(pools, steps: int, batch: int = 16, crop: int = 256, lr: float = 1.5e-3, dilations=DILATIONS,
-          seed: int = 0, init=None, log_every: int = 500, log=print):
+          seed: int = 0, init=None, log_every: int = 500, log=print, time_budget: float = 0.0):
     """Train on a list of (x, t) pools, alternating between them; returns the
-    FP32 parameters and a list of (step, loss)."""
+    FP32 parameters and a list of (step, loss).  With time_budget > 0 the
+    learning-rate schedule runs over elapsed seconds instead of steps and
+    training stops when the budget is spent (at most `steps` steps)."""
     torch = _torch()
     import glsu
     rng = np.random.default_rng(seed)
@@ -134,7 +136,15 @@ def train(pools, steps: int, batch: int = 16, crop: int = 256, lr: float = 1.5e-
     tb = torch.empty_like(xb)
     hist = []
     t0 = time.time()
-    for it in range(steps):
+    it = 0
+    while it < steps:
+        if time_budget > 0:
+            el = time.time() - t0
+            if el >= time_budget:
+                break
+            cur_lr = one_cycle(int(1e6 * el / time_budget), 1_000_000, lr)
+        else:
+            cur_lr = one_cycle(it, steps, lr)
         x, t = pools[it % len(pools)]
         n, H, W = x.shape
         crops = np.stack([rng.integers(0, n, batch), rng.integers(0, H - crop + 1, batch),
@@ -142,10 +152,12 @@ def train(pools, steps: int, batch: int = 16, crop: int = 256, lr: float = 1.5e-
         net.gather(x.data_ptr(), t.data_ptr(), n, H, W, crops, xb.data_ptr(), tb.data_ptr())
         want = (it + 1) % log_every == 0 or it == 0
         loss, _ = net.backward(xb.data_ptr(), tb.data_ptr(), want_loss=want)
-        net.adam(one_cycle(it, steps, lr))
+        net.adam(cur_lr)
         if want:
             hist.append((it + 1, loss))
-            log("step %6d  loss %.5f  lr %.2e  %.1f s" % (it + 1, loss, one_cycle(it, steps, lr), time.time() - t0))
+            log("step %6d  loss %.5f  lr %.2e  %.1f s" % (it + 1, loss, cur_lr, time.time() - t0))
+        it += 1
+    hist.append((it, float("nan")))  # steps taken
     params = net.params
     net.close()
     return params, hist
@@ -166,6 +178,7 @@ def main(argv=None):
     ap.add_argument("--seqs256", type=int, default=1000, help="256^2 sequences (19 pairs each)")
     ap.add_argument("--seqs1024", type=int, default=20, help="1024^2 sequences (20 frames each)")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--time-budget", type=float, default=0.0, help="seconds of training (schedule over time)")
     a = ap.parse_args(argv)
     t0 = time.time()
     small = make_pool(256, a.seqs256, 20, seed=10_000 + a.seed)
@@ -174,13 +187,14 @@ def main(argv=None):
     held_big = make_pool(1024, 2, 5, seed=95_000 + a.seed)
     print("pools: %d + %d training frames, generated in %.1f s" % (small[0].shape[0], big[0].shape[0],
                                                                    time.time() - t0), flush=True)
-    params, hist = train([big, small], a.steps, a.batch, lr=a.lr, seed=a.seed)
+    params, hist = train([big, small], a.steps, a.batch, lr=a.lr, seed=a.seed, time_budget=a.time_budget,
+                         log=lambda m: print(m, flush=True))
     r_small = evaluate(params, *held_small)
     r_big = evaluate(params, *held_big)
     print("held-out phase RMSE vs WFF2: 256^2 %.4f (identity %.4f), 1024^2 %.4f (identity %.4f)"
           % (r_small[0], r_small[1], r_big[0], r_big[1]), flush=True)
     np.savez(a.out, params=params, dilations=np.array(DILATIONS, np.int32), wff=np.array(WFF),
-             radius=RADIUS, steps=a.steps, batch=a.batch, lr=a.lr, seed=a.seed,
+             radius=RADIUS, steps=int(hist[-1][0]) if hist else 0, batch=a.batch, lr=a.lr, seed=a.seed,
              pairs=small[0].shape[0] + 16 * big[0].shape[0],
              rmse_heldout_256=r_small[0], rmse_heldout_1024=r_big[0],
              rmse_identity_256=r_small[1], rmse_identity_1024=r_big[1], loss_history=np.array(hist))
