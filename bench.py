@@ -34,7 +34,19 @@ for _p in (ROOT, PKG):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-METRIC = "G-LS3U frames/s at 1024^2 FP32 (plain path: DPRA 7x7 + WFF2 21x21)"
+METRIC = "G-LS3U frames/s at 1024\u00b2 FP32, surrogate vs plain, at \u22640.02 rad RMSE vs FP64"
+# surrogate form: one exact WFF2 probe patch of 8x8 per 256x256 tile, plain
+# fallback for tiles whose RMS phase residual exceeds 0.05 rad
+SUR_TILE, SUR_PATCH, SUR_TOL = 256, 8, 0.05
+# algorithmic bytes and flops per pixel of the network: layer 0 reads z (8 B)
+# and writes 32 BF16 channels (64 B); each of the six 32->32 layers reads and
+# writes 64 B; layer 7 reads 64 B + z and writes the complex output (8 B)
+SUR_BYTES_PER_PX = 72 + 6 * 128 + 80
+SUR_FLOPS_PER_PX = 2 * 18 * 32 + 6 * 2 * 288 * 32 + 2 * 288 * 2
+# kernels per frame: plain = LS, rows, column sweep, final; surrogate = LS,
+# layer 0, six tensor-core layers, layer 7, probe, residual, three masked
+# WFF2 passes, update
+PLAIN_LAUNCHES, SUR_LAUNCHES = 4, 15
 SIZE = 1024
 RADIUS = 3
 WFF = (10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)
@@ -208,38 +220,13 @@ def run_reference(args, rank, world):
     }
 
 
-def run_ours(args, rank, world, local):
-    import torch
-    import glsu
-    from glsu import synth
-    if not torch.cuda.is_available():
-        raise RuntimeError("no CUDA device: the GB300 path has no CPU fallback")
-    torch.cuda.set_device(local)
-    size = args.size
-    N = size * size
-    wp = glsu.WffParams(*WFF)
-    seed = 1000 + rank
-    nfr = 8
-    frames, phi0, _ = synth.sequence(size, size, nfr, seed=seed)
-
-    # ---- AIA initial phase (5 frames, shifts U(0, 2pi), <= 30 iterations or 1e-4)
-    aframes, _, _ = synth.aia_frames(size, size, 5, seed=seed)
-    aia = glsu.AIA(5, size, size)
-    aia.run(list(aframes), None, max_iter=30, max_err=1e-4, seed=seed)  # warm
-    _, _, aia_ms, aia_iters, aia_err = aia.run(list(aframes), None, max_iter=30, max_err=1e-4, seed=seed)
-    aia.close()
-
-    stream = torch.cuda.Stream()
-    d = glsu.DPRA(phi0.astype(np.float32), 1, RADIUS, "f32", wp)
-    d.set_stream(stream.cuda_stream)
-    d.stage_timing(True)
-    dfr = torch.from_numpy(frames).cuda()
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+def timed_frames(glsu, torch, d, dfr, nfr, args, stream, flush, world, local):
+    """Device time of K frames through handle d (per-frame device call + reference
+    update), L2 flushed before each frame outside the events; max over ranks."""
     for k in range(args.warmup):
         d.per_frame_device(dfr[k % nfr].data_ptr(), glsu.F32)
         d.update_ref_phi()
     torch.cuda.synchronize()
-
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     stage = np.zeros(4)
     barrier(world)
@@ -258,13 +245,13 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     clk = clocks.stop()
     barrier(world)
-    dev_ms = sum(a.elapsed_time(b) for a, b in evs)
-    max_ms = reduce_max(dev_ms, world)
-    value = world * args.steps / (max_ms / 1e3)
+    max_ms = reduce_max(sum(a.elapsed_time(b) for a, b in evs), world)
+    return world * args.steps / (max_ms / 1e3), max_ms, stage / args.steps, clk
 
-    # ---- end to end through the public API (glsu_dpra_sequence, the C-ABI of
-    # DPRA_CUDAF::operator()) with pinned host buffers: K frames uploaded,
-    # processed and downloaded; copies overlap neighbouring frames' compute
+
+def e2e_sequence(glsu, torch, d, frames, nfr, args, stream, flush, world):
+    """Frames/s through glsu_dpra_sequence with pinned host frames and outputs."""
+    size = frames.shape[-1]
     hseq = torch.from_numpy(np.ascontiguousarray(frames[np.arange(args.steps) % nfr])).pin_memory()
     hout = torch.empty((args.steps, size, size), dtype=torch.float32).pin_memory()
     d.sequence_ptr(min(2, args.steps), hseq.data_ptr(), glsu.F32, hout.data_ptr())  # warm the copy streams
@@ -274,45 +261,160 @@ def run_ours(args, rank, world, local):
     barrier(world)
     t0 = time.perf_counter()
     d.sequence_ptr(args.steps, hseq.data_ptr(), glsu.F32, hout.data_ptr())
-    e2e_s = reduce_max(time.perf_counter() - t0, world)
-    e2e = world * args.steps / e2e_s
-    d.close()
+    return world * args.steps / reduce_max(time.perf_counter() - t0, world)
 
-    # ---- roofline of the dominant kernel (the WFF2 column sweep)
-    st = stage / args.steps  # ms: [LS, WFF rows, WFF column sweep, WFF final+update]
-    pitch = (size + 127) // 128 * 128
-    col_bytes = 2 * NFX * size * pitch * 8  # read R_i planes + write C_i planes (complex64)
+
+def surrogate_accuracy(glsu, torch, dfr, phi0, wp, params, dil, nframes):
+    """Teacher-forced phase error of the surrogate form against the plain FP32
+    WFF2 of the same least-squares output (per frame, all pixels), and of the
+    raw least-squares phase (no filtering) for comparison."""
+    size = dfr.shape[-1]
+    d = glsu.DPRA(phi0.astype(np.float32), 1, RADIUS, "f32", wp)
+    d.set_surrogate(params, dil, SUR_TILE, SUR_PATCH, SUR_TOL)
+    w = glsu.WFF2(size, size, "f32", wp)
+    z = torch.empty((size, size), dtype=torch.complex64, device="cuda")
+    ref = torch.empty_like(z)
+    rm, mx, rid = [], [], []
+    for k in range(1, nframes + 1):
+        pref = d.get(glsu.PHI_REF).astype(np.float64)
+        d.per_frame_device(dfr[k].data_ptr(), glsu.F32)
+        d.lsq_device(z.data_ptr())
+        torch.cuda.synchronize()
+        w.run(z.data_ptr(), ref.data_ptr())
+        pc = d.get(glsu.PHI_CURR).astype(np.float64)
+        tp = np.angle(ref.cpu().numpy())
+        e = np.angle(np.exp(1j * (pc - pref - tp)))
+        eid = np.angle(z.cpu().numpy() * np.exp(-1j * tp))
+        rm.append(float(np.sqrt(np.mean(e ** 2))))
+        mx.append(float(np.abs(e).max()))
+        rid.append(float(np.sqrt(np.mean(eid ** 2))))
+        d.update_ref_phi()
+    probed, flagged = d.surrogate_stats()
+    d.close()
+    w.close()
+    return {"rmse_per_frame": rm, "rmse": float(np.sqrt(np.mean(np.square(rm)))), "max_abs": max(mx),
+            "rmse_without_network": float(np.sqrt(np.mean(np.square(rid)))), "frames": nframes,
+            "tiles_probed": probed, "tiles_recomputed": flagged}
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import glsu
+    from glsu import synth
+    from glsu import train_surrogate as TS
+    if not torch.cuda.is_available():
+        raise RuntimeError("no CUDA device: the GB300 path has no CPU fallback")
+    torch.cuda.set_device(local)
+    size = args.size
+    N = size * size
+    wp = glsu.WffParams(*WFF)
+    seed = 1000 + rank
+    nfr = 8
+    frames, phi0, _ = synth.sequence(size, size, nfr, seed=seed)
+
+    # ---- AIA initial phase (5 frames, shifts U(0, 2pi), <= 30 iterations or 1e-4)
+    aframes, _, _ = synth.aia_frames(size, size, 5, seed=seed)
+    aia = glsu.AIA(5, size, size)
+    aia.run(list(aframes), None, max_iter=30, max_err=1e-4, seed=seed)  # warm
+    _, _, aia_ms, aia_iters, aia_err = aia.run(list(aframes), None, max_iter=30, max_err=1e-4, seed=seed)
+    aia.close()
+
+    stream = torch.cuda.Stream()
+    dfr = torch.from_numpy(frames).cuda()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    # ---- plain form: DPRA LS -> WFF2 -> update
+    dp = glsu.DPRA(phi0.astype(np.float32), 1, RADIUS, "f32", wp)
+    dp.set_stream(stream.cuda_stream)
+    dp.stage_timing(True)
+    p_val, p_ms, p_st, p_clk = timed_frames(glsu, torch, dp, dfr, nfr, args, stream, flush, world, local)
+    p_e2e = e2e_sequence(glsu, torch, dp, frames, nfr, args, stream, flush, world)
+    dp.close()
+
+    # ---- surrogate form: DPRA LS -> network -> probes -> per-tile fallback -> update
+    sur = None
+    try:
+        params, dil = TS.load()
+    except (OSError, KeyError) as e:
+        params, dil = None, None
+        sur = {"unavailable": "no trained weights (%s)" % e}
+    if params is not None:
+        ds = glsu.DPRA(phi0.astype(np.float32), 1, RADIUS, "f32", wp)
+        ds.set_stream(stream.cuda_stream)
+        ds.stage_timing(True)
+        ds.set_surrogate(params, dil, SUR_TILE, SUR_PATCH, SUR_TOL)
+        s_val, s_ms, s_st, s_clk = timed_frames(glsu, torch, ds, dfr, nfr, args, stream, flush, world, local)
+        probed, flagged = ds.surrogate_stats()
+        s_e2e = e2e_sequence(glsu, torch, ds, frames, nfr, args, stream, flush, world)
+        ds.close()
+        acc = surrogate_accuracy(glsu, torch, dfr, phi0, wp, params, dil, min(6, nfr - 1))
+        sur = {"frames_per_s": s_val, "ms_per_step": s_ms / args.steps, "speedup_vs_plain": s_val / p_val,
+               "e2e_frames_per_s": s_e2e,
+               "stages_ms": {"dpra_ls": s_st[0], "network": s_st[1], "wff2_probe": s_st[2],
+                             "fallback_and_update": s_st[3]},
+               "fallback_fraction_timed": flagged / probed if probed else None,
+               "probe": {"tile": SUR_TILE, "patch": SUR_PATCH, "tol_rad": SUR_TOL},
+               "dilations": dil, "params": int(params.size),
+               "accuracy_vs_plain_fp32": acc,
+               "rmse_target_rad": 0.02, "meets_rmse_target": acc["rmse"] <= 0.02}
+
+    # ---- rooflines
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
     peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
-    achieved = col_bytes / (st[2] * 1e-3) / 1e9
-    # FP32 work of the column sweep: 2 column filters of 2*sx+1 taps per
-    # frequency and output, complex data (2 FMA per tap), plus the halo rows.
+    pitch = (size + 127) // 128 * 128
+    col_bytes = 2 * NFX * size * pitch * 8  # read R_i planes + write C_i planes (complex64)
     sx = int(np.floor(3 * WFF[0] + 0.5))
     col_fma = NFX * NFY * N * 2 * (2 * sx + 1) * 2
-    sm_mhz = clk.get("sm_mhz") or 1900.0
+    sm_mhz = p_clk.get("sm_mhz") or 1900.0
     fp32_peak_tflops = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    fp32_tflops = 2 * col_fma / (st[2] * 1e-3) / 1e12
+    plain_roof = {"kernel": "wff_cols_kernel (WFF2 column sweep)", "bound": "hbm",
+                  "achieved": col_bytes / (p_st[2] * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                  "frac": col_bytes / (p_st[2] * 1e-3) / 1e9 / hbm_peak, "traffic": None,
+                  "peak_source": peak_kind, "algorithmic_bytes_per_launch": col_bytes,
+                  "fp32_pipe": {"achieved_tflops": 2 * col_fma / (p_st[2] * 1e-3) / 1e12,
+                                "peak_tflops_at_clock": fp32_peak_tflops,
+                                "frac": 2 * col_fma / (p_st[2] * 1e-3) / 1e12 / fp32_peak_tflops}}
+    roof = plain_roof
+    if sur and "stages_ms" in sur:
+        net_bytes = SUR_BYTES_PER_PX * N
+        net_ms = sur["stages_ms"]["network"]
+        net_roof = {"kernel": "surrogate network (sur_l0 + 6 x sur_conv_tc tcgen05 + sur_l7)", "bound": "hbm",
+                    "achieved": net_bytes / (net_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": net_bytes / (net_ms * 1e-3) / 1e9 / hbm_peak, "traffic": None,
+                    "peak_source": peak_kind, "algorithmic_bytes_per_launch": net_bytes,
+                    "tensor": {"achieved_tflops": SUR_FLOPS_PER_PX * N / (net_ms * 1e-3) / 1e12,
+                               "peak_tflops": bf16_peak,
+                               "frac": SUR_FLOPS_PER_PX * N / (net_ms * 1e-3) / 1e12 / bf16_peak}}
+        sur["roofline_network"] = net_roof
+        sur["roofline_plain_column_sweep"] = plain_roof
+        top = max(sur["stages_ms"], key=sur["stages_ms"].get)
+        roof = net_roof if top == "network" else plain_roof if top == "fallback_and_update" else net_roof
+        sur["dominant_stage"] = top
 
+    headline = sur if (sur and "frames_per_s" in sur) else None
     out = {
-        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "metric": METRIC, "value": headline["frames_per_s"] if headline else p_val, "unit": "frames/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": headline["ms_per_step"] if headline else p_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "form": "surrogate" if headline else "plain",
         "config": workload_config(size),
-        "clocks": clk,
-        "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": 4 * N, "d2h_bytes_per_step": 4 * N},
-        "gpu_launches": 4 * args.steps,
-        "stages_ms": {"dpra_ls": st[0], "wff_rows": st[1], "wff_column_sweep": st[2], "wff_final_update": st[3]},
-        "roofline": {"kernel": "wff_cols_kernel (WFF2 column sweep)", "bound": "hbm", "achieved": achieved,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
-                     "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": col_bytes,
-                     "fp32_pipe": {"achieved_tflops": fp32_tflops, "peak_tflops_at_clock": fp32_peak_tflops,
-                                   "frac": fp32_tflops / fp32_peak_tflops}},
+        "clocks": s_clk if headline else p_clk,
+        "e2e": {"value": headline["e2e_frames_per_s"] if headline else p_e2e, "unit": "frames/s",
+                "h2d_bytes_per_step": 4 * N, "d2h_bytes_per_step": 4 * N},
+        "gpu_launches": (SUR_LAUNCHES if headline else PLAIN_LAUNCHES) * args.steps,
+        "roofline": roof,
+        "plain": {"frames_per_s": p_val, "ms_per_step": p_ms / args.steps, "e2e_frames_per_s": p_e2e,
+                  "stages_ms": {"dpra_ls": p_st[0], "wff_rows": p_st[1], "wff_column_sweep": p_st[2],
+                                "wff_final_update": p_st[3]},
+                  "roofline": plain_roof, "clocks": p_clk, "gpu_launches_per_step": PLAIN_LAUNCHES},
+        "surrogate": sur,
         "aia": {"frames": 5, "ms": aia_ms, "iterations": aia_iters, "err": aia_err,
                 "ms_per_frame_over_200": aia_ms / 200},
     }

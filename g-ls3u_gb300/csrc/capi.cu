@@ -75,6 +75,7 @@ struct glsu_dpra {
     bool timing = false;
     bool unwrap = false;  // MATLAB fp_ls3u semantics: dphi = dphi_ref + unwrap(t)
     int unwrap_row = -1, unwrap_col = -1;
+    int ls_method = GLSU_LS_FLOAT_FLOAT;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     int frames_done = 0;
@@ -534,7 +535,8 @@ extern "C" int glsu_dpra_per_frame_device(glsu_dpra *h, const void *d_img, int i
     GLSU_TRY(dpra_check_type(h, img_type));
     cudaEvent_t *ev = h->timing ? h->ev : nullptr;
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[4], h->stream));
-    GLSU_TRY(launch_dpra_ls(h->prec, img_type, d_img, h->d_phi[GLSU_PHI_REF], h->d_z, h->W, h->H, h->r, h->stream));
+    GLSU_TRY(launch_dpra_ls(h->prec, img_type, d_img, h->d_phi[GLSU_PHI_REF], h->d_z, h->W, h->H, h->r, h->stream,
+                            h->ls_method));
     if (h->sur)
         GLSU_TRY(dpra_surrogate_frame(h, ev));
     else
@@ -609,6 +611,15 @@ extern "C" int glsu_dpra_get(glsu_dpra *h, int which, void *h_out)
     const size_t es = h->prec == GLSU_F32 ? 4 : 8;
     GLSU_CUDA_TRY(cudaMemcpyAsync(h_out, p, es * (size_t)h->W * h->H, cudaMemcpyDeviceToHost, h->stream));
     GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_set_ls_method(glsu_dpra *h, int method)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    if (method != GLSU_LS_FLOAT_FLOAT && method != GLSU_LS_FP64_SUMS)
+        return fail(GLSU_ERR_INVALID, "unknown least-squares method");
+    h->ls_method = method;
     return GLSU_OK;
 }
 

@@ -157,7 +157,7 @@ int launch_colfft(const WffPlan &P, cudaStream_t s);
 // kernel launchers
 // ---------------------------------------------------------------------------
 int launch_dpra_ls(int prec, int img_type, const void *d_img, const void *d_phiref, void *d_z, int W, int H,
-                   int r, cudaStream_t s);
+                   int r, cudaStream_t s, int method = GLSU_LS_FLOAT_FLOAT);
 int launch_dpra_update(int prec, const void *d_filtered, const void *phiref, const void *dphiref,
                        void *phicurr, void *dphi, int n, cudaStream_t s);
 // Line-scanning unwrapping in place; d_add (optional) is added to every

@@ -37,6 +37,7 @@ F32, F64, U8 = 0, 1, 2
 PHI_REF, PHI_CURR, DPHI_REF, DPHI = 0, 1, 2, 3
 WFT_WFF, WFT_WFR = 0, 1
 METHOD_AUTO, METHOD_DIRECT, METHOD_FFT = 0, 1, 2
+LS_FLOAT_FLOAT, LS_FP64_SUMS = 0, 1
 
 _lock = threading.Lock()
 _lib = None
@@ -151,6 +152,7 @@ def lib() -> ctypes.CDLL:
             "glsu_dpra_surrogate_stats": ([c_void_p, ctypes.POINTER(ctypes.c_longlong),
                                            ctypes.POINTER(ctypes.c_longlong), fltp, intp], c_int),
             "glsu_dpra_lsq_device": ([c_void_p, c_void_p], c_int),
+            "glsu_dpra_set_ls_method": ([c_void_p, c_int], c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -357,6 +359,10 @@ class DPRA:
     def set_method(self, method: int):
         """Column-sweep method of the WFF2: METHOD_AUTO, METHOD_DIRECT or METHOD_FFT."""
         check(lib().glsu_dpra_set_method(self._h, method))
+
+    def set_ls_method(self, method: int):
+        """FP32 least-squares arithmetic: LS_FLOAT_FLOAT (default) or LS_FP64_SUMS."""
+        check(lib().glsu_dpra_set_ls_method(self._h, method))
 
     def set_unwrap(self, enable: bool = True, start_row: int = -1, start_col: int = -1):
         """dphi = dphi_ref + unwrap(t) (MatLab/fp_ls3u.m:104) instead of dphi_ref + t."""

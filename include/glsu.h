@@ -59,6 +59,14 @@ extern "C" {
 #define GLSU_METHOD_DIRECT 1
 #define GLSU_METHOD_FFT 2
 
+/* Arithmetic of the FP32 DPRA least squares (glsu_dpra_set_ls_method): the
+ * window sums and the solve need more than FP32's 24 bits where phi_ref is
+ * locally smooth.  FLOAT_FLOAT forms them in float-float (pairs of FP32,
+ * about 48 bits) from FP32 regressors rotated to the tile centre; FP64_SUMS
+ * forms them in FP64.  FP64 handles always use FP64. */
+#define GLSU_LS_FLOAT_FLOAT 0
+#define GLSU_LS_FP64_SUMS 1
+
 /* WFT_TYPE of the reference (WFT-FPA.h enum WFT_TYPE) */
 #define GLSU_WFT_WFF 0
 #define GLSU_WFT_WFR 1
@@ -170,6 +178,8 @@ int glsu_dpra_update_ref_phi(glsu_dpra *h);
  * the same either way.  Returns when every output is on the host. */
 int glsu_dpra_sequence(glsu_dpra *h, int nframes, const void *h_frames, int img_type, void *h_dphi_all,
                        double *time_ms);
+/* GLSU_LS_FLOAT_FLOAT (default) or GLSU_LS_FP64_SUMS for FP32 handles. */
+int glsu_dpra_set_ls_method(glsu_dpra *h, int method);
 /* Copy the last frame's least-squares output exp(j dphi) (complex, W*H) to a
  * device buffer, enqueued on the handle's stream. */
 int glsu_dpra_lsq_device(glsu_dpra *h, void *d_out);

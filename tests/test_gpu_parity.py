@@ -118,9 +118,11 @@ def test_wff_threshold_is_kept_after_first_call(glsu, oracle):
     w.close()
 
 
-@pytest.mark.parametrize("prec,r,img", [("f32", 1, "u8"), ("f32", 3, "f32"), ("f32", 4, "f32"),
-                                        ("f64", 2, "f32"), ("f64", 3, "f64"), ("f64", 1, "u8")])
-def test_dpra_least_squares_matches_oracle(glsu, oracle, synth, prec, r, img):
+@pytest.mark.parametrize("prec,r,img,ls", [("f32", 1, "u8", 0), ("f32", 3, "f32", 0), ("f32", 4, "f32", 0),
+                                           ("f32", 3, "u8", 0), ("f32", 1, "u8", 1), ("f32", 3, "f32", 1),
+                                           ("f64", 2, "f32", 0), ("f64", 3, "f64", 0), ("f64", 1, "u8", 0)])
+def test_dpra_least_squares_matches_oracle(glsu, oracle, synth, prec, r, img, ls):
+    """FP32 form in both arithmetics (ls 0: float-float, 1: FP64 sums); FP64 form."""
     H, W = 61, 75
     frames, phi0, _ = synth.sequence(H, W, 3, seed=r)
     fr = frames[2]
@@ -130,13 +132,16 @@ def test_dpra_least_squares_matches_oracle(glsu, oracle, synth, prec, r, img):
         fr = fr.astype(np.float64)
     phi_in = phi0.astype(np.float32 if prec == "f32" else np.float64)
     d = glsu.DPRA(phi_in, 1, r, prec, glsu.WffParams(3.0, -0.5, 0.5, 0.5, 3.0, -0.5, 0.5, 0.5, 0.1))
+    if prec == "f32":
+        d.set_ls_method(ls)
     d.per_frame(fr)
     z = d.get_lsq()
     zr = oracle.dpra_ls(fr.astype(np.float64), phi_in.astype(np.float64), r)
     err = np.abs(np.angle(z * np.conj(zr)))
     kap = oracle.dpra_kappa(phi_in.astype(np.float64), r)
-    print("dpra LS %s r=%d %s: max %.3g rad, rms %.3g, min kappa %.2g" % (prec, r, img, err.max(),
-                                                                         np.sqrt(np.mean(err ** 2)), kap.min()))
+    print("dpra LS %s r=%d %s ls=%d: max %.3g rad, rms %.3g, min kappa %.2g" % (prec, r, img, ls, err.max(),
+                                                                                np.sqrt(np.mean(err ** 2)),
+                                                                                kap.min()))
     if prec == "f32":
         assert err.max() < 1e-4  # FP32 output rounding; the sums and the solve run in FP64
     else:

@@ -33,3 +33,27 @@ def test_bmp_reader_matches_fixture_frames(tmp_path):
     p = str(tmp_path / "f.bmp")
     write_bmp8(p, g["frames"][1])
     assert np.array_equal(io.read_bmp(p), g["frames"][1])
+
+
+def test_cpp_readers_match_python(tmp_path):
+    """include/glsu_io.hpp (reference names) on the reference's own phase map."""
+    import shutil
+    import subprocess
+    from glsu import io
+    gxx = shutil.which("g++")
+    if gxx is None:
+        import pytest
+        pytest.skip("g++ not available")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "test_io")
+    cuda_inc = "/usr/local/cuda/include"
+    subprocess.run([gxx, "-O1", "-std=c++17", "-I", os.path.join(root, "include"), "-I", cuda_inc,
+                    os.path.join(root, "tests", "cpp", "test_io.cpp"), "-o", exe], check=True)
+    src = os.path.join(GOLDEN, "phi_1.bin")
+    out = subprocess.run([exe, src, str(tmp_path / "o.bin"), str(tmp_path / "t.fp")], check=True,
+                         capture_output=True, text=True).stdout.split()
+    a = io.read_matrix_bin(src)
+    assert (int(out[0]), int(out[1])) == a.shape
+    assert abs(float(out[2]) - a.astype(np.float64).sum()) <= 1e-6 * np.abs(a).sum()
+    assert open(str(tmp_path / "o.bin"), "rb").read() == open(src, "rb").read()
+    assert io.read_complex_text(str(tmp_path / "t.fp")).shape == (2, 3)
