@@ -1,4 +1,5 @@
 // capi.cu -- the C ABI (include/glsu.h): handles, buffers, streams, timing.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -480,8 +481,12 @@ extern "C" int glsu_dpra_set_surrogate(glsu_dpra *h, const float *h_params, cons
     dpra_surrogate_release(h);
     if (!h_params) return GLSU_OK;
     if (h->prec != GLSU_F32) return fail(GLSU_ERR_UNSUPPORTED, "the surrogate form is FP32");
-    if (tol > 0 && (tile < 1 || patch < 1 || patch > kProbeMaxP || patch > tile))
-        return fail(GLSU_ERR_INVALID, "probe patch must be 1..8 and not above the tile size");
+    const int s_inst = std::max(h->wff.sxi, h->wff.syi);
+    if (tol > 0 && s_inst > 45)
+        return fail(GLSU_ERR_UNSUPPORTED, "the WFF2 probe supports window half-sizes up to 45");
+    if (tol > 0 && patch == 0) patch = probe_patch_for_half(s_inst);
+    if (tol > 0 && (tile < 1 || patch != probe_patch_for_half(s_inst) || patch > tile))
+        return fail(GLSU_ERR_INVALID, "probe patch must be 0 (default) or the window's patch size, within the tile");
     const size_t N = (size_t)h->W * h->H;
     h->sur = new SurNet();
     h->sur->stream = h->stream;
@@ -495,12 +500,14 @@ extern "C" int glsu_dpra_set_surrogate(glsu_dpra *h, const float *h_params, cons
         h->sur_ntx = (h->W + tile - 1) / tile;
         h->sur_nty = (h->H + tile - 1) / tile;
         const size_t nt = (size_t)h->sur_ntx * h->sur_nty;
-        if (cudaMalloc(&h->probe.partial, nt * h->wff.nfx * patch * patch * sizeof(float2)) != cudaSuccess ||
+        // partials: per tile, wx and part of the wy range (at most 4 parts)
+        if (cudaMalloc(&h->probe.partial, nt * h->wff.nfx * 4 * patch * patch * sizeof(float2)) != cudaSuccess ||
             cudaMalloc(&h->probe.sites, nt * sizeof(int2)) != cudaSuccess ||
             cudaMalloc(&h->probe.resid, nt * sizeof(float)) != cudaSuccess ||
             cudaMalloc(&h->probe.flags, nt * sizeof(int)) != cudaSuccess ||
             cudaMalloc(&h->probe.counts, 2 * sizeof(int)) != cudaSuccess)
             rc = fail(GLSU_ERR_ALLOC, "allocation failed");
+        if (rc == GLSU_OK) rc = h->wff.alloc_tile_list();
         if (rc == GLSU_OK && (cudaMemset(h->probe.counts, 0, 2 * sizeof(int)) != cudaSuccess ||
                               cudaMemset(h->probe.resid, 0, nt * sizeof(float)) != cudaSuccess))
             rc = fail(GLSU_ERR_CUDA, "memset failed");

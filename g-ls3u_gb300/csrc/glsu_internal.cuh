@@ -75,10 +75,12 @@ struct TileMask {
     __device__ __forceinline__ bool at(int y, int x) const { return flags[(y / tile) * ntx + x / tile] != 0; }
 };
 
-// Exact sparse WFF2 probe: per tile one P x P patch (P <= kProbeMaxP).
+// Exact sparse WFF2 probe: per tile one P x P patch, P = 8 for window
+// half-sizes (instantiated) up to 20, 4 above (P <= kProbeMaxP).
 constexpr int kProbeMaxP = 8;
+int probe_patch_for_half(int s_inst);
 struct ProbeOut {
-    float2 *partial = nullptr;  // [ntiles][nfx][P*P] per-wx partial sums
+    float2 *partial = nullptr;  // [ntiles][nfx * parts][P*P] partial sums
     int2 *sites = nullptr;      // [ntiles] (row, col) of each patch
     float *resid = nullptr;     // [ntiles] RMS phase residual of the surrogate
     int *flags = nullptr;       // [ntiles] residual > tolerance
@@ -127,11 +129,15 @@ struct WffPlan {
                 const void *dphi_ref, void *phi_curr, void *dphi, cudaEvent_t *stage_ev);
     int check_device_error(cudaStream_t s);
 
-    // Tile mask of the next enqueue (flags == nullptr: whole frame).
+    // Tile mask of the next enqueue (flags == nullptr: whole frame), and the
+    // device list of column tiles a masked run needs (alloc_tile_list).
     TileMask mask;
+    int2 *d_list = nullptr;
+    int *d_list_count = nullptr;
+    int alloc_tile_list();
     // Ensure the threshold on the device (automatic: from d_f, once).
     int ensure_threshold(cudaStream_t s, const void *d_f);
-    // FP32 only: exact WFF2 of d_f on one P x P patch per tile (patch
+    // FP32 only, half-sizes up to 45: exact WFF2 of d_f on one P x P patch per tile (patch
     // position hashed from seed and the tile), compared with d_cmp (complex,
     // the surrogate's output): RMS phase residual over patch pixels with
     // |WFF2| >= 0.1, flag when above tol.
@@ -182,6 +188,16 @@ struct SurConvArgs {
     uint16_t *out = nullptr;          // [B][H][W][32] BF16
     int relu = 1;
     int *err = nullptr;
+};
+// Weights of the two CUDA-core layers, passed to their kernels by value
+// (a shared-memory copy read once per FMA made these layers load-bound).
+struct SurL0W {
+    float w[32 * 18];  // [co][ci][t], BF16-rounded
+    float b[32];
+};
+struct SurL7W {
+    float w[2 * 288];  // [co][ci][t], BF16-rounded
+    float b[2];
 };
 int sur_make_map(CUtensorMap *tm, const void *act, int B, int H, int W, int dil);
 int launch_sur_conv(const CUtensorMap &tm, const SurConvArgs &a, cudaStream_t s);

@@ -17,6 +17,9 @@ constexpr int kSurSmallPix = 1024;      // pixels per block of the small weight-
 
 static int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, kSurPixBlocks); }
 
+// Blocks of the row-walking per-pixel kernels (a block takes whole image rows).
+int SurNet::rows_grid() const { return std::min(B * H, kSurPixBlocks); }
+
 int SurNet::init(int batch, int width, int height, const int *dilations, bool train)
 {
     if (batch < 1 || width < 1 || height < 1) return fail(GLSU_ERR_INVALID, "surrogate: bad batch or size");
@@ -74,6 +77,13 @@ int SurNet::pack()
 {
     sur_pack_kernel<<<(6 * 9216 + 255) / 256, 256, 0, stream>>>(d_master, d_pk_fwd, d_pk_bwd, d_w0r, d_w7r);
     GLSU_CUDA_TRY(cudaGetLastError());
+    // layers 0 and 7 take their weights as kernel parameters
+    const int off7 = sur_layer_offset(7);
+    GLSU_CUDA_TRY(cudaMemcpyAsync(h_w0.w, d_w0r, sizeof(h_w0.w), cudaMemcpyDeviceToHost, stream));
+    GLSU_CUDA_TRY(cudaMemcpyAsync(h_w0.b, d_master + 576, sizeof(h_w0.b), cudaMemcpyDeviceToHost, stream));
+    GLSU_CUDA_TRY(cudaMemcpyAsync(h_w7.w, d_w7r, sizeof(h_w7.w), cudaMemcpyDeviceToHost, stream));
+    GLSU_CUDA_TRY(cudaMemcpyAsync(h_w7.b, d_master + off7 + 576, sizeof(h_w7.b), cudaMemcpyDeviceToHost, stream));
+    GLSU_CUDA_TRY(cudaStreamSynchronize(stream));
     return GLSU_OK;
 }
 
@@ -112,8 +122,7 @@ int SurNet::check_error()
 // Layers 0..6: z -> a6 (training: d_act[0..6]; inference: ping-pong).
 int SurNet::hidden(const float2 *z)
 {
-    const size_t n = (size_t)B * H * W;
-    sur_l0_kernel<<<grid_for(n), 256, 0, stream>>>(z, B, H, W, dil[0], d_w0r, d_master + 576, d_act[0]);
+    sur_l0_kernel<<<rows_grid(), 256, 0, stream>>>(z, B, H, W, dil[0], h_w0, d_act[0]);
     GLSU_CUDA_TRY(cudaGetLastError());
     for (int l = 1; l <= 6; l++) {
         SurConvArgs a;
@@ -137,9 +146,7 @@ const uint16_t *SurNet::a6() const { return training ? d_act[6] : d_act[0]; }
 int SurNet::forward(const void *d_z, void *d_outp)
 {
     GLSU_TRY(hidden((const float2 *)d_z));
-    const size_t n = (size_t)B * H * W;
-    const float *w7b = d_master + sur_layer_offset(7) + 576;
-    sur_l7_kernel<<<grid_for(n), 256, 0, stream>>>(a6(), (const float2 *)d_z, B, H, W, dil[7], d_w7r, w7b,
+    sur_l7_kernel<<<rows_grid(), 256, 0, stream>>>(a6(), (const float2 *)d_z, B, H, W, dil[7], h_w7,
                                                    (float2 *)d_outp, nullptr, nullptr, nullptr);
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
@@ -148,12 +155,10 @@ int SurNet::forward(const void *d_z, void *d_outp)
 int SurNet::backward(const void *d_z, const void *d_target)
 {
     if (!training) return fail(GLSU_ERR_INVALID, "surrogate handle was not created for training");
-    const size_t n = (size_t)B * H * W;
     const float2 *z = (const float2 *)d_z;
     GLSU_TRY(hidden(z));
-    const int g = grid_for(n);
-    const float *w7b = d_master + sur_layer_offset(7) + 576;
-    sur_l7_kernel<<<g, 256, 0, stream>>>(d_act[6], z, B, H, W, dil[7], d_w7r, w7b, d_out,
+    const int g = rows_grid();
+    sur_l7_kernel<<<g, 256, 0, stream>>>(d_act[6], z, B, H, W, dil[7], h_w7, d_out,
                                          (const float2 *)d_target, d_dh, d_lpart);
     sur_sum_kernel<<<1, 32, 0, stream>>>(d_lpart, g, d_loss);
     // layer 7: weight gradient and dL/da6 (masked)

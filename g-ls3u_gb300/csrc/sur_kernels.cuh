@@ -22,14 +22,17 @@
 // 128 B apart.  A tap's horizontal offset dx * d is then just a shift of the
 // descriptor start by 16 * dx * d bytes, so the 9 taps read the same three
 // input rows without any im2col copy, and TMA zero-fills the image border.
-// A CTA walks one chain of output rows y = r, r + d, r + 2d, ... (the rows a
-// dilated tap pair shares) through a ring of input-row slots; the
-// accumulator is double-buffered in TMEM so the epilogue of row k overlaps
-// the MMAs of row k + 1.
+// Work items are chunks of a chain of output rows y = r, r + d, r + 2d, ...
+// (the rows that share input rows under dilation d).  The kernel is
+// persistent and warp-specialised: one thread streams every item's input
+// rows through a ring of slots by TMA, one thread issues the MMAs, four warps
+// drain the accumulator, which is double-buffered in TMEM so the epilogue of
+// one row overlaps the MMAs of the next.
 #pragma once
 
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "glsu_internal.cuh"
@@ -37,7 +40,7 @@
 
 namespace glsu {
 
-constexpr int kSurSlots = 6;     // input-row ring of the tensor-core conv
+constexpr int kSurSlots = 8;     // input-row ring of the tensor-core conv (TMA loads in flight)
 constexpr int kSurRows = 16;     // output rows per CTA (one chain segment)
 constexpr int kSurWBytes = 9 * 4 * 32 * 16;  // packed B operand of one layer
 
@@ -62,7 +65,36 @@ __device__ __forceinline__ void unpack8(const uint4 u, float *f)
 // ---------------------------------------------------------------------------
 // tensor-core 32 -> 32 conv (forward, or backward-data with flipped weights)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, 2) sur_conv_tc_kernel(const __grid_constant__ CUtensorMap tm, SurConvArgs a)
+// Work item: (image b, 128-pixel segment, residue r mod d, chunk of the
+// chain r, r+d, r+2d, ...), up to kSurRows output rows with 2 halo rows.
+struct SurItem {
+    int b, x0, r, kbeg, nout;
+};
+
+__device__ __forceinline__ SurItem sur_item(const SurConvArgs &a, int item)
+{
+    const int nsx = (a.W + 127) / 128;
+    const int nch = ((a.H + a.dil - 1) / a.dil + kSurRows - 1) / kSurRows;
+    SurItem it;
+    const int ch = item % nch;
+    item /= nch;
+    it.r = item % a.dil;
+    item /= a.dil;
+    it.x0 = (item % nsx) * 128;
+    it.b = item / nsx;
+    it.kbeg = ch * kSurRows;
+    const int chain_len = (a.H - it.r + a.dil - 1) / a.dil;  // rows r, r+d, ... below H
+    it.nout = max(0, min(kSurRows, chain_len - it.kbeg));
+    return it;
+}
+
+// Persistent, warp-specialised: thread 0 of warp 0 issues the TMA row loads
+// into a ring of kSurSlots slots, thread 0 of warp 1 issues the MMAs, warps
+// 4-7 drain the two TMEM accumulators.  All three walk the same item list
+// (blockIdx.x, + gridDim.x, ...); input rows and accumulators are numbered
+// across items, which keeps the mbarrier phases consistent.
+__global__ void __launch_bounds__(256, 1) sur_conv_tc_kernel(const __grid_constant__ CUtensorMap tm, SurConvArgs a,
+                                                             int nitems)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
     const int BW = 128 + 2 * a.dil;
@@ -76,23 +108,6 @@ __global__ void __launch_bounds__(256, 2) sur_conv_tc_kernel(const __grid_consta
     uint64_t *drain = acce + 2;
     float *bias_s = reinterpret_cast<float *>(drain + 1);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(bias_s + 32);
-
-    // work item: (image b, 128-pixel segment sx, residue r mod d, chain chunk)
-    const int nsx = (a.W + 127) / 128;
-    const int nch = ((a.H + a.dil - 1) / a.dil + kSurRows - 1) / kSurRows;
-    int item = blockIdx.x;
-    const int ch = item % nch;
-    item /= nch;
-    const int r = item % a.dil;
-    item /= a.dil;
-    const int sxi = item % nsx;
-    const int b = item / nsx;
-    const int x0 = sxi * 128;
-    const int kbeg = ch * kSurRows;
-    const int chain_len = (a.H - r + a.dil - 1) / a.dil;  // rows r, r+d, ... below H
-    const int nout = min(kSurRows, chain_len - kbeg);
-    if (b >= a.B || nout <= 0) return;  // uniform over the CTA, before any barrier or TMEM use
-    const int nin = nout + 2;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     for (int e = tid; e < kSurWBytes / 16; e += 256)
@@ -117,92 +132,116 @@ __global__ void __launch_bounds__(256, 2) sur_conv_tc_kernel(const __grid_consta
     tc_fence_after();
     const uint32_t tmem = *tslot;
 
-    if (tid == 0) {
-        // ---- producer (TMA) and MMA issuer ----
-        const uint32_t idesc = umma_idesc_bf16(128, 32);
-        const uint32_t wbase = smem_u32(wsm), sbase = smem_u32(slots);
-        const uint32_t lbo_a = (uint32_t)BW * 16;
-        int issued = 0;
+    if (warp == 0 && lane == 0) {
+        // ---- producer: TMA loads of every item's nout + 2 input rows ----
+        uint32_t g = 0;
         bool ok = true;
-        for (int k = 0; k < nout && ok; k++) {
-            while (issued < nin && issued <= k + kSurSlots - 2) {
-                const int s = issued % kSurSlots;
-                if (issued >= kSurSlots && !mbar_wait_bounded(&sfree[s], ((issued / kSurSlots) - 1) & 1)) {
+        for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+            const SurItem it = sur_item(a, item);
+            for (int j = 0; j < it.nout + 2 && it.nout > 0; j++, g++) {
+                const int s = g % kSurSlots;
+                if (g >= kSurSlots && !mbar_wait_bounded(&sfree[s], ((g / kSurSlots) - 1) & 1)) {
                     ok = false;
                     break;
                 }
                 mbar_expect_tx(&full[s], (uint32_t)BW * 64);
-                tma_load_5d(slots + s * slot_bytes, &tm, &full[s], 0, x0 - a.dil, 0, r + (kbeg + issued - 1) * a.dil,
-                            b);
-                issued++;
+                tma_load_5d(slots + s * slot_bytes, &tm, &full[s], 0, it.x0 - a.dil, 0,
+                            it.r + (it.kbeg + j - 1) * a.dil, it.b);
             }
-            if (!ok) break;
-            for (int j = (k == 0 ? 0 : k + 2); j <= k + 2; j++)
-                if (!mbar_wait_bounded(&full[j % kSurSlots], (j / kSurSlots) & 1)) ok = false;
-            if (ok && k >= 2 && !mbar_wait_bounded(&acce[k & 1], ((k >> 1) - 1) & 1)) ok = false;
-            if (!ok) break;
-            tc_fence_after();
-            const uint32_t d = tmem + (uint32_t)(k & 1) * 32;
-#pragma unroll
-            for (int dy = 0; dy < 3; dy++) {
-                const uint32_t srow = sbase + (uint32_t)(((k + dy) % kSurSlots) * slot_bytes);
-#pragma unroll
-                for (int dx = 0; dx < 3; dx++) {
-#pragma unroll
-                    for (int kc = 0; kc < 2; kc++) {
-                        const uint64_t ad = umma_desc(srow + kc * 2 * lbo_a + (uint32_t)(dx * a.dil * 16), lbo_a, 128);
-                        const uint64_t bd = umma_desc(wbase + (uint32_t)((dy * 3 + dx) * 2048 + kc * 1024), 512, 128);
-                        umma_bf16(d, ad, bd, idesc, (dy | dx | kc) ? 1u : 0u);
-                    }
-                }
-            }
-            umma_commit(&accf[k & 1]);
-            umma_commit(&sfree[k % kSurSlots]);  // input row k is not read again
         }
         if (!ok) atomicExch(a.err, GLSU_ERR_TIMEOUT);
-        // drain: the last load of every slot has landed, every MMA has completed
-        for (int j = max(0, issued - kSurSlots); j < issued; j++)
+        // every load has landed before the CTA exits
+        for (uint32_t j = g > (uint32_t)kSurSlots ? g - kSurSlots : 0; j < g; j++)
             mbar_wait_bounded(&full[j % kSurSlots], (j / kSurSlots) & 1);
-        umma_commit(drain);
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer ----
+        const uint32_t idesc = umma_idesc_bf16(128, 32);
+        const uint32_t wbase = smem_u32(wsm), sbase = smem_u32(slots);
+        const uint32_t lbo_a = (uint32_t)BW * 16;
+        uint32_t g0 = 0, waited = 0, acc = 0;
+        bool ok = true;
+        for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+            const SurItem it = sur_item(a, item);
+            if (it.nout <= 0) continue;
+            for (int k = 0; k < it.nout; k++, acc++) {
+                for (; waited < g0 + k + 3; waited++)
+                    if (!mbar_wait_bounded(&full[waited % kSurSlots], (waited / kSurSlots) & 1)) ok = false;
+                if (ok && acc >= 2 && !mbar_wait_bounded(&acce[acc & 1], ((acc >> 1) - 1) & 1)) ok = false;
+                if (!ok) break;
+                tc_fence_after();
+                const uint32_t d = tmem + (acc & 1) * 32;
+#pragma unroll
+                for (int dy = 0; dy < 3; dy++) {
+                    const uint32_t srow = sbase + (uint32_t)(((g0 + k + dy) % kSurSlots) * slot_bytes);
+#pragma unroll
+                    for (int dx = 0; dx < 3; dx++) {
+#pragma unroll
+                        for (int kc = 0; kc < 2; kc++) {
+                            const uint64_t ad =
+                                umma_desc(srow + kc * 2 * lbo_a + (uint32_t)(dx * a.dil * 16), lbo_a, 128);
+                            const uint64_t bd =
+                                umma_desc(wbase + (uint32_t)((dy * 3 + dx) * 2048 + kc * 1024), 512, 128);
+                            umma_bf16(d, ad, bd, idesc, (dy | dx | kc) ? 1u : 0u);
+                        }
+                    }
+                }
+                umma_commit(&accf[acc & 1]);
+                umma_commit(&sfree[(g0 + k) % kSurSlots]);  // input row g0 + k is not read again
+                if (k == it.nout - 1) {
+                    umma_commit(&sfree[(g0 + k + 1) % kSurSlots]);
+                    umma_commit(&sfree[(g0 + k + 2) % kSurSlots]);
+                }
+            }
+            g0 += it.nout + 2;
+        }
+        if (!ok) atomicExch(a.err, GLSU_ERR_TIMEOUT);
+        umma_commit(drain);  // every MMA has completed before TMEM is released
         mbar_wait_bounded(drain, 0);
     } else if (warp >= 4) {
         // ---- epilogue: TMEM -> bias, ReLU, mask -> BF16 NHWC ----
         const int q = warp - 4;
-        const int x = x0 + q * 32 + lane;
-        for (int k = 0; k < nout; k++) {
-            if (!mbar_wait_bounded(&accf[k & 1], (k >> 1) & 1)) {
-                if (lane == 0) atomicExch(a.err, GLSU_ERR_TIMEOUT);
-                break;
-            }
-            tc_fence_after();
-            float v[32];
-            tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(k & 1) * 32, v);
-            tc_fence_before();
-            mbar_arrive(&acce[k & 1]);
-            const int y = r + (kbeg + k) * a.dil;
-            if (x < a.W) {
-                const size_t off = (((size_t)b * a.H + y) * a.W + x) * 32;
-#pragma unroll
-                for (int c = 0; c < 32; c++) {
-                    v[c] += bias_s[c];
-                    if (a.relu) v[c] = fmaxf(v[c], 0.f);
+        uint32_t acc = 0;
+        bool ok = true;
+        for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+            const SurItem it = sur_item(a, item);
+            const int x = it.x0 + q * 32 + lane;
+            for (int k = 0; k < it.nout; k++, acc++) {
+                // warp-uniform: tcgen05.ld below is a warp-collective instruction
+                if (!__all_sync(0xffffffffu, mbar_wait_bounded(&accf[acc & 1], (acc >> 1) & 1))) {
+                    if (lane == 0) atomicExch(a.err, GLSU_ERR_TIMEOUT);
+                    ok = false;
+                    break;
                 }
-                if (a.mask) {
-                    const uint4 *mp = reinterpret_cast<const uint4 *>(a.mask + off);
+                tc_fence_after();
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (acc & 1) * 32, v);
+                tc_fence_before();
+                mbar_arrive(&acce[acc & 1]);
+                const int y = it.r + (it.kbeg + k) * a.dil;
+                if (x < a.W) {
+                    const size_t off = (((size_t)it.b * a.H + y) * a.W + x) * 32;
 #pragma unroll
-                    for (int g = 0; g < 4; g++) {
-                        float mv[8];
-                        unpack8(mp[g], mv);
-#pragma unroll
-                        for (int i = 0; i < 8; i++)
-                            if (!(mv[i] > 0.f)) v[8 * g + i] = 0.f;
+                    for (int c = 0; c < 32; c++) {
+                        v[c] += bias_s[c];
+                        if (a.relu) v[c] = fmaxf(v[c], 0.f);
                     }
-                }
-                uint4 *op = reinterpret_cast<uint4 *>(a.out + off);
+                    if (a.mask) {
+                        const uint4 *mp = reinterpret_cast<const uint4 *>(a.mask + off);
 #pragma unroll
-                for (int g = 0; g < 4; g++)
-                    op[g] = make_uint4(pack_bf2(v[8 * g], v[8 * g + 1]), pack_bf2(v[8 * g + 2], v[8 * g + 3]),
-                                       pack_bf2(v[8 * g + 4], v[8 * g + 5]), pack_bf2(v[8 * g + 6], v[8 * g + 7]));
+                        for (int g = 0; g < 4; g++) {
+                            float mv[8];
+                            unpack8(mp[g], mv);
+#pragma unroll
+                            for (int i = 0; i < 8; i++)
+                                if (!(mv[i] > 0.f)) v[8 * g + i] = 0.f;
+                        }
+                    }
+                    uint4 *op = reinterpret_cast<uint4 *>(a.out + off);
+#pragma unroll
+                    for (int g = 0; g < 4; g++)
+                        op[g] = make_uint4(pack_bf2(v[8 * g], v[8 * g + 1]), pack_bf2(v[8 * g + 2], v[8 * g + 3]),
+                                           pack_bf2(v[8 * g + 4], v[8 * g + 5]), pack_bf2(v[8 * g + 6], v[8 * g + 7]));
+                }
             }
         }
     }
@@ -219,7 +258,7 @@ int sur_conv_smem_bytes(int dil)
     return kSurWBytes + kSurSlots * slot_bytes + (2 * kSurSlots + 5) * 8 + 32 * 4 + 16;
 }
 
-int sur_conv_grid(int B, int H, int W, int dil)
+int sur_conv_items(int B, int H, int W, int dil)
 {
     const int nsx = (W + 127) / 128;
     const int nch = ((H + dil - 1) / dil + kSurRows - 1) / kSurRows;
@@ -247,14 +286,34 @@ int sur_make_map(CUtensorMap *tm, const void *act, int B, int H, int W, int dil)
 
 int launch_sur_conv(const CUtensorMap &tm, const SurConvArgs &a, cudaStream_t s)
 {
-    static int attr_bytes = 0;
+    static int attr_bytes = 0, sms = 0, regs = 0;
     const int smem = sur_conv_smem_bytes(a.dil);
     if (smem > attr_bytes) {
         GLSU_CUDA_TRY(cudaFuncSetAttribute(sur_conv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            sur_conv_smem_bytes(64)));
+        GLSU_CUDA_TRY(cudaFuncSetAttribute(sur_conv_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                           (int)cudaSharedmemCarveoutMaxShared));
         attr_bytes = sur_conv_smem_bytes(64);
     }
-    sur_conv_tc_kernel<<<sur_conv_grid(a.B, a.H, a.W, a.dil), 256, smem, s>>>(tm, a);
+    if (!sms) {
+        int dev = 0;
+        GLSU_CUDA_TRY(cudaGetDevice(&dev));
+        GLSU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        cudaFuncAttributes fa;
+        GLSU_CUDA_TRY(cudaFuncGetAttributes(&fa, sur_conv_tc_kernel));
+        regs = std::max(1, fa.numRegs);
+    }
+    // persistent: as many CTAs as are resident at once, each walking a
+    // strided list of items.  Residency is bounded by registers (per-warp
+    // allocation in units of 256), shared memory (1 KB reserved per CTA) and
+    // the 512 TMEM columns (64 per CTA).
+    const int warp_regs = (regs * 32 + 255) / 256 * 256;
+    const int by_regs = 65536 / (8 * warp_regs);
+    const int by_smem = (228 * 1024) / (smem + 1024);
+    const int per_sm = std::max(1, std::min(std::min(by_regs, by_smem), 8));
+    const int items = sur_conv_items(a.B, a.H, a.W, a.dil);
+    const int grid = std::min(items, per_sm * sms);
+    sur_conv_tc_kernel<<<grid, 256, smem, s>>>(tm, a, items);
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
 }
@@ -262,101 +321,112 @@ int launch_sur_conv(const CUtensorMap &tm, const SurConvArgs &a, cudaStream_t s)
 // ---------------------------------------------------------------------------
 // layer 0 (2 -> 32) and layer 7 (32 -> 2) on CUDA cores
 // ---------------------------------------------------------------------------
-// w0: [32][2][9] (BF16-rounded FP32), b0[32]; z: complex [B][H][W]
+// Layer 0 (2 -> 32, ReLU); z: complex [B][H][W].  The weights are kernel
+// parameters, so every FMA takes its weight from the parameter bank.
 __global__ void __launch_bounds__(256) sur_l0_kernel(const float2 *__restrict__ z, int B, int H, int W, int dil,
-                                                     const float *__restrict__ w0, const float *__restrict__ b0,
-                                                     uint16_t *__restrict__ out)
+                                                     const __grid_constant__ SurL0W wp, uint16_t *__restrict__ out)
 {
-    __shared__ float ws[32 * 18 + 32];
-    for (int e = threadIdx.x; e < 32 * 18; e += 256) ws[e] = w0[e];
-    if (threadIdx.x < 32) ws[576 + threadIdx.x] = b0[threadIdx.x];
-    __syncthreads();
-    const size_t n = (size_t)B * H * W;
-    for (size_t p = (size_t)blockIdx.x * 256 + threadIdx.x; p < n; p += (size_t)gridDim.x * 256) {
-        const int x = (int)(p % W);
-        const int y = (int)((p / W) % H);
-        const size_t img = p - (size_t)y * W - x;
-        float in[18];
+    for (int row = blockIdx.x; row < B * H; row += gridDim.x)
+        for (int x = threadIdx.x; x < W; x += 256) {
+            const int y = row % H;
+            const size_t p = (size_t)row * W + x;
+            const size_t img = (size_t)(row - y) * W;
+            float in[18];
 #pragma unroll
-        for (int t = 0; t < 9; t++) {
-            const int yy = y + (t / 3 - 1) * dil, xx = x + (t % 3 - 1) * dil;
-            float2 v = make_float2(0.f, 0.f);
-            if (yy >= 0 && yy < H && xx >= 0 && xx < W) v = z[img + (size_t)yy * W + xx];
-            in[t] = v.x;
-            in[9 + t] = v.y;
+            for (int t = 0; t < 9; t++) {
+                const int yy = y + (t / 3 - 1) * dil, xx = x + (t % 3 - 1) * dil;
+                float2 v = make_float2(0.f, 0.f);
+                if (yy >= 0 && yy < H && xx >= 0 && xx < W) v = z[img + (size_t)yy * W + xx];
+                in[t] = v.x;
+                in[9 + t] = v.y;
+            }
+            float acc[32];
+#pragma unroll
+            for (int c = 0; c < 32; c++) {
+                float s = wp.b[c];
+#pragma unroll
+                for (int k = 0; k < 18; k++) s = fmaf(wp.w[c * 18 + k], in[k], s);
+                acc[c] = fmaxf(s, 0.f);
+            }
+            uint4 *op = reinterpret_cast<uint4 *>(out + p * 32);
+#pragma unroll
+            for (int g = 0; g < 4; g++)
+                op[g] = make_uint4(pack_bf2(acc[8 * g], acc[8 * g + 1]), pack_bf2(acc[8 * g + 2], acc[8 * g + 3]),
+                                   pack_bf2(acc[8 * g + 4], acc[8 * g + 5]), pack_bf2(acc[8 * g + 6], acc[8 * g + 7]));
         }
-        float acc[32];
-#pragma unroll
-        for (int c = 0; c < 32; c++) {
-            float s = ws[576 + c];
-#pragma unroll
-            for (int k = 0; k < 18; k++) s = fmaf(ws[c * 18 + k], in[k], s);
-            acc[c] = fmaxf(s, 0.f);
-        }
-        uint4 *op = reinterpret_cast<uint4 *>(out + p * 32);
-#pragma unroll
-        for (int g = 0; g < 4; g++)
-            op[g] = make_uint4(pack_bf2(acc[8 * g], acc[8 * g + 1]), pack_bf2(acc[8 * g + 2], acc[8 * g + 3]),
-                               pack_bf2(acc[8 * g + 4], acc[8 * g + 5]), pack_bf2(acc[8 * g + 6], acc[8 * g + 7]));
-    }
 }
 
-// Last layer, residual, renormalisation.  w7: [2][32][9], b7[2].
-// Writes out = y/|y| (complex).  With a target (training): per pixel loss
-// wgt |out - t|^2, wgt = min(|target|, 1), t = target/|target|, and the
-// gradient dL/dh7 of the mean loss into dh; per-block loss sums into part.
-__global__ void __launch_bounds__(256) sur_l7_kernel(const uint16_t *__restrict__ a6, const float2 *__restrict__ z,
-                                                     int B, int H, int W, int dil, const float *__restrict__ w7,
-                                                     const float *__restrict__ b7, float2 *__restrict__ out,
-                                                     const float2 *__restrict__ target, float2 *__restrict__ dh,
-                                                     double *__restrict__ part)
+// Last layer, residual, renormalisation: out = y/|y|, y = z + conv7(a6).
+// Four lanes per pixel, each owning 8 of the 32 input channels (one 16-byte
+// chunk), so a warp's loads cover 8 neighbouring pixels contiguously; the
+// weights sit in shared memory as [chunk][tap][co][8] (chunk stride padded
+// to 148 floats: the four chunk groups of a warp read disjoint banks, two
+// 16-byte loads per tap and output) and two shuffles combine the partial
+// sums.  With a target (training): per pixel loss wgt |out - t|^2, wgt =
+// min(|target|, 1), t = target/|target|, the gradient dL/dh7 of the mean
+// loss into dh, and per-block loss sums into part.
+__global__ void __launch_bounds__(256, 2) sur_l7_kernel(const uint16_t *__restrict__ a6, const float2 *__restrict__ z,
+                                                        int B, int H, int W, int dil,
+                                                        const __grid_constant__ SurL7W wp, float2 *__restrict__ out,
+                                                        const float2 *__restrict__ target, float2 *__restrict__ dh,
+                                                        double *__restrict__ part)
 {
-    __shared__ float ws[2 * 32 * 9 + 2];
+    constexpr int kCS = 148;  // chunk stride (floats)
     __shared__ double red[256];
-    for (int e = threadIdx.x; e < 576; e += 256) ws[e] = w7[e];
-    if (threadIdx.x < 2) ws[576 + threadIdx.x] = b7[threadIdx.x];
+    __shared__ __align__(16) float ws[4 * kCS];
+    for (int e = threadIdx.x; e < 576; e += 256) {
+        const int co = e / 288, ci = (e / 9) % 32, t = e % 9;
+        ws[(ci >> 3) * kCS + (t * 2 + co) * 8 + (ci & 7)] = wp.w[e];
+    }
     __syncthreads();
-    const size_t n = (size_t)B * H * W;
-    const double inv_n = 1.0 / (double)n;
+    const int chunk = threadIdx.x & 3;
+    const float *wc = ws + chunk * kCS;
+    const double inv_n = 1.0 / ((double)B * H * W);
     double lsum = 0;
-    for (size_t p = (size_t)blockIdx.x * 256 + threadIdx.x; p < n; p += (size_t)gridDim.x * 256) {
-        const int x = (int)(p % W);
-        const int y = (int)((p / W) % H);
-        const size_t img = p - (size_t)y * W - x;
-        float h0 = ws[576], h1 = ws[577];
+    for (int row = blockIdx.x; row < B * H; row += gridDim.x) {
+        const int y = row % H;
+        const size_t img = (size_t)(row - y) * W;
+        for (int xb = 0; xb < W; xb += 64) {  // warp-uniform bound: every lane takes part in the shuffles
+            const int x = xb + (threadIdx.x >> 2);
+            const bool act = x < W;
+            float h0 = 0.f, h1 = 0.f;
 #pragma unroll
-        for (int t = 0; t < 9; t++) {
-            const int yy = y + (t / 3 - 1) * dil, xx = x + (t % 3 - 1) * dil;
-            if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
-            const uint4 *ap = reinterpret_cast<const uint4 *>(a6 + (img + (size_t)yy * W + xx) * 32);
-#pragma unroll
-            for (int g = 0; g < 4; g++) {
+            for (int t = 0; t < 9; t++) {
+                const int yy = y + (t / 3 - 1) * dil, xx = x + (t % 3 - 1) * dil;
+                if (!act || yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
                 float av[8];
-                unpack8(ap[g], av);
-#pragma unroll
-                for (int i = 0; i < 8; i++) {
-                    h0 = fmaf(ws[(8 * g + i) * 9 + t], av[i], h0);
-                    h1 = fmaf(ws[288 + (8 * g + i) * 9 + t], av[i], h1);
-                }
+                unpack8(reinterpret_cast<const uint4 *>(a6 + (img + (size_t)yy * W + xx) * 32)[chunk], av);
+                const float4 *w4 = reinterpret_cast<const float4 *>(wc + t * 16);
+                const float4 a0 = w4[0], a1 = w4[1], b0 = w4[2], b1 = w4[3];
+                h0 = fmaf(a0.x, av[0], fmaf(a0.y, av[1], fmaf(a0.z, av[2], fmaf(a0.w, av[3], h0))));
+                h0 = fmaf(a1.x, av[4], fmaf(a1.y, av[5], fmaf(a1.z, av[6], fmaf(a1.w, av[7], h0))));
+                h1 = fmaf(b0.x, av[0], fmaf(b0.y, av[1], fmaf(b0.z, av[2], fmaf(b0.w, av[3], h1))));
+                h1 = fmaf(b1.x, av[4], fmaf(b1.y, av[5], fmaf(b1.z, av[6], fmaf(b1.w, av[7], h1))));
             }
-        }
-        const float2 xv = z[p];
-        const float yr = xv.x + h0, yi = xv.y + h1;
-        const float nrm = sqrtf(yr * yr + yi * yi);
-        const float inv = nrm > 1e-20f ? 1.f / nrm : 0.f;
-        const float orr = yr * inv, oii = yi * inv;
-        out[p] = make_float2(orr, oii);
-        if (target) {
-            const float2 tv = target[p];
-            const float tn = sqrtf(tv.x * tv.x + tv.y * tv.y);
-            const float wgt = fminf(tn, 1.f);
-            const float ti = tn > 1e-20f ? 1.f / tn : 0.f;
-            const float er = orr - tv.x * ti, ei = oii - tv.y * ti;
-            lsum += (double)(wgt * (er * er + ei * ei));
-            // d out: 2 wgt e / n; through out = y/|y|: (g - out (out.g)) / |y|
-            const float gr = (float)(2.0 * inv_n) * wgt * er, gi = (float)(2.0 * inv_n) * wgt * ei;
-            const float dot = orr * gr + oii * gi;
-            dh[p] = make_float2((gr - orr * dot) * inv, (gi - oii * dot) * inv);
+            h0 += __shfl_xor_sync(0xffffffffu, h0, 1);
+            h1 += __shfl_xor_sync(0xffffffffu, h1, 1);
+            h0 += __shfl_xor_sync(0xffffffffu, h0, 2);
+            h1 += __shfl_xor_sync(0xffffffffu, h1, 2);
+            if (!act || chunk != 0) continue;
+            const size_t p = img + (size_t)y * W + x;
+            const float2 xv = z[p];
+            const float yr = xv.x + (h0 + wp.b[0]), yi = xv.y + (h1 + wp.b[1]);
+            const float nrm = sqrtf(yr * yr + yi * yi);
+            const float inv = nrm > 1e-20f ? 1.f / nrm : 0.f;
+            const float orr = yr * inv, oii = yi * inv;
+            out[p] = make_float2(orr, oii);
+            if (target) {
+                const float2 tv = target[p];
+                const float tn = sqrtf(tv.x * tv.x + tv.y * tv.y);
+                const float wgt = fminf(tn, 1.f);
+                const float ti = tn > 1e-20f ? 1.f / tn : 0.f;
+                const float er = orr - tv.x * ti, ei = oii - tv.y * ti;
+                lsum += (double)(wgt * (er * er + ei * ei));
+                // d out: 2 wgt e / n; through out = y/|y|: (g - out (out.g)) / |y|
+                const float gr = (float)(2.0 * inv_n) * wgt * er, gi = (float)(2.0 * inv_n) * wgt * ei;
+                const float dot = orr * gr + oii * gi;
+                dh[p] = make_float2((gr - orr * dot) * inv, (gi - oii * dot) * inv);
+            }
         }
     }
     if (target) {
@@ -380,11 +450,11 @@ __global__ void __launch_bounds__(256) sur_l7_bwd_kernel(const float2 *__restric
     __shared__ float ws[576];
     for (int e = threadIdx.x; e < 576; e += 256) ws[e] = w7[e];
     __syncthreads();
-    const size_t n = (size_t)B * H * W;
-    for (size_t p = (size_t)blockIdx.x * 256 + threadIdx.x; p < n; p += (size_t)gridDim.x * 256) {
-        const int x = (int)(p % W);
-        const int y = (int)((p / W) % H);
-        const size_t img = p - (size_t)y * W - x;
+    for (int row = blockIdx.x; row < B * H; row += gridDim.x)
+    for (int x = threadIdx.x; x < W; x += 256) {
+        const int y = row % H;
+        const size_t p = (size_t)row * W + x;
+        const size_t img = (size_t)(row - y) * W;
         float acc[32];
 #pragma unroll
         for (int c = 0; c < 32; c++) acc[c] = 0.f;

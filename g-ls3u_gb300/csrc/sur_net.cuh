@@ -1,5 +1,5 @@
 // sur_net.cuh -- the surrogate network object shared by the C ABI and the
-// DPRA handle (see sur_kernels.cu for the network and its kernels).
+// DPRA handle (see sur_kernels.cuh for the network and its kernels).
 #pragma once
 
 #include "glsu_internal.cuh"
@@ -16,6 +16,8 @@ struct SurNet {
     float *d_master = nullptr;
     uint16_t *d_pk_fwd = nullptr, *d_pk_bwd = nullptr;
     float *d_w0r = nullptr, *d_w7r = nullptr;
+    SurL0W h_w0;  // host copies of layers 0 and 7 (kernel-parameter weights)
+    SurL7W h_w7;
     // activations [B][H][W][32] BF16: training keeps a0..a6, inference ping-pongs two
     uint16_t *d_act[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     // training
@@ -40,6 +42,7 @@ struct SurNet {
     int backward(const void *d_z, const void *d_target);
     int adam(float lr, float b1, float b2, float eps);
     int check_error();
+    int rows_grid() const;
 };
 
 }  // namespace glsu

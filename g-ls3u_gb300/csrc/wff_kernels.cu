@@ -173,26 +173,18 @@ __global__ void __launch_bounds__(256) wff_rows_demod_kernel(const C2<T> *__rest
 // ---------------------------------------------------------------------------
 // B: column sweep over all wy for one wx and one 32-column tile
 // ---------------------------------------------------------------------------
+// One 32-column x TY-row tile of the sweep for wx index i; the mbarrier
+// phase of this tile's TMA load is `parity`.  False when the load timed out.
 template <typename T, int S>
-__global__ void __launch_bounds__(ColGeom<T, S>::THREADS, 1)
-    wff_cols_kernel(const __grid_constant__ CUtensorMap tmR, C2<T> *__restrict__ Cout,
-                    const C2<T> *__restrict__ ey, int nfy, int H, int pitch, const T *__restrict__ thr_ptr,
-                    Taps<T, S> gA, Taps<T, S> gB, int *__restrict__ err, TileMask tm)
+__device__ __forceinline__ bool cols_tile(const CUtensorMap &tmR, C2<T> *__restrict__ Cout,
+                                          const C2<T> *__restrict__ ey, int nfy, int H, int pitch, T thr, T thr2,
+                                          const Taps<T, S> &gA, const Taps<T, S> &gB, int *__restrict__ err,
+                                          C2<T> *Rt, C2<T> *tt, uint64_t *bar, uint32_t parity, int x0, int y0,
+                                          int i)
 {
     using G = ColGeom<T, S>;
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
-    C2<T> *Rt = reinterpret_cast<C2<T> *>(smem_raw);
-    C2<T> *tt = Rt + G::RT * 32;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(tt + G::TT * 32);
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * G::TY, i = blockIdx.z;
-    if (tm.flags && !tm.any(y0, y0 + G::TY, x0, x0 + 32)) return;  // before any barrier or copy
-
-    if (tid == 0) {
-        mbar_init(bar, 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
+    const size_t eys = (size_t)H + 2 * kPhasorPad;
     if (tid == 0) {
         mbar_expect_tx(bar, G::TX_BYTES);
 #pragma unroll 1
@@ -200,19 +192,16 @@ __global__ void __launch_bounds__(ColGeom<T, S>::THREADS, 1)
             tma_load_3d(Rt + b * G::BOX * 32, &tmR, bar, x0 * G::FPC, y0 - 2 * S + b * G::BOX, i);
     }
     for (int e = G::NBOX * G::BOX * 32 + tid; e < G::RT * 32; e += G::THREADS) Rt[e] = mk<T>(0, 0);
-    const bool late = !mbar_wait_bounded(bar, 0);
+    const bool late = !mbar_wait_bounded(bar, parity);
     if (__syncthreads_or(late)) {
         if (tid == 0) {
             atomicExch(err, GLSU_ERR_TIMEOUT);
-            mbar_wait_bounded(bar, 0);  // let copies still in flight land before exit
+            mbar_wait_bounded(bar, parity);  // let copies still in flight land before exit
         }
         __syncthreads();
-        return;
+        return false;
     }
 
-    const T thr = *thr_ptr;
-    const T thr2 = thr * thr;
-    const size_t eys = (size_t)H + 2 * kPhasorPad;
     T cr_acc[G::KC], ci_acc[G::KC];
 #pragma unroll
     for (int k = 0; k < G::KC; k++) {
@@ -289,6 +278,95 @@ __global__ void __launch_bounds__(ColGeom<T, S>::THREADS, 1)
         const int gr = y0 + w * G::KC + kk;
         if (gr < H) Ci[(size_t)gr * pitch + x0 + lane] = mk<T>(cr_acc[kk], ci_acc[kk]);
     }
+    return true;
+}
+
+template <typename T, int S>
+__global__ void __launch_bounds__(ColGeom<T, S>::THREADS, 1)
+    wff_cols_kernel(const __grid_constant__ CUtensorMap tmR, C2<T> *__restrict__ Cout,
+                    const C2<T> *__restrict__ ey, int nfy, int H, int pitch, const T *__restrict__ thr_ptr,
+                    Taps<T, S> gA, Taps<T, S> gB, int *__restrict__ err)
+{
+    using G = ColGeom<T, S>;
+    extern __shared__ __align__(1024) unsigned char smem_cols[];
+    C2<T> *Rt = reinterpret_cast<C2<T> *>(smem_cols);
+    C2<T> *tt = Rt + G::RT * 32;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(tt + G::TT * 32);
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const T thr = *thr_ptr;
+    cols_tile<T, S>(tmR, Cout, ey, nfy, H, pitch, thr, thr * thr, gA, gB, err, Rt, tt, bar, 0,
+                    blockIdx.x * 32, blockIdx.y * G::TY, blockIdx.z);
+}
+
+// Tile-masked runs: the CTAs of each wx walk the device list of needed tiles.
+template <typename T, int S>
+__global__ void __launch_bounds__(ColGeom<T, S>::THREADS, 1)
+    wff_cols_list_kernel(const __grid_constant__ CUtensorMap tmR, C2<T> *__restrict__ Cout,
+                         const C2<T> *__restrict__ ey, int nfy, int H, int pitch, const T *__restrict__ thr_ptr,
+                         Taps<T, S> gA, Taps<T, S> gB, int *__restrict__ err, const int2 *__restrict__ list,
+                         const int *__restrict__ list_count)
+{
+    using G = ColGeom<T, S>;
+    extern __shared__ __align__(1024) unsigned char smem_cols[];
+    C2<T> *Rt = reinterpret_cast<C2<T> *>(smem_cols);
+    C2<T> *tt = Rt + G::RT * 32;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(tt + G::TT * 32);
+    const int nitems = *list_count;
+    if ((int)blockIdx.x >= nitems) return;  // uniform, before any barrier or copy
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const T thr = *thr_ptr;
+    uint32_t iter = 0;
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x, iter++) {
+        const int2 tile = list[item];
+        __syncthreads();  // the previous item is done with Rt and tt
+        if (!cols_tile<T, S>(tmR, Cout, ey, nfy, H, pitch, thr, thr * thr, gA, gB, err, Rt, tt, bar, iter & 1,
+                             tile.x * 32, tile.y * G::TY, blockIdx.z))
+            return;
+    }
+}
+
+// Tiles (bx, by) of the column sweep whose outputs, grown by (0, mx), meet a
+// flagged tile, compacted in index order (one block; deterministic).
+__global__ void __launch_bounds__(1024) wff_mask_list_kernel(TileMask m, int ncx, int ncy, int ty_rows,
+                                                             int2 *__restrict__ list, int *__restrict__ count)
+{
+    __shared__ int warp_sums[32];
+    __shared__ int base;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    const int n = ncx * ncy;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int c0 = 0; c0 < n; c0 += 1024) {
+        const int e = c0 + threadIdx.x;
+        int need = 0, bx = 0, by = 0;
+        if (e < n) {
+            by = e / ncx;
+            bx = e - by * ncx;
+            need = m.any(by * ty_rows, by * ty_rows + ty_rows, bx * 32, bx * 32 + 32) ? 1 : 0;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, need);
+        if (lane == 0) warp_sums[w] = __popc(bal);
+        __syncthreads();
+        int before = 0;
+        for (int q = 0; q < w; q++) before += warp_sums[q];
+        if (need) list[base + before + __popc(bal & ((1u << lane) - 1u))] = make_int2(bx, by);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int q = 0; q < 32; q++) tot += warp_sums[q];
+            base += tot;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *count = base;
 }
 
 // ---------------------------------------------------------------------------
@@ -596,12 +674,27 @@ int WffPlan::make_tensor_map()
     return GLSU_OK;
 }
 
+int WffPlan::alloc_tile_list()
+{
+    if (d_list) return GLSU_OK;
+    // column tiles are 32 columns x at least 32 rows
+    const size_t cap = (size_t)(pitch / 32) * ((H + 31) / 32);
+    if (cudaMalloc((void **)&d_list, cap * sizeof(int2)) != cudaSuccess ||
+        cudaMalloc((void **)&d_list_count, sizeof(int)) != cudaSuccess)
+        return fail(GLSU_ERR_ALLOC, "cudaMalloc of the tile list failed");
+    return GLSU_OK;
+}
+
 void WffPlan::release()
 {
     release_colfft();
     cudaFree(d_ex);
     cudaFree(d_ey);
+    cudaFree(d_list);
+    cudaFree(d_list_count);
     d_ex = d_ey = nullptr;
+    d_list = nullptr;
+    d_list_count = nullptr;
     if (!external_scratch) {
         cudaFree(d_R);
         cudaFree(d_C);
@@ -671,12 +764,29 @@ template <typename T, int S> static int launch_cols(const WffPlan &P, cudaStream
             cudaFuncSetAttribute(wff_cols_kernel<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM));
         attr = true;
     }
-    dim3 grid(P.pitch / 32, (P.H + G::TY - 1) / G::TY, P.nfx);
-    wff_cols_kernel<T, S><<<grid, G::THREADS, G::SMEM, s>>>(P.tmR, (C2<T> *)P.d_C, (const C2<T> *)P.d_ey, P.nfy, P.H,
-                                                       P.pitch, (const T *)P.d_thr,
-                                                       make_taps<T, S>(P.gy, P.sy, P.inv_norm),
-                                                       make_taps<T, S>(P.gy, P.sy, 1.0), P.d_err,
-                                                       with_margins(P.mask, 0, P.sx));
+    const int ncx = P.pitch / 32, ncy = (P.H + G::TY - 1) / G::TY;
+    const Taps<T, S> gA = make_taps<T, S>(P.gy, P.sy, P.inv_norm), gB = make_taps<T, S>(P.gy, P.sy, 1.0);
+    if (!P.mask.flags) {
+        wff_cols_kernel<T, S><<<dim3(ncx, ncy, P.nfx), G::THREADS, G::SMEM, s>>>(
+            P.tmR, (C2<T> *)P.d_C, (const C2<T> *)P.d_ey, P.nfy, P.H, P.pitch, (const T *)P.d_thr, gA, gB, P.d_err);
+    } else {
+        // tile-masked run: compact the needed column tiles on the device and
+        // let a few CTAs per wx walk that list (an empty list costs one short
+        // launch instead of a full grid of CTAs that exit at once)
+        static bool attr_l = false;
+        if (!attr_l) {
+            GLSU_CUDA_TRY(cudaFuncSetAttribute(wff_cols_list_kernel<T, S>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM));
+            attr_l = true;
+        }
+        if (!P.d_list) return fail(GLSU_ERR_INVALID, "tile-masked run without a tile list buffer");
+        wff_mask_list_kernel<<<1, 1024, 0, s>>>(with_margins(P.mask, 0, P.sx), ncx, ncy, G::TY, P.d_list,
+                                                P.d_list_count);
+        const int per_wx = std::max(1, std::min(ncx * ncy, (2 * 152 + P.nfx - 1) / P.nfx));
+        wff_cols_list_kernel<T, S><<<dim3(per_wx, 1, P.nfx), G::THREADS, G::SMEM, s>>>(
+            P.tmR, (C2<T> *)P.d_C, (const C2<T> *)P.d_ey, P.nfy, P.H, P.pitch, (const T *)P.d_thr, gA, gB, P.d_err,
+            P.d_list, P.d_list_count);
+    }
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
 }

@@ -4,7 +4,7 @@
 // and the tile index) gets the exact FP32 WFF2 output, computed by the same
 // separable, demodulated formulation as the full-frame kernels (rows demod,
 // column sweep with threshold, final rows; WFT/WFT2_CPU.cpp:190-390):
-// one CTA per (tile, wx), holding in shared memory
+// one CTA per (tile, wx, part of the wy range), holding in shared memory
 //   R  the row-filtered, demodulated input over rows py-2sy .. py+P+2sy-1
 //      and columns px-sx .. px+P+sx-1 (zero outside the image, the crop),
 //   U  the thresholded first column filter over rows py-sy .. py+P+sy-1,
@@ -12,29 +12,46 @@
 // then the final row filter on the P x P patch.  The per-wx partials are
 // summed in a fixed order by the residual kernel, which compares the patch
 // with the surrogate's output and flags the tile.
+#include <algorithm>
 #include <cmath>
 
 #include "glsu_internal.cuh"
 
 namespace glsu {
 
-constexpr int kProbeTapC = kMaxHalf;  // taps are stored centred at index 60
-constexpr int kProbeFR = 8;           // input rows staged per pass of the row filter
-
-struct ProbeTaps {
-    float gxr[2 * kMaxHalf + 1];  // row filter of the input (x1)
-    float gyA[2 * kMaxHalf + 1];  // first column filter (x 1/norm)
-    float gyB[2 * kMaxHalf + 1];  // second column filter (x1)
-    float gxf[2 * kMaxHalf + 1];  // final row filter (x scale/norm)
+template <typename T, int S> struct PTaps {
+    T g[2 * S + 1];
 };
+
+// Geometry of the probe for an instantiated window half-size S: the patch P
+// is chosen so that P + 2S fills whole 32-lane column groups (lane = column).
+template <int S> struct ProbeGeom {
+    static constexpr int P = S <= 20 ? 8 : 4;
+    static constexpr int RX = P + 2 * S;      // columns of R, U, C
+    static constexpr int NCG = (RX + 31) / 32;
+    static constexpr int RXP = NCG * 32;
+    static constexpr int NRG = 4;              // warps along the rows
+    static constexpr int THREADS = NCG * NRG * 32;
+    static constexpr int UY = P + 2 * S;       // rows of U
+    static constexpr int KU = (UY + NRG - 1) / NRG;
+    static constexpr int UYP = NRG * KU;
+    static constexpr int RYP = UYP + 2 * S;    // rows of R (>= P + 4S)
+    static constexpr int FR = 8;               // input rows staged per pass of the row filter
+    static constexpr int FX = RXP + 2 * S;
+    static constexpr int CPT = (P + NRG - 1) / NRG;  // C rows per thread
+    static constexpr int UREG = (UYP * RXP > FR * FX + FX) ? UYP * RXP : FR * FX + FX;
+    static constexpr size_t SMEM = sizeof(float2) * ((size_t)RYP * RXP + UREG + RYP);
+};
+
+int probe_patch_for_half(int s_inst) { return s_inst <= 20 ? 8 : 4; }
 
 struct ProbeArgs {
     const float2 *f, *ex, *ey;
     const float *thr;
-    int W, H, pitch, nfx, nfy, sx, sy, P;
-    int tile, ntx, nty;
+    int W, H, pitch, nfx, nfy, P;
+    int tile, ntx, nty, nsplit;
     uint32_t seed;
-    float2 *partial;
+    float2 *partial;  // [ntiles][nfx * nsplit][P*P]
     int2 *sites;
 };
 
@@ -58,135 +75,143 @@ __device__ __forceinline__ int2 probe_site(const ProbeArgs &a, int t)
     return make_int2(y0 + (int)(h1 % (uint32_t)max(1, th - a.P + 1)), x0 + (int)(h2 % (uint32_t)max(1, tw - a.P + 1)));
 }
 
-static int probe_smem_floats2(int P, int sx, int sy)
+// One CTA per (tile, wx, part of the wy range).  Lane = column, warps split
+// the rows; taps come from the parameter bank with compile-time indices.
+template <int S>
+__global__ void __launch_bounds__(ProbeGeom<S>::THREADS) wff_probe_kernel(ProbeArgs a, PTaps<float, S> gxr,
+                                                                          PTaps<float, S> gyA, PTaps<float, S> gyB,
+                                                                          PTaps<float, S> gxf)
 {
-    const int RX = P + 2 * sx, RY = P + 4 * sy, UY = P + 2 * sy, FX = P + 4 * sx;
-    const int ureg = UY * RX > kProbeFR * FX + FX ? UY * RX : kProbeFR * FX + FX;
-    return RY * RX + ureg + P * RX;
-}
-
-__global__ void __launch_bounds__(256) wff_probe_kernel(ProbeArgs a, ProbeTaps tp)
-{
+    using G = ProbeGeom<S>;
+    constexpr int P = G::P, RX = G::RX, RXP = G::RXP, KU = G::KU, RYP = G::RYP, FR = G::FR, FX = G::FX;
     extern __shared__ __align__(16) float2 psm[];
-    const int t = blockIdx.x, i = blockIdx.y, tid = threadIdx.x;
-    const int P = a.P, sx = a.sx, sy = a.sy;
-    const int RX = P + 2 * sx, RY = P + 4 * sy, UY = P + 2 * sy, FX = P + 4 * sx;
-    float2 *R = psm;
-    float2 *U = R + RY * RX;
-    float2 *C = U + (UY * RX > kProbeFR * FX + FX ? UY * RX : kProbeFR * FX + FX);
+    float2 *R = psm;                  // [RYP][RXP]
+    float2 *U = R + RYP * RXP;        // [UYP][RXP]; first the staged input
+    float2 *eys = U + G::UREG;        // [RYP] phasors e^{-j wy y} of the R rows
+    const int t = blockIdx.x, i = blockIdx.y, part = blockIdx.z, tid = threadIdx.x;
+    const int lane = tid & 31, w = tid >> 5, cg = w % G::NCG, rg = w / G::NCG;
+    const int col = cg * 32 + lane;
     const int2 site = probe_site(a, t);
-    if (i == 0 && tid == 0) a.sites[t] = site;
+    if (i == 0 && part == 0 && tid == 0) a.sites[t] = site;
     const int py = site.x, px = site.y;
     const float2 *exi = a.ex + (size_t)i * (a.pitch + 2 * kPhasorPad) + kPhasorPad;
     const float thr = *a.thr, thr2 = thr * thr;
 
-    // ---- R: rows py-2sy .., demodulated by e^{-j wx x}, filtered along x
-    float2 *fs = U;                   // [kProbeFR][FX] staged, demodulated input
-    float2 *es = U + kProbeFR * FX;   // [FX] phasors of the staged columns
-    for (int e = tid; e < FX; e += 256) es[e] = exi[px - 2 * sx + e];
-    for (int r0 = 0; r0 < RY; r0 += kProbeFR) {
+    // ---- R: rows py-2S .., demodulated by e^{-j wx x}, filtered along x (zero outside the image)
+    float2 *fs = U;              // [FR][FX]
+    float2 *es = U + FR * FX;    // [FX]
+    for (int e = tid; e < FX; e += G::THREADS) es[e] = exi[px - 2 * S + e];
+    for (int r0 = 0; r0 < RYP; r0 += FR) {
         __syncthreads();
-        for (int e = tid; e < kProbeFR * FX; e += 256) {
+        for (int e = tid; e < FR * FX; e += G::THREADS) {
             const int rr = e / FX, c = e - rr * FX;
-            const int y = py - 2 * sy + r0 + rr, x = px - 2 * sx + c;
+            const int y = py - 2 * S + r0 + rr, x = px - 2 * S + c;
             float2 v = make_float2(0.f, 0.f);
-            if (r0 + rr < RY && y >= 0 && y < a.H && x >= 0 && x < a.W) v = a.f[(size_t)y * a.W + x];
+            if (y >= 0 && y < a.H && x >= 0 && x < a.W) v = a.f[(size_t)y * a.W + x];
             const float2 p = es[c];
             fs[e] = make_float2(v.x * p.x - v.y * p.y, v.x * p.y + v.y * p.x);
         }
         __syncthreads();
-        for (int e = tid; e < kProbeFR * RX; e += 256) {
-            const int rr = e / RX, c = e - rr * RX;
-            if (r0 + rr >= RY) continue;
-            const int x = px - sx + c;
+        for (int rr = rg; rr < FR && r0 + rr < RYP; rr += G::NRG) {
+            const int x = px - S + col;
             float2 acc = make_float2(0.f, 0.f);
-            if (x >= 0 && x < a.W) {
-                const float2 *row = fs + rr * FX + c;
-                for (int m = 0; m <= 2 * sx; m++) {
-                    const float g = tp.gxr[kProbeTapC - sx + m];
-                    acc.x = fmaf(g, row[m].x, acc.x);
-                    acc.y = fmaf(g, row[m].y, acc.y);
+            if (col < RX && x >= 0 && x < a.W) {
+                const float2 *row = fs + rr * FX + col;
+#pragma unroll
+                for (int m = 0; m <= 2 * S; m++) {
+                    acc.x = fmaf(gxr.g[m], row[m].x, acc.x);
+                    acc.y = fmaf(gxr.g[m], row[m].y, acc.y);
                 }
             }
-            R[(r0 + rr) * RX + c] = acc;
+            R[(r0 + rr) * RXP + col] = acc;
         }
     }
-    for (int e = tid; e < P * RX; e += 256) C[e] = make_float2(0.f, 0.f);
 
-    const size_t eys = (size_t)a.H + 2 * kPhasorPad;
-    const int nub = (UY + 3) / 4;
-    for (int k = 0; k < a.nfy; k++) {
-        const float2 *eyk = a.ey + (size_t)k * eys + kPhasorPad;
-        __syncthreads();
-        // ---- U: first column filter (4 rows per thread), threshold
-        for (int e = tid; e < nub * RX; e += 256) {
-            const int c = e % RX, u0 = (e / RX) * 4;
-            float2 acc[4];
+    float2 cacc[G::CPT];
 #pragma unroll
-            for (int q = 0; q < 4; q++) acc[q] = make_float2(0.f, 0.f);
-            const int jend = min(u0 + 3 + 2 * sy, RY - 1);
-            for (int j = u0; j <= jend; j++) {
-                const float2 r = R[j * RX + c];
-                const float2 p = eyk[py - 2 * sy + j];
+    for (int q = 0; q < G::CPT; q++) cacc[q] = make_float2(0.f, 0.f);
+    const size_t eys_stride = (size_t)a.H + 2 * kPhasorPad;
+    const int k0 = part * a.nfy / a.nsplit, k1 = (part + 1) * a.nfy / a.nsplit;
+    const int u0 = rg * KU;
+    for (int k = k0; k < k1; k++) {
+        const float2 *eyk = a.ey + (size_t)k * eys_stride + kPhasorPad;
+        __syncthreads();  // the previous pass 2 is done with U; R is complete
+        for (int e = tid; e < RYP; e += G::THREADS) eys[e] = eyk[min(py - 2 * S + e, a.H - 1 + kPhasorPad)];
+        __syncthreads();
+        // ---- U rows u0 .. u0+KU-1 of this column: first column filter, threshold
+        {
+            float2 acc[KU];
+#pragma unroll
+            for (int q = 0; q < KU; q++) acc[q] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < KU + 2 * S; j++) {
+                const float2 r = R[(u0 + j) * RXP + col];
+                const float2 p = eys[u0 + j];
                 const float dx = r.x * p.x - r.y * p.y, dy = r.x * p.y + r.y * p.x;
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const int m = j - u0 - q;
-                    if (m >= 0 && m <= 2 * sy) {
-                        const float g = tp.gyA[kProbeTapC - sy + m];
-                        acc[q].x = fmaf(g, dx, acc[q].x);
-                        acc[q].y = fmaf(g, dy, acc[q].y);
+                for (int q = 0; q < KU; q++) {
+                    const int m = j - q;
+                    if (m >= 0 && m <= 2 * S) {
+                        acc[q].x = fmaf(gyA.g[m], dx, acc[q].x);
+                        acc[q].y = fmaf(gyA.g[m], dy, acc[q].y);
                     }
                 }
             }
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int uy = u0 + q;
-                if (uy >= UY) break;
-                const int Y = py - sy + uy;
+            for (int q = 0; q < KU; q++) {
+                const int Y = py - S + u0 + q;
                 const bool keep = Y >= 0 && Y < a.H && acc[q].x * acc[q].x + acc[q].y * acc[q].y >= thr2;
-                U[uy * RX + c] = keep ? acc[q] : make_float2(0.f, 0.f);
+                U[(u0 + q) * RXP + col] = keep ? acc[q] : make_float2(0.f, 0.f);
             }
         }
         __syncthreads();
-        // ---- C += e^{+j wy y} (second column filter)
-        for (int e = tid; e < P * RX; e += 256) {
-            const int cy = e / RX, c = e - cy * RX;
-            float2 acc = make_float2(0.f, 0.f);
-            for (int j = 0; j <= 2 * sy; j++) {
-                const float g = tp.gyB[kProbeTapC - sy + j];
-                const float2 v = U[(cy + j) * RX + c];
-                acc.x = fmaf(g, v.x, acc.x);
-                acc.y = fmaf(g, v.y, acc.y);
+        // ---- C += e^{+j wy y} (second column filter) on the patch rows
+#pragma unroll
+        for (int q = 0; q < G::CPT; q++) {
+            const int r = rg + q * G::NRG;
+            if (r < P) {
+                float2 c = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int m = 0; m <= 2 * S; m++) {
+                    const float2 v = U[(r + m) * RXP + col];
+                    c.x = fmaf(gyB.g[m], v.x, c.x);
+                    c.y = fmaf(gyB.g[m], v.y, c.y);
+                }
+                const float2 p = eys[r + 2 * S];  // row py + r: e^{-j wy y}, multiply by its conjugate
+                cacc[q].x += p.x * c.x + p.y * c.y;
+                cacc[q].y += p.x * c.y - p.y * c.x;
             }
-            const int Y = min(py + cy, a.H - 1 + kPhasorPad);
-            const float2 p = eyk[Y];  // e^{-j wy y}; multiply by its conjugate
-            C[e].x += p.x * acc.x + p.y * acc.y;
-            C[e].y += p.x * acc.y - p.y * acc.x;
         }
     }
     __syncthreads();
+    float2 *C = U;  // [P][RXP]
+#pragma unroll
+    for (int q = 0; q < G::CPT; q++) {
+        const int r = rg + q * G::NRG;
+        if (r < P) C[r * RXP + col] = cacc[q];
+    }
+    __syncthreads();
     // ---- final row filter and modulation on the P x P patch
-    for (int e = tid; e < P * P; e += 256) {
+    for (int e = tid; e < P * P; e += G::THREADS) {
         const int cy = e / P, cx = e - cy * P;
         float2 acc = make_float2(0.f, 0.f);
-        for (int j = 0; j <= 2 * sx; j++) {
-            const float g = tp.gxf[kProbeTapC - sx + j];
-            const float2 v = C[cy * RX + cx + j];
-            acc.x = fmaf(g, v.x, acc.x);
-            acc.y = fmaf(g, v.y, acc.y);
+#pragma unroll
+        for (int m = 0; m <= 2 * S; m++) {
+            const float2 v = C[cy * RXP + cx + m];
+            acc.x = fmaf(gxf.g[m], v.x, acc.x);
+            acc.y = fmaf(gxf.g[m], v.y, acc.y);
         }
         const float2 p = exi[px + cx];
-        a.partial[((size_t)t * a.nfx + i) * P * P + e] =
+        a.partial[((size_t)t * gridDim.y * gridDim.z + i * gridDim.z + part) * P * P + e] =
             make_float2(p.x * acc.x + p.y * acc.y, p.x * acc.y - p.y * acc.x);
     }
 }
 
-// One block of 64 threads per tile: sum the per-wx partials (fixed order),
-// RMS phase residual of cmp against the exact patch where |WFF2| >= 0.1.
+// One block of 64 threads per tile: sum the partials (fixed order), RMS
+// phase residual of cmp against the exact patch where |WFF2| >= 0.1.
 __global__ void __launch_bounds__(64) wff_probe_resid_kernel(const float2 *__restrict__ partial,
-                                                             const int2 *__restrict__ sites, int nfx, int P, int W,
-                                                             int H, const float2 *__restrict__ cmp, float tol,
+                                                             const int2 *__restrict__ sites, int nparts, int P,
+                                                             int W, int H, const float2 *__restrict__ cmp, float tol,
                                                              float *__restrict__ resid, int *__restrict__ flags,
                                                              int *__restrict__ counts)
 {
@@ -197,8 +222,8 @@ __global__ void __launch_bounds__(64) wff_probe_resid_kernel(const float2 *__res
     int cnt = 0;
     if (e < P * P) {
         float2 v = make_float2(0.f, 0.f);
-        for (int i = 0; i < nfx; i++) {
-            const float2 q = partial[((size_t)t * nfx + i) * P * P + e];
+        for (int i = 0; i < nparts; i++) {
+            const float2 q = partial[((size_t)t * nparts + i) * P * P + e];
             v.x += q.x;
             v.y += q.y;
         }
@@ -230,27 +255,69 @@ __global__ void __launch_bounds__(64) wff_probe_resid_kernel(const float2 *__res
     }
 }
 
+template <int S> static PTaps<float, S> probe_taps(const double *g, int strue, double mul)
+{
+    PTaps<float, S> t;
+    for (int m = 0; m <= 2 * S; m++) {
+        const int k = m - S;
+        t.g[m] = (k >= -strue && k <= strue) ? (float)(g[k + strue] * mul) : 0.f;
+    }
+    return t;
+}
+
+static int sm_count()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
+    }
+    return n;
+}
+
+template <int S>
+static int launch_probe(const WffPlan &Pl, ProbeArgs a, cudaStream_t s, const ProbeOut &o, const void *d_cmp,
+                        double tol)
+{
+    using G = ProbeGeom<S>;
+    static bool attr = false;
+    if (!attr) {
+        GLSU_CUDA_TRY(cudaFuncSetAttribute(wff_probe_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)G::SMEM));
+        attr = true;
+    }
+    const int ntiles = a.ntx * a.nty;
+    // split the wy range (at most 4 parts) so that the last wave of CTAs is well filled
+    const int per_sm = (int)((228 * 1024) / (G::SMEM + 1024));
+    const int slots = sm_count() * (per_sm > 0 ? per_sm : 1);
+    double best = 1e30;
+    for (int ns = 1; ns <= 4 && ns <= Pl.nfy; ns++) {
+        const long long ctas = (long long)ntiles * Pl.nfx * ns;
+        const double cost = (double)((ctas + slots - 1) / slots) * (1.0 / ns + 0.06);
+        if (cost < best - 1e-9) {
+            best = cost;
+            a.nsplit = ns;
+        }
+    }
+    wff_probe_kernel<S><<<dim3(ntiles, Pl.nfx, a.nsplit), G::THREADS, G::SMEM, s>>>(
+        a, probe_taps<S>(Pl.gx, Pl.sx, 1.0), probe_taps<S>(Pl.gy, Pl.sy, Pl.inv_norm), probe_taps<S>(Pl.gy, Pl.sy, 1.0),
+        probe_taps<S>(Pl.gx, Pl.sx, Pl.scale * Pl.inv_norm));
+    wff_probe_resid_kernel<<<ntiles, 64, 0, s>>>(o.partial, o.sites, Pl.nfx * a.nsplit, G::P, a.W, a.H,
+                                                 (const float2 *)d_cmp, (float)tol, o.resid, o.flags, o.counts);
+    GLSU_CUDA_TRY(cudaGetLastError());
+    return GLSU_OK;
+}
+
 int WffPlan::enqueue_probe(cudaStream_t s, const void *d_f, const void *d_cmp, int tile, int P, uint32_t seed,
                            double tol, const ProbeOut &o)
 {
     if (prec != GLSU_F32) return fail(GLSU_ERR_UNSUPPORTED, "the WFF2 probe runs in FP32");
-    if (P < 1 || P > kProbeMaxP || tile < P) return fail(GLSU_ERR_INVALID, "probe patch must be 1..8 and <= tile");
-    const int smem = (int)(probe_smem_floats2(P, sx, sy) * sizeof(float2));
-    if (smem > 227 * 1024) return fail(GLSU_ERR_UNSUPPORTED, "probe patch too large for this window (use P = 4)");
+    const int S = std::max(sxi, syi);
+    if (S > 45) return fail(GLSU_ERR_UNSUPPORTED, "the WFF2 probe supports window half-sizes up to 45");
+    if (P != probe_patch_for_half(S)) return fail(GLSU_ERR_INVALID, "probe patch size does not match the window");
+    if (tile < P) return fail(GLSU_ERR_INVALID, "probe patch larger than the tile");
     GLSU_TRY(ensure_threshold(s, d_f));
-    static int attr = 0;
-    if (smem > attr) {
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(wff_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        attr = smem;
-    }
-    ProbeTaps tp;
-    for (int m = -kMaxHalf; m <= kMaxHalf; m++) {
-        const bool inx = m >= -sx && m <= sx, iny = m >= -sy && m <= sy;
-        tp.gxr[m + kProbeTapC] = inx ? (float)gx[m + sx] : 0.f;
-        tp.gxf[m + kProbeTapC] = inx ? (float)(gx[m + sx] * scale * inv_norm) : 0.f;
-        tp.gyA[m + kProbeTapC] = iny ? (float)(gy[m + sy] * inv_norm) : 0.f;
-        tp.gyB[m + kProbeTapC] = iny ? (float)gy[m + sy] : 0.f;
-    }
     ProbeArgs a;
     a.f = (const float2 *)d_f;
     a.ex = (const float2 *)d_ex;
@@ -261,21 +328,20 @@ int WffPlan::enqueue_probe(cudaStream_t s, const void *d_f, const void *d_cmp, i
     a.pitch = pitch;
     a.nfx = nfx;
     a.nfy = nfy;
-    a.sx = sx;
-    a.sy = sy;
     a.P = P;
     a.tile = tile;
     a.ntx = (W + tile - 1) / tile;
     a.nty = (H + tile - 1) / tile;
+    a.nsplit = 1;
     a.seed = seed;
     a.partial = o.partial;
     a.sites = o.sites;
-    const int ntiles = a.ntx * a.nty;
-    wff_probe_kernel<<<dim3(ntiles, nfx), 256, smem, s>>>(a, tp);
-    wff_probe_resid_kernel<<<ntiles, 64, 0, s>>>(o.partial, o.sites, nfx, P, W, H, (const float2 *)d_cmp,
-                                                 (float)tol, o.resid, o.flags, o.counts);
-    GLSU_CUDA_TRY(cudaGetLastError());
-    return GLSU_OK;
+    switch (S) {
+    case 12: return launch_probe<12>(*this, a, s, o, d_cmp, tol);
+    case 20: return launch_probe<20>(*this, a, s, o, d_cmp, tol);
+    case 30: return launch_probe<30>(*this, a, s, o, d_cmp, tol);
+    default: return launch_probe<45>(*this, a, s, o, d_cmp, tol);
+    }
 }
 
 }  // namespace glsu

@@ -280,7 +280,10 @@ int glsu_sur_conv32(const void *d_in, void *d_out, int batch, int width, int hei
  * above; NULL h_params switches back to the plain WFF2).  Every frame, one
  * patch x patch patch per tile x tile tile gets the exact WFF2 (the sparse
  * probe); tiles whose RMS phase residual exceeds tol (radians) are
- * recomputed by the plain WFF2.  tol <= 0 turns the probes off. */
+ * recomputed by the plain WFF2.  tol <= 0 turns the probes off.  The patch
+ * size follows the WFF2 window: 8 for half-sizes round(3 sigma) up to 20, 4
+ * from 21 to 45 (patch = 0 selects it; other values are rejected); probes
+ * need half-sizes up to 45. */
 int glsu_dpra_set_surrogate(glsu_dpra *h, const float *h_params, const int *dilations, int tile, int patch,
                             double tol);
 /* Cumulative probe counts; h_resid (optional, one float per tile, tiles
