@@ -20,6 +20,22 @@ static int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, kS
 // Blocks of the row-walking per-pixel kernels (a block takes whole image rows).
 int SurNet::rows_grid() const { return std::min(B * H, kSurPixBlocks); }
 
+// Blocks of the last layer: one per 128-pixel row segment.
+int SurNet::l7_grid() const { return B * H * ((W + kL7Seg - 1) / kL7Seg); }
+
+int SurNet::launch_l7(const float2 *z, float2 *outp, const float2 *target, float2 *dhp, double *partp)
+{
+    static int attr = 0;
+    const int smem = sur_l7_smem(dil[7]);
+    if (smem > attr) {
+        GLSU_CUDA_TRY(cudaFuncSetAttribute(sur_l7_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sur_l7_smem(64)));
+        attr = sur_l7_smem(64);
+    }
+    sur_l7_kernel<<<l7_grid(), kL7Seg, smem, stream>>>(a6(), z, B, H, W, dil[7], h_w7, outp, target, dhp, partp);
+    GLSU_CUDA_TRY(cudaGetLastError());
+    return GLSU_OK;
+}
+
 int SurNet::init(int batch, int width, int height, const int *dilations, bool train)
 {
     if (batch < 1 || width < 1 || height < 1) return fail(GLSU_ERR_INVALID, "surrogate: bad batch or size");
@@ -43,7 +59,7 @@ int SurNet::init(int batch, int width, int height, const int *dilations, bool tr
     if (training && ok) {
         ok = A((void **)&d_g[0], abytes) && A((void **)&d_g[1], abytes) && A((void **)&d_dh, n * 8) &&
              A((void **)&d_out, n * 8) && A((void **)&d_grad, kSurParams * 4) && A((void **)&d_m, kSurParams * 4) &&
-             A((void **)&d_v, kSurParams * 4) && A((void **)&d_lpart, kSurPixBlocks * 8) &&
+             A((void **)&d_v, kSurParams * 4) && A((void **)&d_lpart, (size_t)l7_grid() * 8) &&
              A((void **)&d_loss, 8);
         nb32 = sur_dw32_blocks(B, H, W);
         nbs = (int)((n + kSurSmallPix - 1) / kSurSmallPix);
@@ -146,10 +162,7 @@ const uint16_t *SurNet::a6() const { return training ? d_act[6] : d_act[0]; }
 int SurNet::forward(const void *d_z, void *d_outp)
 {
     GLSU_TRY(hidden((const float2 *)d_z));
-    sur_l7_kernel<<<rows_grid(), 256, 0, stream>>>(a6(), (const float2 *)d_z, B, H, W, dil[7], h_w7,
-                                                   (float2 *)d_outp, nullptr, nullptr, nullptr);
-    GLSU_CUDA_TRY(cudaGetLastError());
-    return GLSU_OK;
+    return launch_l7((const float2 *)d_z, (float2 *)d_outp, nullptr, nullptr, nullptr);
 }
 
 int SurNet::backward(const void *d_z, const void *d_target)
@@ -158,9 +171,8 @@ int SurNet::backward(const void *d_z, const void *d_target)
     const float2 *z = (const float2 *)d_z;
     GLSU_TRY(hidden(z));
     const int g = rows_grid();
-    sur_l7_kernel<<<g, 256, 0, stream>>>(d_act[6], z, B, H, W, dil[7], h_w7, d_out,
-                                         (const float2 *)d_target, d_dh, d_lpart);
-    sur_sum_kernel<<<1, 32, 0, stream>>>(d_lpart, g, d_loss);
+    GLSU_TRY(launch_l7(z, d_out, (const float2 *)d_target, d_dh, d_lpart));
+    sur_sum_kernel<<<1, 32, 0, stream>>>(d_lpart, l7_grid(), d_loss);
     // layer 7: weight gradient and dL/da6 (masked)
     sur_dw_small_kernel<2, 32><<<nbs, 256, 0, stream>>>(d_dh, d_act[6], B, H, W, dil[7], kSurSmallPix, d_part);
     sur_reduce_kernel<<<(kSurL7Params + 255) / 256, 256, 0, stream>>>(d_part, nbs, kSurL7Params,

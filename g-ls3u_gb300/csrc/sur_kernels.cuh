@@ -357,86 +357,88 @@ __global__ void __launch_bounds__(256) sur_l0_kernel(const float2 *__restrict__ 
 }
 
 // Last layer, residual, renormalisation: out = y/|y|, y = z + conv7(a6).
-// Four lanes per pixel, each owning 8 of the 32 input channels (one 16-byte
-// chunk), so a warp's loads cover 8 neighbouring pixels contiguously; the
-// weights sit in shared memory as [chunk][tap][co][8] (chunk stride padded
-// to 148 floats: the four chunk groups of a warp read disjoint banks, two
-// 16-byte loads per tap and output) and two shuffles combine the partial
-// sums.  With a target (training): per pixel loss wgt |out - t|^2, wgt =
-// min(|target|, 1), t = target/|target|, the gradient dL/dh7 of the mean
-// loss into dh, and per-block loss sums into part.
-__global__ void __launch_bounds__(256, 2) sur_l7_kernel(const uint16_t *__restrict__ a6, const float2 *__restrict__ z,
-                                                        int B, int H, int W, int dil,
+// One CTA per 128-pixel segment of an image row: the three input rows
+// y - d, y, y + d (columns x0 - d .. x0 + 127 + d, zero outside the image)
+// are staged in shared memory by coalesced 16-byte loads, with an 80-byte
+// pixel stride so that the per-pixel 16-byte reads are free of bank
+// conflicts; one thread per pixel, weights in the parameter bank.  With a
+// target (training): per pixel loss wgt |out - t|^2, wgt = min(|target|, 1),
+// t = target/|target|, the gradient dL/dh7 of the mean loss into dh, and per
+// block loss sums into part.
+constexpr int kL7Seg = 128;
+constexpr int kL7Pix = 5;  // uint4 per staged pixel: 4 of data, 1 of padding
+
+int sur_l7_smem(int dil) { return 3 * (kL7Seg + 2 * dil) * kL7Pix * 16; }
+
+__global__ void __launch_bounds__(kL7Seg) sur_l7_kernel(const uint16_t *__restrict__ a6,
+                                                        const float2 *__restrict__ z, int B, int H, int W, int dil,
                                                         const __grid_constant__ SurL7W wp, float2 *__restrict__ out,
                                                         const float2 *__restrict__ target, float2 *__restrict__ dh,
                                                         double *__restrict__ part)
 {
-    constexpr int kCS = 148;  // chunk stride (floats)
-    __shared__ double red[256];
-    __shared__ __align__(16) float ws[4 * kCS];
-    for (int e = threadIdx.x; e < 576; e += 256) {
-        const int co = e / 288, ci = (e / 9) % 32, t = e % 9;
-        ws[(ci >> 3) * kCS + (t * 2 + co) * 8 + (ci & 7)] = wp.w[e];
+    extern __shared__ __align__(16) uint4 st7[];
+    __shared__ double red[kL7Seg];
+    const int nseg = (W + kL7Seg - 1) / kL7Seg;
+    const int row = blockIdx.x / nseg, seg = blockIdx.x - row * nseg;
+    const int y = row % H;
+    const size_t img = (size_t)(row - y) * W;
+    const int x0 = seg * kL7Seg, SW = kL7Seg + 2 * dil, tid = threadIdx.x;
+    for (int e = tid; e < 3 * SW * 4; e += kL7Seg) {
+        const int r = e / (SW * 4), rem = e - r * SW * 4, px = rem >> 2, c = rem & 3;
+        const int yy = y + (r - 1) * dil, xx = x0 - dil + px;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+            v = reinterpret_cast<const uint4 *>(a6 + (img + (size_t)yy * W + xx) * 32)[c];
+        st7[(r * SW + px) * kL7Pix + c] = v;
     }
     __syncthreads();
-    const int chunk = threadIdx.x & 3;
-    const float *wc = ws + chunk * kCS;
-    const double inv_n = 1.0 / ((double)B * H * W);
+    const int x = x0 + tid;
     double lsum = 0;
-    for (int row = blockIdx.x; row < B * H; row += gridDim.x) {
-        const int y = row % H;
-        const size_t img = (size_t)(row - y) * W;
-        for (int xb = 0; xb < W; xb += 64) {  // warp-uniform bound: every lane takes part in the shuffles
-            const int x = xb + (threadIdx.x >> 2);
-            const bool act = x < W;
-            float h0 = 0.f, h1 = 0.f;
+    if (x < W) {
+        float h0 = wp.b[0], h1 = wp.b[1];
 #pragma unroll
-            for (int t = 0; t < 9; t++) {
-                const int yy = y + (t / 3 - 1) * dil, xx = x + (t % 3 - 1) * dil;
-                if (!act || yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
+        for (int t = 0; t < 9; t++) {
+            const uint4 *sp = st7 + ((t / 3) * SW + tid + (t % 3) * dil) * kL7Pix;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
                 float av[8];
-                unpack8(reinterpret_cast<const uint4 *>(a6 + (img + (size_t)yy * W + xx) * 32)[chunk], av);
-                const float4 *w4 = reinterpret_cast<const float4 *>(wc + t * 16);
-                const float4 a0 = w4[0], a1 = w4[1], b0 = w4[2], b1 = w4[3];
-                h0 = fmaf(a0.x, av[0], fmaf(a0.y, av[1], fmaf(a0.z, av[2], fmaf(a0.w, av[3], h0))));
-                h0 = fmaf(a1.x, av[4], fmaf(a1.y, av[5], fmaf(a1.z, av[6], fmaf(a1.w, av[7], h0))));
-                h1 = fmaf(b0.x, av[0], fmaf(b0.y, av[1], fmaf(b0.z, av[2], fmaf(b0.w, av[3], h1))));
-                h1 = fmaf(b1.x, av[4], fmaf(b1.y, av[5], fmaf(b1.z, av[6], fmaf(b1.w, av[7], h1))));
+                unpack8(sp[c], av);
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    h0 = fmaf(wp.w[(8 * c + i) * 9 + t], av[i], h0);
+                    h1 = fmaf(wp.w[288 + (8 * c + i) * 9 + t], av[i], h1);
+                }
             }
-            h0 += __shfl_xor_sync(0xffffffffu, h0, 1);
-            h1 += __shfl_xor_sync(0xffffffffu, h1, 1);
-            h0 += __shfl_xor_sync(0xffffffffu, h0, 2);
-            h1 += __shfl_xor_sync(0xffffffffu, h1, 2);
-            if (!act || chunk != 0) continue;
-            const size_t p = img + (size_t)y * W + x;
-            const float2 xv = z[p];
-            const float yr = xv.x + (h0 + wp.b[0]), yi = xv.y + (h1 + wp.b[1]);
-            const float nrm = sqrtf(yr * yr + yi * yi);
-            const float inv = nrm > 1e-20f ? 1.f / nrm : 0.f;
-            const float orr = yr * inv, oii = yi * inv;
-            out[p] = make_float2(orr, oii);
-            if (target) {
-                const float2 tv = target[p];
-                const float tn = sqrtf(tv.x * tv.x + tv.y * tv.y);
-                const float wgt = fminf(tn, 1.f);
-                const float ti = tn > 1e-20f ? 1.f / tn : 0.f;
-                const float er = orr - tv.x * ti, ei = oii - tv.y * ti;
-                lsum += (double)(wgt * (er * er + ei * ei));
-                // d out: 2 wgt e / n; through out = y/|y|: (g - out (out.g)) / |y|
-                const float gr = (float)(2.0 * inv_n) * wgt * er, gi = (float)(2.0 * inv_n) * wgt * ei;
-                const float dot = orr * gr + oii * gi;
-                dh[p] = make_float2((gr - orr * dot) * inv, (gi - oii * dot) * inv);
-            }
+        }
+        const size_t p = img + (size_t)y * W + x;
+        const float2 xv = z[p];
+        const float yr = xv.x + h0, yi = xv.y + h1;
+        const float nrm = sqrtf(yr * yr + yi * yi);
+        const float inv = nrm > 1e-20f ? 1.f / nrm : 0.f;
+        const float orr = yr * inv, oii = yi * inv;
+        out[p] = make_float2(orr, oii);
+        if (target) {
+            const double inv_n = 1.0 / ((double)B * H * W);
+            const float2 tv = target[p];
+            const float tn = sqrtf(tv.x * tv.x + tv.y * tv.y);
+            const float wgt = fminf(tn, 1.f);
+            const float ti = tn > 1e-20f ? 1.f / tn : 0.f;
+            const float er = orr - tv.x * ti, ei = oii - tv.y * ti;
+            lsum = (double)(wgt * (er * er + ei * ei)) * inv_n;
+            // d out: 2 wgt e / n; through out = y/|y|: (g - out (out.g)) / |y|
+            const float gr = (float)(2.0 * inv_n) * wgt * er, gi = (float)(2.0 * inv_n) * wgt * ei;
+            const float dot = orr * gr + oii * gi;
+            dh[p] = make_float2((gr - orr * dot) * inv, (gi - oii * dot) * inv);
         }
     }
     if (target) {
-        red[threadIdx.x] = lsum;
+        red[tid] = lsum;
         __syncthreads();
-        for (int s = 128; s > 0; s >>= 1) {
-            if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        for (int s = kL7Seg / 2; s > 0; s >>= 1) {
+            if (tid < s) red[tid] += red[tid + s];
             __syncthreads();
         }
-        if (threadIdx.x == 0) part[blockIdx.x] = red[0] * inv_n;
+        if (tid == 0) part[blockIdx.x] = red[0];
     }
 }
 

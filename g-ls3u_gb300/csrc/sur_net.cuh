@@ -43,6 +43,8 @@ struct SurNet {
     int adam(float lr, float b1, float b2, float eps);
     int check_error();
     int rows_grid() const;
+    int l7_grid() const;
+    int launch_l7(const float2 *z, float2 *outp, const float2 *target, float2 *dhp, double *partp);
 };
 
 }  // namespace glsu
