@@ -1,12 +1,26 @@
 #!/usr/bin/env python
-"""G-LS3U benchmark: frames/s of the per-frame hot path at 1024x1024 FP32.
+"""G-LS3U benchmark: frames/s of the per-frame hot path at 1024x1024 FP32,
+surrogate form against plain form.
 
-A step is one frame of the plain G-LS3U path -- DPRA least squares (7x7
-window) -> WFF2 (sigma 10, 21x21 frequencies on [-1, 1], threshold 0.2) ->
-phase update -> reference update (rate 1) -- on a 1024x1024 frame of the
-seeded synthetic sequence generator (glsu/synth.py).  The sequence's initial
-phase comes from AIA on 5 phase-shifted frames (timed separately, reported
-under "aia").
+A step is one frame of a seeded synthetic sequence (glsu/synth.py) with the
+frame already in HBM:
+
+* plain form -- DPRA least squares (7x7 window) -> WFF2 (sigma 10, 21x21
+  frequencies on [-1, 1], threshold 0.2) -> phase update -> reference update
+  (rate 1);
+* surrogate form (the headline "value") -- DPRA least squares -> the learned
+  8-layer dilated residual network (BF16 tcgen05 convolutions) in place of
+  WFF2 -> exact FP32 WFF2 on one 4x4 probe patch per 256x256 tile -> plain
+  WFF2 recomputation of every tile whose RMS phase residual exceeds 0.05 rad
+  -> phase update -> reference update.
+
+Both forms are timed with CUDA events over K consecutive frames after W
+warm-up frames, L2 flushed (256 MiB write) before each frame outside the
+events.  "e2e" runs K further frames of the same sequence through
+glsu_dpra_sequence (pinned host frames in, dphi out).  The surrogate form's
+accuracy is measured teacher-forced against the plain FP32 WFF2 of the same
+least-squares output over 6 frames.  The sequence's initial phase comes from
+AIA on 5 phase-shifted frames (timed separately, reported under "aia").
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -47,6 +61,11 @@ SUR_FLOPS_PER_PX = 2 * 18 * 32 + 6 * 2 * 288 * 32 + 2 * 288 * 2
 # layer 0, six tensor-core layers, layer 7, probe, residual, three masked
 # WFF2 passes, update
 PLAIN_LAUNCHES, SUR_LAUNCHES = 4, 15
+# one 32->32 tensor-core layer per pixel: read 64 B, write 64 B; 2*288*32 flops
+SUR_CONV_BYTES_PER_PX, SUR_CONV_FLOPS_PER_PX = 128, 2 * 288 * 32
+# DRAM bytes (read + write) of one sur_conv_tc_kernel launch at 1024x1024,
+# from the ncu capture summarised in profiles/sur_conv_tc_kernel_1024.md
+SUR_CONV_TRAFFIC_1024 = 67.349760e6 + 18.997248e6
 SIZE = 1024
 RADIUS = 3
 WFF = (10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)
@@ -67,20 +86,46 @@ def parse():
     return ap.parse_args()
 
 
+def fft_padded(n):
+    """Smallest even 7-smooth size >= n: the reference's FFT size table
+    (WFT/WFT.h:18-32) is exactly the even 7-smooth numbers up to 4096."""
+    while True:
+        m = n
+        for p in (2, 3, 5, 7):
+            while m % p == 0:
+                m //= p
+        if m == 1 and n % 2 == 0:
+            return n
+        n += 1
+
+
+def fft_model_bytes(size):
+    """Algorithmic bytes of one frame of the FFT formulation of WFF2 (the
+    reference's WFT2_CUDAF::cuWFF2, WFT/WFT2_CUDAf.cu:1016-1173): four passes
+    over the padded complex64 plane per frequency (16 B each way per element)
+    plus the forward transform of the input: (64 * n_freq + 32) * P bytes."""
+    s = int(np.floor(3 * WFF[0] + 0.5))
+    P = fft_padded(size + 2 * s) ** 2
+    return (64 * NFX * NFY + 32) * P, P
+
+
 def workload_config(size):
     return {
-        "workload": "G-LS3U plain per-frame path, %dx%d FP32, DPRA %dx%d window, WFF2 sigma=%g, "
-                    "xi in [%g,%g] step %g (%dx%d frequencies), thr=%g, reference rate 1; 200-frame "
-                    "sequence generator with AIA (5 frames) initial phase"
+        "workload": "G-LS3U per-frame path, %dx%d FP32, DPRA %dx%d window, WFF2 sigma=%g, "
+                    "xi in [%g,%g] step %g (%dx%d frequencies), thr=%g, reference rate 1; surrogate form "
+                    "(8-layer dilated residual CNN, BF16 tcgen05, one %dx%d exact-WFF2 probe per %dx%d tile, "
+                    "plain fallback above %g rad) vs plain form; 200-frame sequence generator with AIA "
+                    "(5 frames) initial phase"
                     % (size, size, 2 * RADIUS + 1, 2 * RADIUS + 1, WFF[0], WFF[1], WFF[2], WFF[3], NFX, NFY,
-                       WFF[8]),
+                       WFF[8], SUR_PATCH, SUR_PATCH, SUR_TILE, SUR_TILE, SUR_TOL),
         "frame": [size, size],
         "dpra_window": 2 * RADIUS + 1,
         "wff": {"sigma": WFF[0], "wl": WFF[1], "wh": WFF[2], "wi": WFF[3], "thr": WFF[8], "n_freq": NFX * NFY},
+        "surrogate": {"tile": SUR_TILE, "probe_patch": SUR_PATCH, "tol_rad": SUR_TOL},
         "l2": "flushed before every timed step (256 MiB device write outside the timed events)",
         "e2e_path": "glsu_dpra_sequence over K consecutive pinned host frames after W warm-up frames on a "
                     "fresh handle (H2D, D2H on their own streams, overlapped with neighbouring frames); L2 "
-                    "flushed once before, and each plain frame streams 352 MB of WFF2 planes (more than the "
+                    "flushed once before; each plain frame streams 352 MB of WFF2 planes (more than the "
                     "129 MB L2)",
     }
 
@@ -229,7 +274,7 @@ def timed_frames(glsu, torch, d, dfr, nfr, args, stream, flush, world, local):
         d.update_ref_phi()
     torch.cuda.synchronize()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    stage = np.zeros(4)
+    stage = None
     barrier(world)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
@@ -242,7 +287,8 @@ def timed_frames(glsu, torch, d, dfr, nfr, args, stream, flush, world, local):
         d.per_frame_device(dfr[(args.warmup + k) % nfr].data_ptr(), glsu.F32)
         d.update_ref_phi()
         evs[k][1].record(stream)
-        stage += np.array(d.stage_times())  # synchronises the stream (outside the events)
+        st = np.array(d.stage_times())  # synchronises the stream (outside the events)
+        stage = st if stage is None else stage + st
     torch.cuda.synchronize()
     clk = clocks.stop()
     barrier(world)
@@ -374,6 +420,7 @@ def run_ours(args, rank, world, local):
                "e2e_frames_per_s": s_e2e,
                "stages_ms": {"dpra_ls": s_st[0], "network": s_st[1], "wff2_probe": s_st[2],
                              "fallback_and_update": s_st[3]},
+               "network_ms": {"layer0": s_st[4], "tensor_core_layers_1_6": s_st[5], "layer7": s_st[6]},
                "fallback_fraction_timed": flagged / probed if probed else None,
                "probe": {"tile": SUR_TILE, "patch": SUR_PATCH, "tol_rad": SUR_TOL},
                "dilations": dil, "params": int(params.size),
@@ -402,6 +449,12 @@ def run_ours(args, rank, world, local):
                   "fp32_pipe": {"achieved_tflops": 2 * col_fma / (p_st[2] * 1e-3) / 1e12,
                                 "peak_tflops_at_clock": fp32_peak_tflops,
                                 "frac": 2 * col_fma / (p_st[2] * 1e-3) / 1e12 / fp32_peak_tflops}}
+    fb, P = fft_model_bytes(size)
+    plain_roof["fft_model"] = {
+        "what": "frame throughput x the FFT formulation's algorithmic bytes per frame ((64 n_freq + 32) P, "
+                "P = padded plane %d^2); the direct formulation here moves only the compulsory bytes" % int(P ** 0.5),
+        "bytes_per_frame": fb, "achieved": fb * p_val / world / 1e9, "peak": hbm_peak, "unit": "GB/s",
+        "frac": fb * p_val / world / 1e9 / hbm_peak}
     roof = plain_roof
     if sur and "stages_ms" in sur:
         net_bytes = SUR_BYTES_PER_PX * N
@@ -413,11 +466,28 @@ def run_ours(args, rank, world, local):
                     "tensor": {"achieved_tflops": SUR_FLOPS_PER_PX * N / (net_ms * 1e-3) / 1e12,
                                "peak_tflops": bf16_peak,
                                "frac": SUR_FLOPS_PER_PX * N / (net_ms * 1e-3) / 1e12 / bf16_peak}}
+        # the tensor-core layer: six launches per frame, timed together
+        conv_ms = sur["network_ms"]["tensor_core_layers_1_6"] / 6
+        conv_bytes, conv_flops = SUR_CONV_BYTES_PER_PX * N, SUR_CONV_FLOPS_PER_PX * N
+        conv_roof = {"kernel": "sur_conv_tc_kernel (tcgen05 32->32 dilated 3x3 layer, per launch)", "bound": "hbm",
+                     "achieved": conv_bytes / (conv_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": conv_bytes / (conv_ms * 1e-3) / 1e9 / hbm_peak,
+                     "traffic": SUR_CONV_TRAFFIC_1024 if size == 1024 else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at "
+                                       "1024x1024 (profiles/sur_conv_tc_kernel_1024.md)",
+                     "peak_source": peak_kind, "algorithmic_bytes_per_launch": conv_bytes,
+                     "launch_ms": conv_ms,
+                     "tensor": {"achieved_tflops": conv_flops / (conv_ms * 1e-3) / 1e12,
+                                "peak_tflops": bf16_peak,
+                                "frac": conv_flops / (conv_ms * 1e-3) / 1e12 / bf16_peak}}
         sur["roofline_network"] = net_roof
+        sur["roofline_tensor_core_layer"] = conv_roof
         sur["roofline_plain_column_sweep"] = plain_roof
-        top = max(sur["stages_ms"], key=sur["stages_ms"].get)
-        roof = net_roof if top == "network" else plain_roof if top == "fallback_and_update" else net_roof
-        sur["dominant_stage"] = top
+        kern = {"sur_conv_tc_kernel x6": sur["network_ms"]["tensor_core_layers_1_6"],
+                "wff_probe_kernel": sur["stages_ms"]["wff2_probe"], "dpra_ls_ff_kernel": sur["stages_ms"]["dpra_ls"],
+                "sur_l7_kernel": sur["network_ms"]["layer7"], "sur_l0_kernel": sur["network_ms"]["layer0"]}
+        sur["dominant_kernel"] = max(kern, key=kern.get)
+        roof = conv_roof
 
     headline = sur if (sur and "frames_per_s" in sur) else None
     out = {

@@ -77,7 +77,7 @@ struct glsu_dpra {
     bool unwrap = false;  // MATLAB fp_ls3u semantics: dphi = dphi_ref + unwrap(t)
     int unwrap_row = -1, unwrap_col = -1;
     int ls_method = GLSU_LS_FLOAT_FLOAT;
-    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     int frames_done = 0;
     // pipelined sequence over pinned host buffers: frame slot s uses
@@ -363,7 +363,7 @@ extern "C" int glsu_dpra_create(glsu_dpra **out, int precision, const void *h_ph
             cudaMemset(h->d_phi[GLSU_DPHI], 0, es * N) != cudaSuccess)
             rc = fail(GLSU_ERR_CUDA, "initial phase upload failed");
     }
-    for (int k = 0; k < 6 && rc == GLSU_OK; k++)
+    for (int k = 0; k < 8 && rc == GLSU_OK; k++)
         if (cudaEventCreate(&h->ev[k]) != cudaSuccess) rc = fail(GLSU_ERR_CUDA, "cudaEventCreate failed");
     if (rc == GLSU_OK && (cudaEventCreate(&h->t0) != cudaSuccess || cudaEventCreate(&h->t1) != cudaSuccess))
         rc = fail(GLSU_ERR_CUDA, "cudaEventCreate failed");
@@ -385,7 +385,7 @@ extern "C" int glsu_dpra_destroy(glsu_dpra *h)
     for (int k = 0; k < 4; k++) cudaFree(h->d_phi[k]);
     cudaFreeHost(h->h_in);
     cudaFreeHost(h->h_out);
-    for (int k = 0; k < 6; k++)
+    for (int k = 0; k < 8; k++)
         if (h->ev[k]) cudaEventDestroy(h->ev[k]);
     if (h->t0) cudaEventDestroy(h->t0);
     if (h->t1) cudaEventDestroy(h->t1);
@@ -438,18 +438,21 @@ static void dpra_surrogate_release(glsu_dpra *h)
     cudaFree(h->probe.resid);
     cudaFree(h->probe.flags);
     cudaFree(h->probe.counts);
+    cudaFree(h->probe.rows);
     h->d_filt = nullptr;
     h->probe = ProbeOut();
 }
 
 // Surrogate form of one frame after the LS stage (d_z): network -> probes ->
-// plain WFF2 on flagged tiles -> phase update.  Stage events: after the
-// network, after the probes, after fallback and update.
+// plain WFF2 on flagged tiles -> phase update.  Stage events: ev[0] before
+// the network, ev[6] after its layer 0, ev[7] after its six tensor-core
+// layers, ev[1] after the network, ev[2] after the probes, ev[3] after
+// fallback and update.
 static int dpra_surrogate_frame(glsu_dpra *h, cudaEvent_t *ev)
 {
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[0], h->stream));
     h->sur->stream = h->stream;
-    GLSU_TRY(h->sur->forward(h->d_z, h->d_filt));
+    GLSU_TRY(h->sur->forward(h->d_z, h->d_filt, ev ? ev + 6 : nullptr));
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[1], h->stream));
     if (h->sur_tol > 0) {
         GLSU_TRY(h->wff.enqueue_probe(h->stream, h->d_z, h->d_filt, h->sur_tile, h->sur_patch,
@@ -505,7 +508,8 @@ extern "C" int glsu_dpra_set_surrogate(glsu_dpra *h, const float *h_params, cons
             cudaMalloc(&h->probe.sites, nt * sizeof(int2)) != cudaSuccess ||
             cudaMalloc(&h->probe.resid, nt * sizeof(float)) != cudaSuccess ||
             cudaMalloc(&h->probe.flags, nt * sizeof(int)) != cudaSuccess ||
-            cudaMalloc(&h->probe.counts, 2 * sizeof(int)) != cudaSuccess)
+            cudaMalloc(&h->probe.counts, 2 * sizeof(int)) != cudaSuccess ||
+            cudaMalloc(&h->probe.rows, nt * h->wff.nfx * probe_rows_elems(s_inst) * sizeof(float2)) != cudaSuccess)
             rc = fail(GLSU_ERR_ALLOC, "allocation failed");
         if (rc == GLSU_OK) rc = h->wff.alloc_tile_list();
         if (rc == GLSU_OK && (cudaMemset(h->probe.counts, 0, 2 * sizeof(int)) != cudaSuccess ||
@@ -769,6 +773,10 @@ extern "C" int glsu_dpra_stage_times(glsu_dpra *h, float *ms, int n)
     const cudaEvent_t seq[5] = {h->ev[4], h->ev[0], h->ev[1], h->ev[2], h->ev[3]};
     int k = 0;
     for (; k < 4 && k < n; k++) GLSU_CUDA_TRY(cudaEventElapsedTime(&ms[k], seq[k], seq[k + 1]));
+    if (!h->sur) return k;
+    // surrogate form: the network split into layer 0, layers 1-6, layer 7
+    const cudaEvent_t net[4] = {h->ev[0], h->ev[6], h->ev[7], h->ev[1]};
+    for (int j = 0; j < 3 && k < n; j++, k++) GLSU_CUDA_TRY(cudaEventElapsedTime(&ms[k], net[j], net[j + 1]));
     return k;
 }
 

@@ -79,12 +79,15 @@ struct TileMask {
 // half-sizes (instantiated) up to 20, 4 above (P <= kProbeMaxP).
 constexpr int kProbeMaxP = 8;
 int probe_patch_for_half(int s_inst);
+// complex elements of the probe's row-pass block of one (tile, wx)
+size_t probe_rows_elems(int s_inst);
 struct ProbeOut {
     float2 *partial = nullptr;  // [ntiles][nfx * parts][P*P] partial sums
     int2 *sites = nullptr;      // [ntiles] (row, col) of each patch
     float *resid = nullptr;     // [ntiles] RMS phase residual of the surrogate
     int *flags = nullptr;       // [ntiles] residual > tolerance
     int *counts = nullptr;      // [2] cumulative: tiles probed, tiles flagged
+    float2 *rows = nullptr;     // [ntiles][nfx][probe_rows_elems]: row-filtered input of each (tile, wx)
 };
 
 // ---------------------------------------------------------------------------

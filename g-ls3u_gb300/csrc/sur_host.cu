@@ -136,10 +136,11 @@ int SurNet::check_error()
 }
 
 // Layers 0..6: z -> a6 (training: d_act[0..6]; inference: ping-pong).
-int SurNet::hidden(const float2 *z)
+int SurNet::hidden(const float2 *z, cudaEvent_t *ev)
 {
     sur_l0_kernel<<<rows_grid(), 256, 0, stream>>>(z, B, H, W, dil[0], h_w0, d_act[0]);
     GLSU_CUDA_TRY(cudaGetLastError());
+    if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[0], stream));
     for (int l = 1; l <= 6; l++) {
         SurConvArgs a;
         a.B = B;
@@ -154,14 +155,15 @@ int SurNet::hidden(const float2 *z)
         a.err = d_err;
         GLSU_TRY(launch_sur_conv(map_fwd[l], a, stream));
     }
+    if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[1], stream));
     return GLSU_OK;
 }
 
 const uint16_t *SurNet::a6() const { return training ? d_act[6] : d_act[0]; }
 
-int SurNet::forward(const void *d_z, void *d_outp)
+int SurNet::forward(const void *d_z, void *d_outp, cudaEvent_t *ev)
 {
-    GLSU_TRY(hidden((const float2 *)d_z));
+    GLSU_TRY(hidden((const float2 *)d_z, ev));
     return launch_l7((const float2 *)d_z, (float2 *)d_outp, nullptr, nullptr, nullptr);
 }
 

@@ -34,10 +34,11 @@ struct SurNet {
     int pack();
     int set_params(const float *h);
     int get_params(float *h);
-    int hidden(const float2 *z);
+    // layers 0..6; ev (optional, 2 events) is recorded after layer 0 and after layer 6
+    int hidden(const float2 *z, cudaEvent_t *ev = nullptr);
     const uint16_t *a6() const;
     // out = y / |y| of the network on z (complex [B][H][W]), enqueued on stream
-    int forward(const void *d_z, void *d_out);
+    int forward(const void *d_z, void *d_out, cudaEvent_t *ev = nullptr);
     // forward with loss and all parameter gradients into d_grad / d_loss
     int backward(const void *d_z, const void *d_target);
     int adam(float lr, float b1, float b2, float eps);

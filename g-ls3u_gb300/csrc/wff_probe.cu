@@ -36,14 +36,30 @@ template <int S> struct ProbeGeom {
     static constexpr int KU = (UY + NRG - 1) / NRG;
     static constexpr int UYP = NRG * KU;
     static constexpr int RYP = UYP + 2 * S;    // rows of R (>= P + 4S)
-    static constexpr int FR = 8;               // input rows staged per pass of the row filter
-    static constexpr int FX = RXP + 2 * S;
     static constexpr int CPT = (P + NRG - 1) / NRG;  // C rows per thread
-    static constexpr int UREG = (UYP * RXP > FR * FX + FX) ? UYP * RXP : FR * FX + FX;
-    static constexpr size_t SMEM = sizeof(float2) * ((size_t)RYP * RXP + UREG + RYP);
+    static constexpr size_t R_ELEMS = (size_t)RYP * RXP;  // one (tile, wx) block of R
+    static constexpr size_t SMEM = sizeof(float2) * (R_ELEMS + (size_t)UYP * RXP + RYP);
+    // row pass: a thread takes 16 adjacent columns of one row, 64 rows per chunk
+    static constexpr int SEG = 16;
+    static constexpr int NSEG = RXP / SEG;
+    static constexpr int CR = 64;
+    static constexpr int RTHREADS = NSEG * CR;
+    static constexpr int FX = RXP + 2 * S;     // staged input columns
+    static constexpr int FXS = FX | 1;         // odd row stride (float2): a warp's rows hit distinct bank pairs
+    static constexpr size_t RSMEM = sizeof(float2) * ((size_t)CR * FXS + FX);
 };
 
 int probe_patch_for_half(int s_inst) { return s_inst <= 20 ? 8 : 4; }
+
+size_t probe_rows_elems(int s_inst)
+{
+    switch (s_inst) {
+    case 12: return ProbeGeom<12>::R_ELEMS;
+    case 20: return ProbeGeom<20>::R_ELEMS;
+    case 30: return ProbeGeom<30>::R_ELEMS;
+    default: return ProbeGeom<45>::R_ELEMS;
+    }
+}
 
 struct ProbeArgs {
     const float2 *f, *ex, *ey;
@@ -53,6 +69,7 @@ struct ProbeArgs {
     uint32_t seed;
     float2 *partial;  // [ntiles][nfx * nsplit][P*P]
     int2 *sites;
+    float2 *rows;     // [ntiles][nfx][RYP][RXP]: R of each (tile, wx)
 };
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x)
@@ -75,19 +92,77 @@ __device__ __forceinline__ int2 probe_site(const ProbeArgs &a, int t)
     return make_int2(y0 + (int)(h1 % (uint32_t)max(1, th - a.P + 1)), x0 + (int)(h2 % (uint32_t)max(1, tw - a.P + 1)));
 }
 
+// Row pass, one CTA per (tile, wx): R = the rows py-2S .. py-2S+RYP-1,
+// demodulated by e^{-j wx x} and filtered along x, for the columns
+// px-S .. px-S+RXP-1 (zero outside the image and beyond RX).  A thread takes
+// 16 adjacent output columns of one row from 16+2S staged inputs, summing
+// the taps in ascending order for each output.
+template <int S>
+__global__ void __launch_bounds__(ProbeGeom<S>::RTHREADS) wff_probe_rows_kernel(ProbeArgs a, PTaps<float, S> gxr)
+{
+    using G = ProbeGeom<S>;
+    constexpr int RX = G::RX, RXP = G::RXP, RYP = G::RYP, FX = G::FX, FXS = G::FXS, CR = G::CR, SEG = G::SEG;
+    extern __shared__ __align__(16) float2 psm[];
+    float2 *fs = psm;            // [CR][FXS] demodulated input rows
+    float2 *es = fs + CR * FXS;  // [FX] e^{-j wx x}
+    const int t = blockIdx.x, i = blockIdx.y, tid = threadIdx.x;
+    const int rl = tid % CR, seg = tid / CR;
+    const int2 site = probe_site(a, t);
+    const int py = site.x, px = site.y;
+    const float2 *exi = a.ex + (size_t)i * (a.pitch + 2 * kPhasorPad) + kPhasorPad;
+    float2 *Rg = a.rows + ((size_t)t * gridDim.y + i) * G::R_ELEMS;
+    for (int e = tid; e < FX; e += G::RTHREADS) es[e] = exi[px - 2 * S + e];
+    for (int r0 = 0; r0 < RYP; r0 += CR) {
+        __syncthreads();  // es is written; the previous chunk has been consumed
+        for (int e = tid; e < CR * FX; e += G::RTHREADS) {
+            const int rr = e / FX, c = e - rr * FX;
+            const int y = py - 2 * S + r0 + rr, x = px - 2 * S + c;
+            float2 v = make_float2(0.f, 0.f);
+            if (r0 + rr < RYP && y >= 0 && y < a.H && x >= 0 && x < a.W) v = a.f[(size_t)y * a.W + x];
+            const float2 p = es[c];
+            fs[rr * FXS + c] = make_float2(v.x * p.x - v.y * p.y, v.x * p.y + v.y * p.x);
+        }
+        __syncthreads();
+        float2 acc[SEG];
+#pragma unroll
+        for (int q = 0; q < SEG; q++) acc[q] = make_float2(0.f, 0.f);
+        const float2 *row = fs + rl * FXS + seg * SEG;
+#pragma unroll
+        for (int j = 0; j < SEG + 2 * S; j++) {
+            const float2 v = row[j];
+#pragma unroll
+            for (int q = 0; q < SEG; q++) {
+                const int m = j - q;
+                if (m >= 0 && m <= 2 * S) {
+                    acc[q].x = fmaf(gxr.g[m], v.x, acc[q].x);
+                    acc[q].y = fmaf(gxr.g[m], v.y, acc[q].y);
+                }
+            }
+        }
+        const int r = r0 + rl;
+        if (r < RYP) {
+#pragma unroll
+            for (int q = 0; q < SEG; q++) {
+                const int col = seg * SEG + q, x = px - S + col;
+                const bool keep = col < RX && x >= 0 && x < a.W;
+                Rg[(size_t)r * RXP + col] = keep ? acc[q] : make_float2(0.f, 0.f);
+            }
+        }
+    }
+}
+
 // One CTA per (tile, wx, part of the wy range).  Lane = column, warps split
 // the rows; taps come from the parameter bank with compile-time indices.
 template <int S>
-__global__ void __launch_bounds__(ProbeGeom<S>::THREADS) wff_probe_kernel(ProbeArgs a, PTaps<float, S> gxr,
-                                                                          PTaps<float, S> gyA, PTaps<float, S> gyB,
-                                                                          PTaps<float, S> gxf)
+__global__ void __launch_bounds__(ProbeGeom<S>::THREADS) wff_probe_kernel(ProbeArgs a, PTaps<float, S> gyA,
+                                                                          PTaps<float, S> gyB, PTaps<float, S> gxf)
 {
     using G = ProbeGeom<S>;
-    constexpr int P = G::P, RX = G::RX, RXP = G::RXP, KU = G::KU, RYP = G::RYP, FR = G::FR, FX = G::FX;
+    constexpr int P = G::P, RXP = G::RXP, KU = G::KU, RYP = G::RYP;
     extern __shared__ __align__(16) float2 psm[];
     float2 *R = psm;                  // [RYP][RXP]
-    float2 *U = R + RYP * RXP;        // [UYP][RXP]; first the staged input
-    float2 *eys = U + G::UREG;        // [RYP] phasors e^{-j wy y} of the R rows
+    float2 *U = R + RYP * RXP;        // [UYP][RXP]
+    float2 *eys = U + G::UYP * RXP;   // [RYP] phasors e^{-j wy y} of the R rows
     const int t = blockIdx.x, i = blockIdx.y, part = blockIdx.z, tid = threadIdx.x;
     const int lane = tid & 31, w = tid >> 5, cg = w % G::NCG, rg = w / G::NCG;
     const int col = cg * 32 + lane;
@@ -97,34 +172,11 @@ __global__ void __launch_bounds__(ProbeGeom<S>::THREADS) wff_probe_kernel(ProbeA
     const float2 *exi = a.ex + (size_t)i * (a.pitch + 2 * kPhasorPad) + kPhasorPad;
     const float thr = *a.thr, thr2 = thr * thr;
 
-    // ---- R: rows py-2S .., demodulated by e^{-j wx x}, filtered along x (zero outside the image)
-    float2 *fs = U;              // [FR][FX]
-    float2 *es = U + FR * FX;    // [FX]
-    for (int e = tid; e < FX; e += G::THREADS) es[e] = exi[px - 2 * S + e];
-    for (int r0 = 0; r0 < RYP; r0 += FR) {
-        __syncthreads();
-        for (int e = tid; e < FR * FX; e += G::THREADS) {
-            const int rr = e / FX, c = e - rr * FX;
-            const int y = py - 2 * S + r0 + rr, x = px - 2 * S + c;
-            float2 v = make_float2(0.f, 0.f);
-            if (y >= 0 && y < a.H && x >= 0 && x < a.W) v = a.f[(size_t)y * a.W + x];
-            const float2 p = es[c];
-            fs[e] = make_float2(v.x * p.x - v.y * p.y, v.x * p.y + v.y * p.x);
-        }
-        __syncthreads();
-        for (int rr = rg; rr < FR && r0 + rr < RYP; rr += G::NRG) {
-            const int x = px - S + col;
-            float2 acc = make_float2(0.f, 0.f);
-            if (col < RX && x >= 0 && x < a.W) {
-                const float2 *row = fs + rr * FX + col;
-#pragma unroll
-                for (int m = 0; m <= 2 * S; m++) {
-                    acc.x = fmaf(gxr.g[m], row[m].x, acc.x);
-                    acc.y = fmaf(gxr.g[m], row[m].y, acc.y);
-                }
-            }
-            R[(r0 + rr) * RXP + col] = acc;
-        }
+    // ---- R of this (tile, wx) from the row pass (L2-resident)
+    {
+        const float4 *src = reinterpret_cast<const float4 *>(a.rows + ((size_t)t * gridDim.y + i) * G::R_ELEMS);
+        float4 *dst = reinterpret_cast<float4 *>(R);
+        for (int e = tid; e < (int)(G::R_ELEMS / 2); e += G::THREADS) dst[e] = src[e];
     }
 
     float2 cacc[G::CPT];
@@ -285,6 +337,8 @@ static int launch_probe(const WffPlan &Pl, ProbeArgs a, cudaStream_t s, const Pr
     if (!attr) {
         GLSU_CUDA_TRY(cudaFuncSetAttribute(wff_probe_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)G::SMEM));
+        GLSU_CUDA_TRY(cudaFuncSetAttribute(wff_probe_rows_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)G::RSMEM));
         attr = true;
     }
     const int ntiles = a.ntx * a.nty;
@@ -294,14 +348,15 @@ static int launch_probe(const WffPlan &Pl, ProbeArgs a, cudaStream_t s, const Pr
     double best = 1e30;
     for (int ns = 1; ns <= 4 && ns <= Pl.nfy; ns++) {
         const long long ctas = (long long)ntiles * Pl.nfx * ns;
-        const double cost = (double)((ctas + slots - 1) / slots) * (1.0 / ns + 0.06);
+        const double cost = (double)((ctas + slots - 1) / slots) * (1.0 / ns + 0.02);
         if (cost < best - 1e-9) {
             best = cost;
             a.nsplit = ns;
         }
     }
+    wff_probe_rows_kernel<S><<<dim3(ntiles, Pl.nfx), G::RTHREADS, G::RSMEM, s>>>(a, probe_taps<S>(Pl.gx, Pl.sx, 1.0));
     wff_probe_kernel<S><<<dim3(ntiles, Pl.nfx, a.nsplit), G::THREADS, G::SMEM, s>>>(
-        a, probe_taps<S>(Pl.gx, Pl.sx, 1.0), probe_taps<S>(Pl.gy, Pl.sy, Pl.inv_norm), probe_taps<S>(Pl.gy, Pl.sy, 1.0),
+        a, probe_taps<S>(Pl.gy, Pl.sy, Pl.inv_norm), probe_taps<S>(Pl.gy, Pl.sy, 1.0),
         probe_taps<S>(Pl.gx, Pl.sx, Pl.scale * Pl.inv_norm));
     wff_probe_resid_kernel<<<ntiles, 64, 0, s>>>(o.partial, o.sites, Pl.nfx * a.nsplit, G::P, a.W, a.H,
                                                  (const float2 *)d_cmp, (float)tol, o.resid, o.flags, o.counts);
@@ -336,6 +391,8 @@ int WffPlan::enqueue_probe(cudaStream_t s, const void *d_f, const void *d_cmp, i
     a.seed = seed;
     a.partial = o.partial;
     a.sites = o.sites;
+    a.rows = o.rows;
+    if (!o.rows || !o.partial || !o.sites) return fail(GLSU_ERR_INVALID, "probe buffers not allocated");
     switch (S) {
     case 12: return launch_probe<12>(*this, a, s, o, d_cmp, tol);
     case 20: return launch_probe<20>(*this, a, s, o, d_cmp, tol);

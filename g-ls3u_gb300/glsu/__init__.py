@@ -401,8 +401,10 @@ class DPRA:
         check(lib().glsu_dpra_stage_timing(self._h, int(enable)))
 
     def stage_times(self):
-        ms = (ctypes.c_float * 4)()
-        n = check(lib().glsu_dpra_stage_times(self._h, ms, 4))
+        """Stage times (ms) of the last frame: 4 stages, plus the network's
+        layer 0 / tensor-core layers / layer 7 split in the surrogate form."""
+        ms = (ctypes.c_float * 7)()
+        n = check(lib().glsu_dpra_stage_times(self._h, ms, 7))
         return list(ms[:n])
 
 

@@ -200,9 +200,12 @@ int glsu_dpra_set_unwrap(glsu_dpra *h, int enable, int start_row, int start_col)
 int glsu_dpra_set_method(glsu_dpra *h, int method);
 /* Record CUDA events between the stages of each frame (off by default). */
 int glsu_dpra_stage_timing(glsu_dpra *h, int enable);
-/* Device times (ms) of the stages of the last frame: [0] LS solve, [1] WFF
- * row pass, [2] WFF column sweep, [3] WFF final row pass + phase update.
- * Returns the number of stages written. */
+/* Device times (ms) of the stages of the last frame.  Plain form: [0] LS
+ * solve, [1] WFF row pass, [2] WFF column sweep, [3] WFF final row pass +
+ * phase update.  Surrogate form: [0] LS solve, [1] network, [2] WFF2 probes,
+ * [3] fallback + phase update, then the network split into [4] layer 0,
+ * [5] the six tensor-core layers, [6] layer 7.  Returns the number of
+ * stages written (at most n). */
 int glsu_dpra_stage_times(glsu_dpra *h, float *ms, int n);
 
 /* ---- spatial unwrapping: MatLab/fp_unwrapping.m ------------------------- */
