@@ -203,7 +203,8 @@ struct SurL7W {
     float b[2];
 };
 int sur_make_map(CUtensorMap *tm, const void *act, int B, int H, int W, int dil);
-int launch_sur_conv(const CUtensorMap &tm, const SurConvArgs &a, cudaStream_t s);
+int sur_make_out_map(CUtensorMap *tm, const void *act, int B, int H, int W);
+int launch_sur_conv(const CUtensorMap &tm, const CUtensorMap &tmo, const SurConvArgs &a, cudaStream_t s);
 
 // AIA
 struct AiaDev {

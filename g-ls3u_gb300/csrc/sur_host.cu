@@ -75,8 +75,13 @@ int SurNet::init(int batch, int width, int height, const int *dilations, bool tr
     // tensor maps: forward layer l reads its input with dilation dil[l]
     for (int l = 1; l <= 6; l++) {
         const void *in = training ? d_act[l - 1] : d_act[(l - 1) & 1];
+        const void *out = training ? d_act[l] : d_act[l & 1];
         GLSU_TRY(sur_make_map(&map_fwd[l], in, B, H, W, dil[l]));
-        if (training) GLSU_TRY(sur_make_map(&map_bwd[l], d_g[(6 - l) & 1], B, H, W, dil[l]));
+        GLSU_TRY(sur_make_out_map(&map_fwd_out[l], out, B, H, W));
+        if (training) {
+            GLSU_TRY(sur_make_map(&map_bwd[l], d_g[(6 - l) & 1], B, H, W, dil[l]));
+            GLSU_TRY(sur_make_out_map(&map_bwd_out[l], d_g[(7 - l) & 1], B, H, W));
+        }
     }
     return pack();
 }
@@ -153,7 +158,7 @@ int SurNet::hidden(const float2 *z, cudaEvent_t *ev)
         a.out = training ? d_act[l] : d_act[l & 1];
         a.relu = 1;
         a.err = d_err;
-        GLSU_TRY(launch_sur_conv(map_fwd[l], a, stream));
+        GLSU_TRY(launch_sur_conv(map_fwd[l], map_fwd_out[l], a, stream));
     }
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[1], stream));
     return GLSU_OK;
@@ -204,7 +209,7 @@ int SurNet::backward(const void *d_z, const void *d_target)
         a.out = gprev;
         a.relu = 0;
         a.err = d_err;
-        GLSU_TRY(launch_sur_conv(map_bwd[l], a, stream));
+        GLSU_TRY(launch_sur_conv(map_bwd[l], map_bwd_out[l], a, stream));
     }
     // layer 0: weight gradient from g0 (in d_g[0] after six swaps) and the input
     sur_dw_small_kernel<32, 2><<<nbs, 256, 0, stream>>>(d_g[0], z, B, H, W, dil[0], kSurSmallPix, d_part);
@@ -377,8 +382,9 @@ extern "C" int glsu_sur_conv32(const void *d_in, void *d_out, int batch, int wid
         cudaMalloc(&d_pkb, 6 * 9216 * 2) != cudaSuccess || cudaMalloc(&d_w0r, 576 * 4) != cudaSuccess ||
         cudaMalloc(&d_w7r, 576 * 4) != cudaSuccess || cudaMalloc(&d_err, 4) != cudaSuccess)
         rc = fail(GLSU_ERR_ALLOC, "allocation failed");
-    CUtensorMap tm;
+    CUtensorMap tm, tmo;
     if (rc == GLSU_OK) rc = sur_make_map(&tm, d_in, batch, height, width, dilation);
+    if (rc == GLSU_OK) rc = sur_make_out_map(&tmo, d_out, batch, height, width);
     if (rc == GLSU_OK) {
         cudaMemcpyAsync(d_master, master.data(), kSurParams * 4, cudaMemcpyHostToDevice, s);
         cudaMemsetAsync(d_err, 0, 4, s);
@@ -394,7 +400,7 @@ extern "C" int glsu_sur_conv32(const void *d_in, void *d_out, int batch, int wid
         a.out = (uint16_t *)d_out;
         a.relu = relu;
         a.err = d_err;
-        rc = launch_sur_conv(tm, a, s);
+        rc = launch_sur_conv(tm, tmo, a, s);
     }
     int e = 0;
     if (rc == GLSU_OK && cudaMemcpyAsync(&e, d_err, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)

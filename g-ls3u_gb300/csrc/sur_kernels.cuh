@@ -12,22 +12,36 @@
 // tensor-core layers).  Activations are NHWC [B][H][W][32] BF16, 64 bytes a
 // pixel.
 //
-// Tensor-core layer (sur_conv_tc_kernel): one MMA tile is 128 consecutive
-// pixels of one output row (M = 128) x 32 output channels (N = 32), and
-// K = 9 taps x 32 input channels, issued as 18 tcgen05.mma of K = 16.  The
-// input rows are loaded by TMA through a 5-D tensor map whose box is
-// {8 channels, 128 + 2d pixels, 4 channel chunks} -- in shared memory that
-// is "chunk-planar": chunk c at c * (128 + 2d) * 16 bytes, pixel p at p * 16
-// within it, i.e. the K-major no-swizzle operand layout with 8-row groups
-// 128 B apart.  A tap's horizontal offset dx * d is then just a shift of the
-// descriptor start by 16 * dx * d bytes, so the 9 taps read the same three
-// input rows without any im2col copy, and TMA zero-fills the image border.
-// Work items are chunks of a chain of output rows y = r, r + d, r + 2d, ...
-// (the rows that share input rows under dilation d).  The kernel is
-// persistent and warp-specialised: one thread streams every item's input
-// rows through a ring of slots by TMA, one thread issues the MMAs, four warps
-// drain the accumulator, which is double-buffered in TMEM so the epilogue of
-// one row overlaps the MMAs of the next.
+// Tensor-core layer (sur_conv_tc_kernel): the MMA tile is 128 consecutive
+// pixels of one row (M = 128), K = 16 input channels per tcgen05.mma.  The
+// input rows are loaded by TMA through a 4-D tensor map {32 channels, W, H,
+// B} with box {32, 128 + 2d, 1, 1} and 64-byte swizzle: each pixel's 64
+// bytes arrive as one line, and in shared memory they form the K-major
+// SWIZZLE_64B operand layout (rows of 64 bytes, 8-row groups 512 bytes
+// apart, the 16-byte chunks of a row permuted by address bits 7-8).  A tap's
+// horizontal offset dx * d is a shift of the descriptor start by 64 * dx * d
+// bytes, the second K = 16 half a shift by 32 bytes, with the base offset
+// field left at 0: the tensor core applies the swizzle to the absolute
+// shared-memory address, as TMA does (measured: every dilation 1..16 and odd
+// shifts agree with the oracle), so no im2col copy is needed, and TMA
+// zero-fills the image border.  The epilogue writes each warp's 32 output pixels into a
+// staging tile in the same swizzled layout (conflict-free 16-byte stores)
+// and one thread stores the tile with a TMA tensor store.
+// Work items are chunks of kSurRows output rows of one chain y = r, r + d,
+// r + 2d, ... (the rows that share input rows under dilation d).  Input row j
+// of an item (j = 0 .. nout + 1) feeds output rows j - 2, j - 1, j through
+// the vertical taps dy = 2, 1, 0, so each input row is consumed by ONE MMA
+// per (dx, K half) with N = 96: the B operand stacks the three vertical taps'
+// weights [dy = 2 | dy = 1 | dy = 0] and the D columns are the three output
+// rows' accumulators, which sit side by side in TMEM (output row k of the
+// item at columns 32k .. 32k + 31).  At the ends of an item N shrinks to 64
+// or 32.  Every MMA accumulates: the epilogue fills each accumulator with the
+// bias before its first use and again after draining it.  A row's 18 K = 16
+// products are thus 6 MMAs of up to N = 96 instead of 18 of N = 32 (an N = 32
+// MMA costs nearly as much as an N = 96 one).
+// The kernel is persistent and warp-specialised: one thread streams every
+// item's input rows through a ring of slots by TMA, one thread issues the
+// MMAs, four warps drain the accumulators.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -41,8 +55,15 @@
 namespace glsu {
 
 constexpr int kSurSlots = 8;     // input-row ring of the tensor-core conv (TMA loads in flight)
-constexpr int kSurRows = 16;     // output rows per CTA (one chain segment)
+constexpr int kSurRows = 8;      // output rows per work item = TMEM accumulators (32 columns each)
+constexpr int kSurTmemCols = kSurRows * 32;
 constexpr int kSurWBytes = 9 * 4 * 32 * 16;  // packed B operand of one layer
+// packed B operand: [dx][K half kc][8-channel chunk h][96 rows][8 channels],
+// row n = 32 * (2 - dy) + output channel
+constexpr int kSurBRows = 96;
+constexpr int kSurBHalf = kSurBRows * 16;      // bytes between the two 8-channel chunks of one K = 16 step
+constexpr int kSurBStep = 2 * kSurBHalf;       // bytes of one (dx, kc) operand
+constexpr int kSurStageBytes = 32 * 64;        // one epilogue warp's output tile
 
 __device__ __forceinline__ float bf2f(uint16_t v) { return __uint_as_float((uint32_t)v << 16); }
 
@@ -90,10 +111,13 @@ __device__ __forceinline__ SurItem sur_item(const SurConvArgs &a, int item)
 
 // Persistent, warp-specialised: thread 0 of warp 0 issues the TMA row loads
 // into a ring of kSurSlots slots, thread 0 of warp 1 issues the MMAs, warps
-// 4-7 drain the two TMEM accumulators.  All three walk the same item list
-// (blockIdx.x, + gridDim.x, ...); input rows and accumulators are numbered
-// across items, which keeps the mbarrier phases consistent.
-__global__ void __launch_bounds__(256, 1) sur_conv_tc_kernel(const __grid_constant__ CUtensorMap tm, SurConvArgs a,
+// 4-7 drain the accumulators.  All three walk the same item list
+// (blockIdx.x, + gridDim.x, ...); input rows are numbered across items and
+// each accumulator completes one phase of its two mbarriers per item (a
+// block that an item leaves unused gets an empty phase), which keeps the
+// mbarrier parities consistent.
+__global__ void __launch_bounds__(256, 1) sur_conv_tc_kernel(const __grid_constant__ CUtensorMap tm,
+                                                             const __grid_constant__ CUtensorMap tmo, SurConvArgs a,
                                                              int nitems)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
@@ -101,31 +125,32 @@ __global__ void __launch_bounds__(256, 1) sur_conv_tc_kernel(const __grid_consta
     const int slot_bytes = (BW * 64 + 1023) & ~1023;
     unsigned char *wsm = sm;
     unsigned char *slots = sm + kSurWBytes;
-    uint64_t *full = reinterpret_cast<uint64_t *>(slots + kSurSlots * slot_bytes);
+    unsigned char *stage = slots + kSurSlots * slot_bytes;  // [4 warps][32 px][64 B], 64-byte swizzle
+    uint64_t *full = reinterpret_cast<uint64_t *>(stage + 4 * kSurStageBytes);
     uint64_t *sfree = full + kSurSlots;
-    uint64_t *accf = sfree + kSurSlots;
-    uint64_t *acce = accf + 2;
-    uint64_t *drain = acce + 2;
+    uint64_t *accf = sfree + kSurSlots;  // [kSurRows] accumulator complete
+    uint64_t *acce = accf + kSurRows;    // [kSurRows] accumulator drained and refilled with the bias
+    uint64_t *drain = acce + kSurRows;
     float *bias_s = reinterpret_cast<float *>(drain + 1);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(bias_s + 32);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int e = tid; e < kSurWBytes / 16; e += 256)
-        reinterpret_cast<uint4 *>(wsm)[e] = reinterpret_cast<const uint4 *>(a.wpack)[e];
-    if (tid < 32) bias_s[tid] = a.bias ? a.bias[tid] : 0.f;
     if (tid == 0) {
         for (int s = 0; s < kSurSlots; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&sfree[s], 1);
         }
-        mbar_init(&accf[0], 1);
-        mbar_init(&accf[1], 1);
-        mbar_init(&acce[0], 128);
-        mbar_init(&acce[1], 128);
+        for (int b = 0; b < kSurRows; b++) {
+            mbar_init(&accf[b], 1);
+            mbar_init(&acce[b], 128);
+        }
         mbar_init(drain, 1);
         fence_mbar_init();
     }
-    if (warp == 0) tmem_alloc(tslot, 64);
+    if (warp == 0) tmem_alloc(tslot, kSurTmemCols);
+    for (int e = tid; e < kSurWBytes / 16; e += 256)
+        reinterpret_cast<uint4 *>(wsm)[e] = reinterpret_cast<const uint4 *>(a.wpack)[e];
+    if (tid < 32) bias_s[tid] = a.bias ? a.bias[tid] : 0.f;
     fence_proxy_async_smem();  // the weight image was written by generic stores
     tc_fence_before();
     __syncthreads();
@@ -145,8 +170,8 @@ __global__ void __launch_bounds__(256, 1) sur_conv_tc_kernel(const __grid_consta
                     break;
                 }
                 mbar_expect_tx(&full[s], (uint32_t)BW * 64);
-                tma_load_5d(slots + s * slot_bytes, &tm, &full[s], 0, it.x0 - a.dil, 0,
-                            it.r + (it.kbeg + j - 1) * a.dil, it.b);
+                tma_load_4d(slots + s * slot_bytes, &tm, &full[s], 0, it.x0 - a.dil, it.r + (it.kbeg + j - 1) * a.dil,
+                            it.b);
             }
         }
         if (!ok) atomicExch(a.err, GLSU_ERR_TIMEOUT);
@@ -155,107 +180,134 @@ __global__ void __launch_bounds__(256, 1) sur_conv_tc_kernel(const __grid_consta
             mbar_wait_bounded(&full[j % kSurSlots], (j / kSurSlots) & 1);
     } else if (warp == 1 && lane == 0) {
         // ---- MMA issuer ----
-        const uint32_t idesc = umma_idesc_bf16(128, 32);
         const uint32_t wbase = smem_u32(wsm), sbase = smem_u32(slots);
-        const uint32_t lbo_a = (uint32_t)BW * 16;
-        uint32_t g0 = 0, waited = 0, acc = 0;
+        uint32_t g = 0, li = 0;
         bool ok = true;
-        for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+        for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x, li++) {
             const SurItem it = sur_item(a, item);
-            if (it.nout <= 0) continue;
-            for (int k = 0; k < it.nout; k++, acc++) {
-                for (; waited < g0 + k + 3; waited++)
-                    if (!mbar_wait_bounded(&full[waited % kSurSlots], (waited / kSurSlots) & 1)) ok = false;
-                if (ok && acc >= 2 && !mbar_wait_bounded(&acce[acc & 1], ((acc >> 1) - 1) & 1)) ok = false;
+            if (it.nout <= 0) {
+                li--;
+                continue;
+            }
+            const uint32_t par = li & 1;
+            for (int j = 0; j < it.nout + 2 && ok; j++, g++) {
+                const int s = g % kSurSlots;
+                if (!mbar_wait_bounded(&full[s], (g / kSurSlots) & 1)) ok = false;
+                // output row j is first written by this input row: its accumulator must hold the bias
+                if (ok && j < it.nout && !mbar_wait_bounded(&acce[j], par)) ok = false;
                 if (!ok) break;
                 tc_fence_after();
-                const uint32_t d = tmem + (acc & 1) * 32;
+                const int klo = max(0, j - 2), khi = min(it.nout - 1, j);
+                const uint32_t id = khi == klo       ? umma_idesc_bf16(128, 32)
+                                    : khi == klo + 1 ? umma_idesc_bf16(128, 64)
+                                                     : umma_idesc_bf16(128, 96);
+                const uint32_t d = tmem + (uint32_t)(klo * 32);
+                const uint32_t srow = sbase + (uint32_t)(s * slot_bytes);
+                const uint32_t brow = wbase + (uint32_t)((2 - j + klo) * 32 * 16);
 #pragma unroll
-                for (int dy = 0; dy < 3; dy++) {
-                    const uint32_t srow = sbase + (uint32_t)(((g0 + k + dy) % kSurSlots) * slot_bytes);
+                for (int dx = 0; dx < 3; dx++) {
 #pragma unroll
-                    for (int dx = 0; dx < 3; dx++) {
-#pragma unroll
-                        for (int kc = 0; kc < 2; kc++) {
-                            const uint64_t ad =
-                                umma_desc(srow + kc * 2 * lbo_a + (uint32_t)(dx * a.dil * 16), lbo_a, 128);
-                            const uint64_t bd =
-                                umma_desc(wbase + (uint32_t)((dy * 3 + dx) * 2048 + kc * 1024), 512, 128);
-                            umma_bf16(d, ad, bd, idesc, (dy | dx | kc) ? 1u : 0u);
-                        }
+                    for (int kc = 0; kc < 2; kc++) {
+                        const uint32_t astart = srow + (uint32_t)(dx * a.dil * 64 + kc * 32);
+                        const uint64_t ad = umma_desc_sw64(astart, 0);
+                        const uint64_t bd = umma_desc(brow + (uint32_t)((dx * 2 + kc) * kSurBStep), kSurBHalf, 128);
+                        umma_bf16(d, ad, bd, id, 1u);
                     }
                 }
-                umma_commit(&accf[acc & 1]);
-                umma_commit(&sfree[(g0 + k) % kSurSlots]);  // input row g0 + k is not read again
-                if (k == it.nout - 1) {
-                    umma_commit(&sfree[(g0 + k + 1) % kSurSlots]);
-                    umma_commit(&sfree[(g0 + k + 2) % kSurSlots]);
-                }
+                umma_commit(&sfree[s]);              // input row g is not read again
+                if (j >= 2) umma_commit(&accf[j - 2]);  // output row j - 2 has all its products
             }
-            g0 += it.nout + 2;
+            // accumulators this item leaves unused: an empty phase
+            for (int b = it.nout; b < kSurRows && ok; b++) {
+                if (!mbar_wait_bounded(&acce[b], par)) ok = false;
+                else umma_commit(&accf[b]);
+            }
         }
         if (!ok) atomicExch(a.err, GLSU_ERR_TIMEOUT);
         umma_commit(drain);  // every MMA has completed before TMEM is released
         mbar_wait_bounded(drain, 0);
     } else if (warp >= 4) {
-        // ---- epilogue: TMEM -> bias, ReLU, mask -> BF16 NHWC ----
+        // ---- epilogue: TMEM -> ReLU, mask -> BF16 NHWC; refill with the bias ----
         const int q = warp - 4;
-        uint32_t acc = 0;
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+        unsigned char *my_stage = stage + q * kSurStageBytes;
+        float bias[32];
+#pragma unroll
+        for (int c = 0; c < 32; c++) bias[c] = bias_s[c];
+        for (int b = 0; b < kSurRows; b++) tmem_st32(lane_base + b * 32, bias);
+        tc_fence_before();
+        for (int b = 0; b < kSurRows; b++) mbar_arrive(&acce[b]);
+        uint32_t li = 0;
         bool ok = true;
         for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
             const SurItem it = sur_item(a, item);
+            if (it.nout <= 0) continue;
             const int x = it.x0 + q * 32 + lane;
-            for (int k = 0; k < it.nout; k++, acc++) {
-                // warp-uniform: tcgen05.ld below is a warp-collective instruction
-                if (!__all_sync(0xffffffffu, mbar_wait_bounded(&accf[acc & 1], (acc >> 1) & 1))) {
+            for (int k = 0; k < kSurRows; k++) {
+                // warp-uniform: tcgen05.ld / st below are warp-collective instructions
+                if (!__all_sync(0xffffffffu, mbar_wait_bounded(&accf[k], li & 1))) {
                     if (lane == 0) atomicExch(a.err, GLSU_ERR_TIMEOUT);
                     ok = false;
                     break;
                 }
                 tc_fence_after();
                 float v[32];
-                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (acc & 1) * 32, v);
+                if (k < it.nout) {
+                    tmem_ld32(lane_base + k * 32, v);
+                    tmem_st32(lane_base + k * 32, bias);
+                }
                 tc_fence_before();
-                mbar_arrive(&acce[acc & 1]);
+                mbar_arrive(&acce[k]);
+                if (k >= it.nout) continue;
                 const int y = it.r + (it.kbeg + k) * a.dil;
-                if (x < a.W) {
-                    const size_t off = (((size_t)it.b * a.H + y) * a.W + x) * 32;
+                if (a.relu) {
 #pragma unroll
-                    for (int c = 0; c < 32; c++) {
-                        v[c] += bias_s[c];
-                        if (a.relu) v[c] = fmaxf(v[c], 0.f);
+                    for (int c = 0; c < 32; c++) v[c] = fmaxf(v[c], 0.f);
+                }
+                if (a.mask && x < a.W) {
+                    const uint4 *mp =
+                        reinterpret_cast<const uint4 *>(a.mask + (((size_t)it.b * a.H + y) * a.W + x) * 32);
+#pragma unroll
+                    for (int g = 0; g < 4; g++) {
+                        float mv[8];
+                        unpack8(mp[g], mv);
+#pragma unroll
+                        for (int i = 0; i < 8; i++)
+                            if (!(mv[i] > 0.f)) v[8 * g + i] = 0.f;
                     }
-                    if (a.mask) {
-                        const uint4 *mp = reinterpret_cast<const uint4 *>(a.mask + off);
+                }
+                // the previous tile of this warp has been read by its TMA store
+                if (lane == 0) bulk_wait_read0();
+                __syncwarp();
 #pragma unroll
-                        for (int g = 0; g < 4; g++) {
-                            float mv[8];
-                            unpack8(mp[g], mv);
-#pragma unroll
-                            for (int i = 0; i < 8; i++)
-                                if (!(mv[i] > 0.f)) v[8 * g + i] = 0.f;
-                        }
-                    }
-                    uint4 *op = reinterpret_cast<uint4 *>(a.out + off);
-#pragma unroll
-                    for (int g = 0; g < 4; g++)
-                        op[g] = make_uint4(pack_bf2(v[8 * g], v[8 * g + 1]), pack_bf2(v[8 * g + 2], v[8 * g + 3]),
-                                           pack_bf2(v[8 * g + 4], v[8 * g + 5]), pack_bf2(v[8 * g + 6], v[8 * g + 7]));
+                for (int g = 0; g < 4; g++)
+                    *reinterpret_cast<uint4 *>(my_stage + lane * 64 + ((g ^ ((lane >> 1) & 3)) * 16)) =
+                        make_uint4(pack_bf2(v[8 * g], v[8 * g + 1]), pack_bf2(v[8 * g + 2], v[8 * g + 3]),
+                                   pack_bf2(v[8 * g + 4], v[8 * g + 5]), pack_bf2(v[8 * g + 6], v[8 * g + 7]));
+                fence_proxy_async_smem();
+                __syncwarp();
+                // columns beyond W are clipped by the store
+                if (lane == 0 && it.x0 + q * 32 < a.W) {
+                    tma_store_4d(&tmo, my_stage, 0, it.x0 + q * 32, y, it.b);
+                    bulk_commit();
                 }
             }
+            li++;
         }
+        if (lane == 0) bulk_wait0();  // every output tile has been written
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, 64);
+    if (warp == 0) tmem_dealloc(tmem, kSurTmemCols);
 }
 
 int sur_conv_smem_bytes(int dil)
 {
     const int BW = 128 + 2 * dil;
     const int slot_bytes = (BW * 64 + 1023) & ~1023;
-    return kSurWBytes + kSurSlots * slot_bytes + (2 * kSurSlots + 5) * 8 + 32 * 4 + 16;
+    return kSurWBytes + kSurSlots * slot_bytes + 4 * kSurStageBytes + (2 * kSurSlots + 2 * kSurRows + 1) * 8 + 32 * 4 +
+           16;
 }
 
 int sur_conv_items(int B, int H, int W, int dil)
@@ -265,26 +317,37 @@ int sur_conv_items(int B, int H, int W, int dil)
     return B * nsx * dil * nch;
 }
 
-// 5-D map of a [B][H][W][32] BF16 activation tensor: {8 channels, W, 4
-// chunks, H, B} with strides {64 B, 16 B, W*64 B, H*W*64 B}; box
-// {8, 128 + 2d, 4, 1, 1}.
-int sur_make_map(CUtensorMap *tm, const void *act, int B, int H, int W, int dil)
+// 4-D map {32 channels, W, H, B} of a [B][H][W][32] BF16 activation tensor
+// (strides 64 B, W*64 B, H*W*64 B) with box {32, box_px, 1, 1} and 64-byte
+// swizzle: the conv's input rows (box_px = 128 + 2d) and output tiles
+// (box_px = 32).
+static int sur_make_map_box(CUtensorMap *tm, const void *act, int B, int H, int W, int box_px)
 {
     auto enc = get_encode_fn();
     if (!enc) return fail(GLSU_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-    if (dil < 1 || 128 + 2 * dil > 256) return fail(GLSU_ERR_INVALID, "surrogate dilation must be 1..64");
-    cuuint64_t dims[5] = {8, (cuuint64_t)W, 4, (cuuint64_t)H, (cuuint64_t)B};
-    cuuint64_t strides[4] = {64, 16, (cuuint64_t)W * 64, (cuuint64_t)H * W * 64};
-    cuuint32_t box[5] = {8, (cuuint32_t)(128 + 2 * dil), 4, 1, 1};
-    cuuint32_t es[5] = {1, 1, 1, 1, 1};
-    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(act), dims, strides, box, es,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+    cuuint64_t dims[4] = {32, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    cuuint64_t strides[3] = {64, (cuuint64_t)W * 64, (cuuint64_t)H * W * 64};
+    cuuint32_t box[4] = {32, (cuuint32_t)box_px, 1, 1};
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(act), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(GLSU_ERR_CUDA, "cuTensorMapEncodeTiled failed for an activation map");
     return GLSU_OK;
 }
 
-int launch_sur_conv(const CUtensorMap &tm, const SurConvArgs &a, cudaStream_t s)
+int sur_make_map(CUtensorMap *tm, const void *act, int B, int H, int W, int dil)
+{
+    if (dil < 1 || 128 + 2 * dil > 256) return fail(GLSU_ERR_INVALID, "surrogate dilation must be 1..64");
+    return sur_make_map_box(tm, act, B, H, W, 128 + 2 * dil);
+}
+
+int sur_make_out_map(CUtensorMap *tm, const void *act, int B, int H, int W)
+{
+    return sur_make_map_box(tm, act, B, H, W, 32);
+}
+
+int launch_sur_conv(const CUtensorMap &tm, const CUtensorMap &tmo, const SurConvArgs &a, cudaStream_t s)
 {
     static int attr_bytes = 0, sms = 0, regs = 0;
     const int smem = sur_conv_smem_bytes(a.dil);
@@ -306,14 +369,15 @@ int launch_sur_conv(const CUtensorMap &tm, const SurConvArgs &a, cudaStream_t s)
     // persistent: as many CTAs as are resident at once, each walking a
     // strided list of items.  Residency is bounded by registers (per-warp
     // allocation in units of 256), shared memory (1 KB reserved per CTA) and
-    // the 512 TMEM columns (64 per CTA).
+    // the 512 TMEM columns.
     const int warp_regs = (regs * 32 + 255) / 256 * 256;
     const int by_regs = 65536 / (8 * warp_regs);
     const int by_smem = (228 * 1024) / (smem + 1024);
-    const int per_sm = std::max(1, std::min(std::min(by_regs, by_smem), 8));
+    const int by_tmem = 512 / kSurTmemCols;
+    const int per_sm = std::max(1, std::min(std::min(by_regs, by_smem), by_tmem));
     const int items = sur_conv_items(a.B, a.H, a.W, a.dil);
     const int grid = std::min(items, per_sm * sms);
-    sur_conv_tc_kernel<<<grid, 256, smem, s>>>(tm, a, items);
+    sur_conv_tc_kernel<<<grid, 256, smem, s>>>(tm, tmo, a, items);
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
 }
@@ -652,10 +716,20 @@ __global__ void sur_adam_kernel(float *__restrict__ w, const float *__restrict__
 
 __device__ __forceinline__ float bf16_round(float f) { return __bfloat162float(__float2bfloat16_rn(f)); }
 
+// Element index in the packed B operand of one layer: tap t = 3 dy + dx, K
+// index k (input channel of the layer), N index n (output channel):
+// [dx][kc = k / 16][h = (k / 8) % 2][row 32 (2 - dy) + n][k % 8].
+__device__ __forceinline__ int sur_bpack_index(int t, int k, int n)
+{
+    const int dy = t / 3, dx = t % 3;
+    return ((dx * 2 + k / 16) * 2 + (k / 8) % 2) * kSurBRows * 8 + (32 * (2 - dy) + n) * 8 + k % 8;
+}
+
 // From the FP32 master parameters (per layer W[co][ci][3][3] then b[co]):
-//   pk_fwd[l][t][chunk][n=co][8 ci] and pk_bwd[l][t'][chunk][n=ci][8 co]
-//   (t' = 8 - t: the transposed, flipped kernel of the backward-data pass)
-//   for the six tensor-core layers; BF16-rounded FP32 copies of layers 0, 7.
+//   pk_fwd[l] with B[n = co][k = ci] and pk_bwd[l] with B[n = ci][k = co] of
+//   the flipped tap 8 - t (the transposed, flipped kernel of the
+//   backward-data pass) for the six tensor-core layers; BF16-rounded FP32
+//   copies of layers 0 and 7.
 __global__ void sur_pack_kernel(const float *__restrict__ master, uint16_t *__restrict__ pk_fwd,
                                 uint16_t *__restrict__ pk_bwd, float *__restrict__ w0r, float *__restrict__ w7r)
 {
@@ -669,10 +743,10 @@ __global__ void sur_pack_kernel(const float *__restrict__ master, uint16_t *__re
     const float wv = master[kSurL0Params + l * kSurL32Params + e];
     const __nv_bfloat16 h = __float2bfloat16_rn(wv);
     const uint16_t bits = *reinterpret_cast<const uint16_t *>(&h);
-    // forward: B[n = co][k = ci] of tap t
-    pk_fwd[(size_t)l * 9216 + ((t * 4 + ci / 8) * 32 + co) * 8 + (ci % 8)] = bits;
-    // backward data: B[n = ci][k = co] of tap 8 - t
-    pk_bwd[(size_t)l * 9216 + (((8 - t) * 4 + co / 8) * 32 + ci) * 8 + (co % 8)] = bits;
+    // forward: B[n = 32 (2 - dy) + co][k = ci] of tap t = 3 dy + dx
+    pk_fwd[(size_t)l * 9216 + sur_bpack_index(t, ci, co)] = bits;
+    // backward data: B[n = 32 (2 - dy') + ci][k = co] of the flipped tap t' = 8 - t
+    pk_bwd[(size_t)l * 9216 + sur_bpack_index(8 - t, co, ci)] = bits;
 }
 
 // Gather training crops: x[b] = pool_x[idx[b]][oy:oy+h, ox:ox+w] (complex),

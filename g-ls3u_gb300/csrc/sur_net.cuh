@@ -27,7 +27,8 @@ struct SurNet {
     double *d_lpart = nullptr, *d_loss = nullptr;
     int nb32 = 0, nbs = 0, adam_t = 0;
     int *d_err = nullptr;
-    CUtensorMap map_fwd[7], map_bwd[7];
+    CUtensorMap map_fwd[7], map_bwd[7];        // conv inputs (box 128 + 2d)
+    CUtensorMap map_fwd_out[7], map_bwd_out[7];  // conv outputs (32-pixel tiles)
 
     int init(int batch, int width, int height, const int *dilations, bool train);
     void release();
