@@ -92,11 +92,11 @@ __device__ __forceinline__ int2 probe_site(const ProbeArgs &a, int t)
     return make_int2(y0 + (int)(h1 % (uint32_t)max(1, th - a.P + 1)), x0 + (int)(h2 % (uint32_t)max(1, tw - a.P + 1)));
 }
 
-// Row pass, one CTA per (tile, wx): R = the rows py-2S .. py-2S+RYP-1,
-// demodulated by e^{-j wx x} and filtered along x, for the columns
-// px-S .. px-S+RXP-1 (zero outside the image and beyond RX).  A thread takes
-// 16 adjacent output columns of one row from 16+2S staged inputs, summing
-// the taps in ascending order for each output.
+// Row pass, one CTA per (tile, wx, chunk of 64 rows): R = the rows
+// py-2S .. py-2S+RYP-1, demodulated by e^{-j wx x} and filtered along x, for
+// the columns px-S .. px-S+RXP-1 (zero outside the image and beyond RX).  A
+// thread takes 16 adjacent output columns of one row from 16+2S staged
+// inputs, summing the taps in ascending order for each output.
 template <int S>
 __global__ void __launch_bounds__(ProbeGeom<S>::RTHREADS) wff_probe_rows_kernel(ProbeArgs a, PTaps<float, S> gxr)
 {
@@ -112,8 +112,9 @@ __global__ void __launch_bounds__(ProbeGeom<S>::RTHREADS) wff_probe_rows_kernel(
     const float2 *exi = a.ex + (size_t)i * (a.pitch + 2 * kPhasorPad) + kPhasorPad;
     float2 *Rg = a.rows + ((size_t)t * gridDim.y + i) * G::R_ELEMS;
     for (int e = tid; e < FX; e += G::RTHREADS) es[e] = exi[px - 2 * S + e];
-    for (int r0 = 0; r0 < RYP; r0 += CR) {
-        __syncthreads();  // es is written; the previous chunk has been consumed
+    {
+        const int r0 = blockIdx.z * CR;
+        __syncthreads();  // es is written
         for (int e = tid; e < CR * FX; e += G::RTHREADS) {
             const int rr = e / FX, c = e - rr * FX;
             const int y = py - 2 * S + r0 + rr, x = px - 2 * S + c;
@@ -274,6 +275,8 @@ __global__ void __launch_bounds__(64) wff_probe_resid_kernel(const float2 *__res
     int cnt = 0;
     if (e < P * P) {
         float2 v = make_float2(0.f, 0.f);
+        // fixed summation order; unrolled so that several loads are in flight
+#pragma unroll 12
         for (int i = 0; i < nparts; i++) {
             const float2 q = partial[((size_t)t * nparts + i) * P * P + e];
             v.x += q.x;
@@ -354,7 +357,8 @@ static int launch_probe(const WffPlan &Pl, ProbeArgs a, cudaStream_t s, const Pr
             a.nsplit = ns;
         }
     }
-    wff_probe_rows_kernel<S><<<dim3(ntiles, Pl.nfx), G::RTHREADS, G::RSMEM, s>>>(a, probe_taps<S>(Pl.gx, Pl.sx, 1.0));
+    wff_probe_rows_kernel<S><<<dim3(ntiles, Pl.nfx, (G::RYP + G::CR - 1) / G::CR), G::RTHREADS, G::RSMEM, s>>>(
+        a, probe_taps<S>(Pl.gx, Pl.sx, 1.0));
     wff_probe_kernel<S><<<dim3(ntiles, Pl.nfx, a.nsplit), G::THREADS, G::SMEM, s>>>(
         a, probe_taps<S>(Pl.gy, Pl.sy, Pl.inv_norm), probe_taps<S>(Pl.gy, Pl.sy, 1.0),
         probe_taps<S>(Pl.gx, Pl.sx, Pl.scale * Pl.inv_norm));
