@@ -62,6 +62,14 @@ struct glsu_wff {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
+struct glsu_wfr {
+    WffPlan plan;
+    WfrBuffers buf;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
 struct glsu_dpra {
     int prec = GLSU_F32;
     int W = 0, H = 0, rr = 1, r = 1;
@@ -253,6 +261,90 @@ extern "C" int glsu_wff_run_async(glsu_wff *h, const void *d_f, void *d_filtered
 {
     if (!h || !d_f || !d_filtered) return fail(GLSU_ERR_INVALID, "null argument");
     return h->plan.enqueue(h->stream, d_f, d_filtered, 0, nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+
+// ===========================================================================
+// WFR2
+// ===========================================================================
+extern "C" int glsu_wfr_create(glsu_wfr **out, int precision, int width, int height, const glsu_wff_params *p)
+{
+    if (!out) return fail(GLSU_ERR_INVALID, "null handle pointer");
+    *out = nullptr;
+    glsu_wff_params prm;
+    if (p) prm = *p;
+    else glsu_wft_default_params(GLSU_WFT_WFR, &prm);
+    prm.thr = 0;  // not used by WFR2
+    glsu_wfr *h = new glsu_wfr();
+    int rc = h->plan.init(precision, width, height, prm);
+    if (rc == GLSU_OK) rc = wff_setup_stream(&h->stream, &h->own_stream);
+    if (rc == GLSU_OK) rc = h->plan.alloc_device();
+    if (rc == GLSU_OK) rc = h->plan.upload_tables(h->stream);
+    if (rc == GLSU_OK) rc = h->plan.make_tensor_map();
+    if (rc == GLSU_OK) rc = h->buf.alloc(h->plan);
+    if (rc == GLSU_OK && (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess))
+        rc = fail(GLSU_ERR_CUDA, "cudaEventCreate failed");
+    if (rc != GLSU_OK) {
+        glsu_wfr_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_wfr_destroy(glsu_wfr *h)
+{
+    if (!h) return GLSU_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    h->buf.release();
+    h->plan.release();
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_wfr_set_stream(glsu_wfr *h, void *stream)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    if (h->own_stream && h->stream) {
+        cudaStreamSynchronize(h->stream);
+        cudaStreamDestroy(h->stream);
+    }
+    h->stream = (cudaStream_t)stream;
+    h->own_stream = false;
+    return GLSU_OK;
+}
+
+static int wfr_check_results(const glsu_wfr_results *z)
+{
+    if (!z || !z->wx || !z->wy || !z->phase || !z->phase_comp || !z->b || !z->r || !z->cxx || !z->cyy)
+        return fail(GLSU_ERR_INVALID, "null WFR result map");
+    return GLSU_OK;
+}
+
+extern "C" int glsu_wfr_run_async(glsu_wfr *h, const void *d_f, const glsu_wfr_results *z)
+{
+    if (!h || !d_f) return fail(GLSU_ERR_INVALID, "null argument");
+    GLSU_TRY(wfr_check_results(z));
+    return enqueue_wfr(h->plan, h->buf, h->stream, d_f, *z);
+}
+
+extern "C" int glsu_wfr_run(glsu_wfr *h, const void *d_f, const glsu_wfr_results *z, double *time_ms)
+{
+    if (!h || !d_f) return fail(GLSU_ERR_INVALID, "null argument");
+    GLSU_TRY(wfr_check_results(z));
+    GLSU_CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+    GLSU_TRY(enqueue_wfr(h->plan, h->buf, h->stream, d_f, *z));
+    GLSU_CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
+    GLSU_CUDA_TRY(cudaEventSynchronize(h->ev1));
+    GLSU_TRY(h->plan.check_device_error(h->stream));
+    if (time_ms) {
+        float ms = 0;
+        GLSU_CUDA_TRY(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+        *time_ms = ms;
+    }
+    return GLSU_OK;
 }
 
 extern "C" int glsu_wff_run(glsu_wff *h, const void *d_f, void *d_filtered, double *time_ms)

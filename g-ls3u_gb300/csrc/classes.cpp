@@ -75,33 +75,67 @@ cv::Mat cv::imread(const std::string &path)
 namespace WFT_FPA {
 namespace WFT {
 
-WFT2_DeviceResultsF::~WFT2_DeviceResultsF()
+template <typename Z> static void free_results(Z &z)
 {
-    if (m_d_filtered) cudaFree(m_d_filtered);
-    m_d_filtered = nullptr;
+    void *ps[] = {z.m_d_filtered, z.m_d_wx, z.m_d_wy, z.m_d_phase, z.m_d_phase_comp,
+                  z.m_d_b,        z.m_d_r,  z.m_d_cxx, z.m_d_cyy};
+    for (void *p : ps)
+        if (p) cudaFree(p);
+    z.m_d_filtered = nullptr;
+    z.m_d_wx = z.m_d_wy = z.m_d_phase = z.m_d_phase_comp = z.m_d_b = z.m_d_r = z.m_d_cxx = z.m_d_cyy = nullptr;
 }
 
-WFT2_DeviceResults::~WFT2_DeviceResults()
+WFT2_DeviceResultsF::~WFT2_DeviceResultsF() { free_results(*this); }
+WFT2_DeviceResults::~WFT2_DeviceResults() { free_results(*this); }
+
+// Allocates the results of the WFT type: the filtered field for WFF, the
+// eight ridge maps for WFR (element type E).
+template <typename Z, typename C, typename E> static bool alloc_results(Z &z, WFT_TYPE type, size_t n)
 {
-    if (m_d_filtered) cudaFree(m_d_filtered);
-    m_d_filtered = nullptr;
+    if (type == WFT_TYPE::WFF) return cudaMalloc((void **)&z.m_d_filtered, sizeof(C) * n) == cudaSuccess;
+    E **maps[] = {&z.m_d_wx, &z.m_d_wy, &z.m_d_phase, &z.m_d_phase_comp, &z.m_d_b, &z.m_d_r, &z.m_d_cxx, &z.m_d_cyy};
+    for (E **m : maps)
+        if (cudaMalloc((void **)m, sizeof(E) * n) != cudaSuccess) return false;
+    return true;
 }
 
-static glsu_wff *make_wff(int prec, int w, int h, WFT_TYPE type, const glsu_wff_params *p)
+template <typename Z> static glsu_wfr_results wfr_maps(Z &z)
 {
-    if (type != WFT_TYPE::WFF) throw std::runtime_error("WFT_TYPE::WFR is not implemented on this path");
-    glsu_wff *hd = nullptr;
-    throw_if(glsu_wff_create(&hd, prec, w, h, p), "WFT2 construction failed");
-    return hd;
+    glsu_wfr_results r;
+    r.wx = z.m_d_wx;
+    r.wy = z.m_d_wy;
+    r.phase = z.m_d_phase;
+    r.phase_comp = z.m_d_phase_comp;
+    r.b = z.m_d_b;
+    r.r = z.m_d_r;
+    r.cxx = z.m_d_cxx;
+    r.cyy = z.m_d_cyy;
+    return r;
+}
+
+// Creates the handle of the WFT type (the other stays null).
+static void make_wft(int prec, int w, int h, WFT_TYPE type, const glsu_wff_params *p, glsu_wff **hf,
+                     glsu_wfr **hr)
+{
+    if (type == WFT_TYPE::WFF) throw_if(glsu_wff_create(hf, prec, w, h, p), "WFT2 construction failed");
+    else throw_if(glsu_wfr_create(hr, prec, w, h, p), "WFT2 (WFR) construction failed");
+}
+
+static void destroy_wft(glsu_wff *hf, glsu_wfr *hr)
+{
+    glsu_wff_destroy(hf);
+    glsu_wfr_destroy(hr);
 }
 
 WFT2_CUDAF::WFT2_CUDAF(int iWidth, int iHeight, WFT_TYPE type, WFT2_DeviceResultsF &z, int)
     : w_(iWidth), hgt_(iHeight)
 {
-    h_ = make_wff(GLSU_F32, iWidth, iHeight, type, nullptr);
-    if (cudaMalloc((void **)&z.m_d_filtered, sizeof(cuFloatComplex) * (size_t)iWidth * iHeight) != cudaSuccess) {
-        glsu_wff_destroy(h_);
-        throw std::runtime_error("cudaMalloc of the filtered result failed");
+    glsu_wff_params p;
+    glsu_wft_default_params(type == WFT_TYPE::WFF ? GLSU_WFT_WFF : GLSU_WFT_WFR, &p);
+    make_wft(GLSU_F32, iWidth, iHeight, type, &p, &h_, &hr_);
+    if (!alloc_results<WFT2_DeviceResultsF, cuFloatComplex, float>(z, type, (size_t)iWidth * iHeight)) {
+        destroy_wft(h_, hr_);
+        throw std::runtime_error("cudaMalloc of the WFT2 results failed");
     }
 }
 
@@ -110,27 +144,34 @@ WFT2_CUDAF::WFT2_CUDAF(int iWidth, int iHeight, WFT_TYPE type, float rSigmaX, fl
     : w_(iWidth), hgt_(iHeight)
 {
     glsu_wff_params p = make_params(rSigmaX, rWxl, rWxh, rWxi, rSigmaY, rWyl, rWyh, rWyi, rThr);
-    h_ = make_wff(GLSU_F32, iWidth, iHeight, type, &p);
-    if (cudaMalloc((void **)&z.m_d_filtered, sizeof(cuFloatComplex) * (size_t)iWidth * iHeight) != cudaSuccess) {
-        glsu_wff_destroy(h_);
-        throw std::runtime_error("cudaMalloc of the filtered result failed");
+    make_wft(GLSU_F32, iWidth, iHeight, type, &p, &h_, &hr_);
+    if (!alloc_results<WFT2_DeviceResultsF, cuFloatComplex, float>(z, type, (size_t)iWidth * iHeight)) {
+        destroy_wft(h_, hr_);
+        throw std::runtime_error("cudaMalloc of the WFT2 results failed");
     }
 }
 
-WFT2_CUDAF::~WFT2_CUDAF() { glsu_wff_destroy(h_); }
+WFT2_CUDAF::~WFT2_CUDAF() { destroy_wft(h_, hr_); }
 
 void WFT2_CUDAF::operator()(cuFloatComplex *d_f, WFT2_DeviceResultsF &d_z, double &time)
 {
-    throw_if(glsu_wff_run(h_, d_f, d_z.m_d_filtered, &time), "WFF2 failed");
+    if (h_) {
+        throw_if(glsu_wff_run(h_, d_f, d_z.m_d_filtered, &time), "WFF2 failed");
+    } else {
+        const glsu_wfr_results z = wfr_maps(d_z);
+        throw_if(glsu_wfr_run(hr_, d_f, &z, &time), "WFR2 failed");
+    }
 }
 
 WFT2_CUDA::WFT2_CUDA(int iWidth, int iHeight, WFT_TYPE type, WFT2_DeviceResults &z, int)
     : w_(iWidth), hgt_(iHeight)
 {
-    h_ = make_wff(GLSU_F64, iWidth, iHeight, type, nullptr);
-    if (cudaMalloc((void **)&z.m_d_filtered, sizeof(cuDoubleComplex) * (size_t)iWidth * iHeight) != cudaSuccess) {
-        glsu_wff_destroy(h_);
-        throw std::runtime_error("cudaMalloc of the filtered result failed");
+    glsu_wff_params p;
+    glsu_wft_default_params(type == WFT_TYPE::WFF ? GLSU_WFT_WFF : GLSU_WFT_WFR, &p);
+    make_wft(GLSU_F64, iWidth, iHeight, type, &p, &h_, &hr_);
+    if (!alloc_results<WFT2_DeviceResults, cuDoubleComplex, double>(z, type, (size_t)iWidth * iHeight)) {
+        destroy_wft(h_, hr_);
+        throw std::runtime_error("cudaMalloc of the WFT2 results failed");
     }
 }
 
@@ -139,18 +180,23 @@ WFT2_CUDA::WFT2_CUDA(int iWidth, int iHeight, WFT_TYPE type, double rSigmaX, dou
     : w_(iWidth), hgt_(iHeight)
 {
     glsu_wff_params p = make_params(rSigmaX, rWxl, rWxh, rWxi, rSigmaY, rWyl, rWyh, rWyi, rThr);
-    h_ = make_wff(GLSU_F64, iWidth, iHeight, type, &p);
-    if (cudaMalloc((void **)&z.m_d_filtered, sizeof(cuDoubleComplex) * (size_t)iWidth * iHeight) != cudaSuccess) {
-        glsu_wff_destroy(h_);
-        throw std::runtime_error("cudaMalloc of the filtered result failed");
+    make_wft(GLSU_F64, iWidth, iHeight, type, &p, &h_, &hr_);
+    if (!alloc_results<WFT2_DeviceResults, cuDoubleComplex, double>(z, type, (size_t)iWidth * iHeight)) {
+        destroy_wft(h_, hr_);
+        throw std::runtime_error("cudaMalloc of the WFT2 results failed");
     }
 }
 
-WFT2_CUDA::~WFT2_CUDA() { glsu_wff_destroy(h_); }
+WFT2_CUDA::~WFT2_CUDA() { destroy_wft(h_, hr_); }
 
 void WFT2_CUDA::operator()(cuDoubleComplex *d_f, WFT2_DeviceResults &d_z, double &time)
 {
-    throw_if(glsu_wff_run(h_, d_f, d_z.m_d_filtered, &time), "WFF2 failed");
+    if (h_) {
+        throw_if(glsu_wff_run(h_, d_f, d_z.m_d_filtered, &time), "WFF2 failed");
+    } else {
+        const glsu_wfr_results z = wfr_maps(d_z);
+        throw_if(glsu_wfr_run(hr_, d_f, &z, &time), "WFR2 failed");
+    }
 }
 
 }  // namespace WFT

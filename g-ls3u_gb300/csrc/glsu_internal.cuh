@@ -130,6 +130,8 @@ struct WffPlan {
     // instead (phi_ref, dphi_ref -> phi_curr, dphi).
     int enqueue(cudaStream_t s, const void *d_f, void *d_out, int final_mode, const void *phi_ref,
                 const void *dphi_ref, void *phi_curr, void *dphi, cudaEvent_t *stage_ev);
+    // Only the row pass of d_f into the R planes (whole frame, no tile mask).
+    int enqueue_rows(cudaStream_t s, const void *d_f);
     int check_device_error(cudaStream_t s);
 
     // Tile mask of the next enqueue (flags == nullptr: whole frame), and the
@@ -204,6 +206,20 @@ struct SurL7W {
 };
 int sur_make_map(CUtensorMap *tm, const void *act, int B, int H, int W, int dil);
 int sur_make_out_map(CUtensorMap *tm, const void *act, int B, int H, int W);
+
+// ---------------------------------------------------------------------------
+// WFR2 (wfr_kernels.cu): per-wx partial arg-max planes and curvature scratch
+// ---------------------------------------------------------------------------
+struct WfrBuffers {
+    void *pabs = nullptr;  // [nfx][H][W] T: best |sf| over wy
+    int *pk = nullptr;     // [nfx][H][W]: its wy index
+    void *pph = nullptr;   // [nfx][H][W] T: its angle(sf)
+    void *A = nullptr, *B = nullptr;  // H x W T: row pass of the curvature convolutions
+    int alloc(const WffPlan &P);
+    void release();
+};
+// Enqueue one WFR2 of d_f (H x W complex) into the eight result maps.
+int enqueue_wfr(WffPlan &P, const WfrBuffers &wb, cudaStream_t s, const void *d_f, const glsu_wfr_results &z);
 int launch_sur_conv(const CUtensorMap &tm, const CUtensorMap &tmo, const SurConvArgs &a, cudaStream_t s);
 
 // AIA

@@ -32,39 +32,10 @@
 #include <vector>
 
 #include "glsu_internal.cuh"
+#include "wff_common.cuh"
 #include "ptx_sm103.cuh"
 
 namespace glsu {
-
-// ---------------------------------------------------------------------------
-// small device helpers
-// ---------------------------------------------------------------------------
-template <typename T, int S> struct Taps {
-    T g[2 * S + 1];
-};
-
-template <typename T> __device__ __forceinline__ C2<T> mk(T x, T y)
-{
-    C2<T> r;
-    r.x = x;
-    r.y = y;
-    return r;
-}
-
-// acc += g * v for a real tap g and a complex v: two scalar FMAs, whose tap
-// operand comes straight from the kernel-parameter bank.  (The packed
-// __ffma2_rn needs {g, g} in a register pair; with 2S+1 = 61 taps that cost a
-// move per FMA and made the 1024^2 column sweep 2.9x slower, 16.2 vs 5.5 ms.)
-__device__ __forceinline__ void cfma(float2 &acc, float g, float2 v)
-{
-    acc.x = fmaf(g, v.x, acc.x);
-    acc.y = fmaf(g, v.y, acc.y);
-}
-__device__ __forceinline__ void cfma(double2 &acc, double g, double2 v)
-{
-    acc.x = fma(g, v.x, acc.x);
-    acc.y = fma(g, v.y, acc.y);
-}
 
 // ---------------------------------------------------------------------------
 // geometry
@@ -727,16 +698,6 @@ static TileMask with_margins(TileMask m, int my, int mx)
     return m;
 }
 
-template <typename T, int S> static Taps<T, S> make_taps(const double *g, int strue, double mul)
-{
-    Taps<T, S> t;
-    for (int m = 0; m <= 2 * S; m++) {
-        const int k = m - S;  // offset
-        t.g[m] = (k >= -strue && k <= strue) ? (T)(g[k + strue] * mul) : (T)0;
-    }
-    return t;
-}
-
 template <typename T, int S>
 static int launch_rows_demod(const WffPlan &P, const void *d_f, cudaStream_t s)
 {
@@ -753,6 +714,21 @@ static int launch_rows_demod(const WffPlan &P, const void *d_f, cudaStream_t s)
         make_taps<T, S>(P.gx, P.sx, 1.0), with_margins(P.mask, 2 * P.sy, P.sx));
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
+}
+
+int WffPlan::enqueue_rows(cudaStream_t s, const void *d_f)
+{
+    if (mask.flags) return fail(GLSU_ERR_INVALID, "full-frame row pass with a tile mask set");
+#define GLSU_ROWS(SS) \
+    return prec == GLSU_F32 ? launch_rows_demod<float, SS>(*this, d_f, s) : launch_rows_demod<double, SS>(*this, d_f, s);
+    switch (sxi) {
+    case 12: GLSU_ROWS(12)
+    case 20: GLSU_ROWS(20)
+    case 30: GLSU_ROWS(30)
+    case 45: GLSU_ROWS(45)
+    default: GLSU_ROWS(60)
+    }
+#undef GLSU_ROWS
 }
 
 template <typename T, int S> static int launch_cols(const WffPlan &P, cudaStream_t s)

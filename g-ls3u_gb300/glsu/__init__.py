@@ -49,6 +49,14 @@ class GlsuError(RuntimeError):
         self.code = code
 
 
+WFR_FIELDS = ("wx", "wy", "phase", "phase_comp", "b", "r", "cxx", "cyy")
+
+
+class WfrResultsC(ctypes.Structure):
+    """glsu_wfr_results: device addresses of the eight H*W WFR2 result maps."""
+    _fields_ = [(n, ctypes.c_void_p) for n in WFR_FIELDS]
+
+
 class WffParamsC(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in
                 ("sigma_x", "wxl", "wxh", "wxi", "sigma_y", "wyl", "wyh", "wyi", "thr")]
@@ -104,6 +112,11 @@ def lib() -> ctypes.CDLL:
             "glsu_wff_count": ([c_double, c_double, c_double, c_int], c_int),
             "glsu_aia_random_deltas": ([c_int, ctypes.c_uint64, fltp], c_int),
             "glsu_wff_create": ([pp, c_int, c_int, c_int, prm], c_int),
+            "glsu_wfr_create": ([pp, c_int, c_int, c_int, prm], c_int),
+            "glsu_wfr_destroy": ([c_void_p], c_int),
+            "glsu_wfr_set_stream": ([c_void_p, c_void_p], c_int),
+            "glsu_wfr_run": ([c_void_p, c_void_p, ctypes.POINTER(WfrResultsC), dblp], c_int),
+            "glsu_wfr_run_async": ([c_void_p, c_void_p, ctypes.POINTER(WfrResultsC)], c_int),
             "glsu_wff_destroy": ([c_void_p], c_int),
             "glsu_wff_set_stream": ([c_void_p, c_void_p], c_int),
             "glsu_wff_run": ([c_void_p, c_void_p, c_void_p, dblp], c_int),
@@ -223,6 +236,46 @@ def _img_type(a: np.ndarray) -> int:
     raise TypeError("frames must be uint8, float32 or float64")
 
 
+class WFR2:
+    """Windowed Fourier ridges (WFT2_CUDAF / WFT2_CUDA with WFT_TYPE::WFR).
+
+    ``run(d_f, maps)`` takes the device address of the H*W complex input
+    (complex64 for f32, complex128 for f64) and a dict of the device
+    addresses of the eight H*W real result maps (float32 / float64) named as
+    in ``WFR_FIELDS``: wx, wy, phase, phase_comp, b, r, cxx, cyy."""
+
+    def __init__(self, width: int, height: int, precision="f32", params: WffParams | None = None):
+        self.width, self.height, self.precision = width, height, _prec(precision)
+        h = ctypes.c_void_p()
+        pc = ctypes.byref(params.c()) if params is not None else None
+        check(lib().glsu_wfr_create(ctypes.byref(h), self.precision, width, height, pc))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().glsu_wfr_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def set_stream(self, stream_ptr: int):
+        check(lib().glsu_wfr_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
+
+    @staticmethod
+    def _maps(maps) -> WfrResultsC:
+        return WfrResultsC(*[ctypes.c_void_p(int(maps[k])) for k in WFR_FIELDS])
+
+    def run(self, d_f: int, maps) -> float:
+        t = ctypes.c_double(0)
+        z = self._maps(maps)
+        check(lib().glsu_wfr_run(self._h, ctypes.c_void_p(d_f), ctypes.byref(z), ctypes.byref(t)))
+        return t.value
+
+    def run_async(self, d_f: int, maps):
+        z = self._maps(maps)
+        check(lib().glsu_wfr_run_async(self._h, ctypes.c_void_p(d_f), ctypes.byref(z)))
+
+
 class WFF2:
     """Windowed Fourier filtering (WFT2_CUDAF / WFT2_CUDA with WFT_TYPE::WFF).
 
@@ -232,7 +285,7 @@ class WFF2:
     def __init__(self, width: int, height: int, precision="f32", params: WffParams | None = None,
                  wft_type: int = WFT_WFF):
         if wft_type != WFT_WFF:
-            raise GlsuError(ERR_UNSUPPORTED, "only WFT_TYPE::WFF is implemented")
+            raise GlsuError(ERR_UNSUPPORTED, "WFT_TYPE::WFR is the WFR2 class")
         self.width, self.height, self.precision = width, height, _prec(precision)
         h = ctypes.c_void_p()
         pc = ctypes.byref(params.c()) if params is not None else None

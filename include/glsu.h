@@ -9,6 +9,7 @@
  *
  * Reference interfaces replaced (paths inside the reference project):
  *   glsu_wff_*   WFT_FPA::WFT::WFT2_CUDAF / WFT2_CUDA with WFT_TYPE::WFF
+ *   glsu_wfr_*   WFT_FPA::WFT::WFT2_CUDAF / WFT2_CUDA with WFT_TYPE::WFR
  *                (WFT/WFT2_CUDAf.h:11-40, WFT/WFT2_CUDA.h), whose CPU twin is
  *                WFT/WFT2_CPU.cpp:190-390
  *   glsu_dpra_*  DPRA::DPRA_CUDAF (DPRA/dpra_cudaf.h:21-46) and the empty
@@ -34,7 +35,7 @@ extern "C" {
 #define GLSU_ERR_PADDING (-2)     /* padded size beyond 4096 (reference: throw -1) */
 #define GLSU_ERR_CUDA (-3)        /* a CUDA runtime call failed                */
 #define GLSU_ERR_ALLOC (-4)       /* device or pinned allocation failed        */
-#define GLSU_ERR_UNSUPPORTED (-5) /* e.g. WFT_TYPE::WFR, window beyond limits  */
+#define GLSU_ERR_UNSUPPORTED (-5) /* e.g. a window beyond the limits        */
 #define GLSU_ERR_NOT_POSDEF (-6)  /* AIA normal matrix not positive definite   */
 #define GLSU_ERR_TIMEOUT (-7)     /* a bounded device-side wait gave up        */
 #define GLSU_ERR_NO_DEVICE (-8)   /* no CUDA device visible                    */
@@ -146,6 +147,37 @@ int glsu_wff_padded_size(const glsu_wff *h, int *padded_width, int *padded_heigh
  * recomputed on every call, since nothing is kept between calls. */
 int glsu_wff_run_noalloc(int width, int height, const glsu_wff_params *p, const void *d_f, void *d_filtered,
                          void *cuda_stream);
+
+/* ---- WFR2: WFT2_CUDAF / WFT2_CUDA with WFT_TYPE::WFR -------------------- */
+/* WFT/WFT2_CUDAf.h:21-40 (cuWFR2, WFT/WFT2_CUDAf.cu:1174-1319), computed in
+ * the formulation of the CPU reference WFT2_cpu::WFR2 (WFT/WFT2_CPU.cpp:
+ * 391-694): per pixel the frequency of the largest windowed Fourier
+ * coefficient |sf| over the (wx, wy) grid (ties: the later one in wy-major,
+ * wx-minor order), its phase, and the curvature least squares.  The eight
+ * maps are the WFR fields of WFT2_DeviceResults[F] (WFT/WFT.h:99-135):
+ * device arrays of H*W elements of the handle's precision (float or double). */
+typedef struct glsu_wfr_results {
+    void *wx;          /* local frequency in x of the ridge */
+    void *wy;          /* local frequency in y */
+    void *phase;       /* angle(sf) at the ridge */
+    void *phase_comp;  /* phase compensated by the curvature estimate */
+    void *b;           /* amplitude */
+    void *r;           /* ridge value max |sf| */
+    void *cxx;         /* curvature estimate in x */
+    void *cyy;         /* curvature estimate in y */
+} glsu_wfr_results;
+
+typedef struct glsu_wfr glsu_wfr;
+/* p: sigma, frequency grid (thr is not used); NULL selects the WFR defaults
+ * of glsu_wft_default_params(GLSU_WFT_WFR). */
+int glsu_wfr_create(glsu_wfr **out, int precision, int width, int height, const glsu_wff_params *p);
+int glsu_wfr_destroy(glsu_wfr *h);
+int glsu_wfr_set_stream(glsu_wfr *h, void *cuda_stream);
+/* WFT2_CUDAF::operator() for WFR: d_f device H*W complex input; the eight
+ * device maps of z receive the results; time_ms (may be NULL) the device time. */
+int glsu_wfr_run(glsu_wfr *h, const void *d_f, const glsu_wfr_results *z, double *time_ms);
+/* Same, enqueued on the handle's stream without waiting. */
+int glsu_wfr_run_async(glsu_wfr *h, const void *d_f, const glsu_wfr_results *z);
 
 /* ---- DPRA: DPRA_CUDAF (F32) / DPRA_CUDA (F64) --------------------------- */
 /* h_phi0: HOST pointer to W*H initial phase in the handle's precision

@@ -2,7 +2,7 @@
 //
 // Drop-in replacements (paths inside the reference project):
 //   WFT_FPA::WFT::WFT2_CUDAF / WFT2_CUDA      WFT/WFT2_CUDAf.h:11-40, WFT/WFT2_CUDA.h:11-40
-//   WFT_FPA::WFT::WFT2_DeviceResults[F]        WFT/WFT.h:92-135 (owns m_d_filtered)
+//   WFT_FPA::WFT::WFT2_DeviceResults[F]        WFT/WFT.h:92-135 (owns m_d_filtered and the WFR maps)
 //   DPRA::DPRA_CUDAF                            DPRA/dpra_cudaf.h:21-46
 //   DPRA::DPRA_CUDA  (empty in the reference)   DPRA/dpra_cuda.h:9-14; interface of DPRA_CPU, dpra_cpu.h:30-64
 //   AIA::AIA_CUDAF                              AIA/aia_cudaf.h:15-38
@@ -13,7 +13,8 @@
 //     throws int -1); the C ABI underneath returns status codes;
 //   - the per-parameter WFT2 constructor sets the y lower bound from wyl (the
 //     reference assigns m_rWyl(rWxl), WFT/WFT2_CUDAf.cu:903);
-//   - WFT_TYPE::WFR is rejected (only WFF is on this path);
+//   - WFT_TYPE::WFR follows the CPU reference's formulation (truncated
+//     window, WFT/WFT2_CPU.cpp:391-694), as WFF does;
 //   - DPRA_CUDAF's batch operator() overloads, empty in the reference
 //     (DPRA/dpra_cudaf.cu:193-205), run the DPRA_CPU::operator() loop;
 //   - times are in milliseconds everywhere.
@@ -78,8 +79,18 @@ namespace WFT {
 
 enum class WFT_TYPE { WFF, WFR };
 
+// H*W device arrays allocated by the WFT2 constructor: m_d_filtered for
+// WFT_TYPE::WFF, the eight ridge maps for WFT_TYPE::WFR.
 struct WFT2_DeviceResultsF {
-    cuFloatComplex *m_d_filtered = nullptr;  // H*W, allocated by the WFT2_CUDAF constructor
+    cuFloatComplex *m_d_filtered = nullptr;
+    float *m_d_wx = nullptr;          // local frequency in x
+    float *m_d_wy = nullptr;          // local frequency in y
+    float *m_d_phase = nullptr;       // phase
+    float *m_d_phase_comp = nullptr;  // compensated by the estimation of c
+    float *m_d_b = nullptr;           // amplitude
+    float *m_d_r = nullptr;           // ridge value
+    float *m_d_cxx = nullptr;         // estimation of c in x
+    float *m_d_cyy = nullptr;         // estimation of c in y
     WFT2_DeviceResultsF() = default;
     WFT2_DeviceResultsF(const WFT2_DeviceResultsF &) = delete;
     ~WFT2_DeviceResultsF();
@@ -87,6 +98,8 @@ struct WFT2_DeviceResultsF {
 
 struct WFT2_DeviceResults {
     cuDoubleComplex *m_d_filtered = nullptr;
+    double *m_d_wx = nullptr, *m_d_wy = nullptr, *m_d_phase = nullptr, *m_d_phase_comp = nullptr;
+    double *m_d_b = nullptr, *m_d_r = nullptr, *m_d_cxx = nullptr, *m_d_cyy = nullptr;
     WFT2_DeviceResults() = default;
     WFT2_DeviceResults(const WFT2_DeviceResults &) = delete;
     ~WFT2_DeviceResults();
@@ -103,12 +116,15 @@ class WFT2_CUDAF {
                float rSigmaY, float rWyl, float rWyh, float rWyi, float rThr, WFT2_DeviceResultsF &z,
                int iNumStreams = 1);
     ~WFT2_CUDAF();
-    // d_f: device W*H input; d_z.m_d_filtered receives the result; time in ms
+    // d_f: device W*H input; d_z.m_d_filtered (WFF) or the ridge maps (WFR)
+    // receive the result; time in ms
     void operator()(cuFloatComplex *d_f, WFT2_DeviceResultsF &d_z, double &time);
     glsu_wff *handle() const { return h_; }
+    glsu_wfr *wfr_handle() const { return hr_; }
 
   private:
     glsu_wff *h_ = nullptr;
+    glsu_wfr *hr_ = nullptr;
     int w_, hgt_;
 };
 
@@ -124,9 +140,11 @@ class WFT2_CUDA {
     ~WFT2_CUDA();
     void operator()(cuDoubleComplex *d_f, WFT2_DeviceResults &d_z, double &time);
     glsu_wff *handle() const { return h_; }
+    glsu_wfr *wfr_handle() const { return hr_; }
 
   private:
     glsu_wff *h_ = nullptr;
+    glsu_wfr *hr_ = nullptr;
     int w_, hgt_;
 };
 

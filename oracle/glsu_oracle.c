@@ -444,6 +444,178 @@ int or_wff2(int W, int H, const double *f, double sigx, double wxl, double wxh, 
     return 0;
 }
 
+/*
+ * WFR2, windowed Fourier ridges (WFT/WFT2_CPU.cpp:391-694, WFR2_Init
+ * :846-956): for every frequency of the grid, sf = f conv (g e^{j(wx x + wy y)})
+ * by FFT as in or_wff2; per pixel the largest |sf| (ties: the later
+ * frequency in wy-major, wx-minor order, as the single-thread loop with
+ * `>=` at :505-518), its wx, wy and angle; then the curvature least squares
+ * cxx = -conv2(wx, x.*g, 'same') / sum(x.*x.*g) with the map replicated
+ * beyond the border (:551-631, :636-671), cyy alike, the compensated phase
+ * and the amplitude (:674-692).
+ * out: 8 arrays of H*W doubles: wx, wy, phase, phase_comp, b, r, cxx, cyy.
+ * Returns 0, or -1 when the padded size leaves the LUT.
+ */
+int or_wfr2(int W, int H, const double *f, double sigx, double wxl, double wxh, double wxi, double sigy,
+            double wyl, double wyh, double wyi, double *wx, double *wy, double *phase, double *phase_comp,
+            double *b, double *r, double *cxx, double *cyy, int nthreads)
+{
+    const int sx = (int)round(3 * sigx), sy = (int)round(3 * sigy);
+    const int winW = 2 * sx + 1, winH = 2 * sy + 1;
+    const int iH = or_first_greater(H + winH - 1), iW = or_first_greater(W + winW - 1);
+    if (iH < 0 || iW < 0) return -1;
+    const int Hp = g_lut[iH], Wp = g_lut[iW];
+    const size_t P = (size_t)Hp * Wp;
+    const size_t N = (size_t)H * W;
+
+    double *g = (double *)calloc((size_t)winH * winW, sizeof(double));
+    double *Ff = (double *)calloc(2 * P, sizeof(double));
+    if (!g || !Ff) return -2;
+    double nrm = 0;
+    for (int i = 0; i < winH; i++)
+        for (int j = 0; j < winW; j++) {
+            double y = (double)(i - (winH - 1) / 2), x = (double)(j - (winW - 1) / 2);
+            double v = exp(-(x * x) / 2 / sigx / sigx - (y * y) / 2 / sigy / sigy);
+            g[(size_t)i * winW + j] = v;
+            nrm += v * v;
+        }
+    nrm = sqrt(nrm);
+    for (size_t k = 0; k < (size_t)winH * winW; k++) g[k] *= 1 / nrm;
+    for (int i = 0; i < H; i++)
+        for (int j = 0; j < W; j++) {
+            Ff[2 * ((size_t)i * Wp + j)] = f[2 * ((size_t)i * W + j)];
+            Ff[2 * ((size_t)i * Wp + j) + 1] = f[2 * ((size_t)i * W + j) + 1];
+        }
+    {
+        fft2_plan p;
+        if (fft2_init(&p, Wp, Hp)) return -2;
+        fft2_exec(&p, Ff, 0);
+        fft2_free(&p);
+    }
+    const int iwx = or_wff_count(wxl, wxh, wxi), iwy = or_wff_count(wyl, wyh, wyi);
+    /* per frequency row: best |sf|, its wx index and angle (ties: later wx) */
+    double *pr = (double *)malloc(sizeof(double) * N * (size_t)iwy);
+    double *pp = (double *)malloc(sizeof(double) * N * (size_t)iwy);
+    int *px = (int *)malloc(sizeof(int) * N * (size_t)iwy);
+    if (!pr || !pp || !px) return -2;
+    const double invP = 1.0 / (double)P;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel
+#endif
+    {
+        double *Fg = (double *)malloc(sizeof(double) * 2 * P);
+        double *Sf = (double *)malloc(sizeof(double) * 2 * P);
+        fft2_plan p;
+        fft2_init(&p, Wp, Hp);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+        for (int yy = 0; yy < iwy; yy++) {
+            double *rr = pr + N * (size_t)yy, *ph = pp + N * (size_t)yy;
+            int *ix = px + N * (size_t)yy;
+            for (size_t k = 0; k < N; k++) {
+                rr[k] = 0;
+                ph[k] = 0;
+                ix[k] = 0;
+            }
+            for (int xx = 0; xx < iwx; xx++) {
+                const double wyt = wyl + (double)yy * wyi, wxt = wxl + (double)xx * wxi;
+                memset(Fg, 0, sizeof(double) * 2 * P);
+                for (int i = 0; i < winH; i++)
+                    for (int j = 0; j < winW; j++) {
+                        size_t id = (size_t)i * Wp + j;
+                        double ys = (double)(i - (winH - 1) / 2), xs = (double)(j - (winW - 1) / 2);
+                        double gv = g[(size_t)i * winW + j];
+                        Fg[2 * id] = gv * cos(wxt * xs + wyt * ys);
+                        Fg[2 * id + 1] = gv * sin(wxt * xs + wyt * ys);
+                    }
+                fft2_exec(&p, Fg, 0);
+                for (size_t k = 0; k < P; k++) {
+                    double ar = Ff[2 * k], ai = Ff[2 * k + 1], br = Fg[2 * k], bi = Fg[2 * k + 1];
+                    Sf[2 * k] = (ar * br - ai * bi) * invP;
+                    Sf[2 * k + 1] = (ar * bi + ai * br) * invP;
+                }
+                fft2_exec(&p, Sf, 1);
+                for (int i = 0; i < H; i++)
+                    for (int j = 0; j < W; j++) {
+                        size_t s = (size_t)(i + sy) * Wp + (j + sx), d = (size_t)i * W + j;
+                        double re = Sf[2 * s], im = Sf[2 * s + 1];
+                        double a = sqrt(re * re + im * im);
+                        if (a >= rr[d]) {
+                            rr[d] = a;
+                            ix[d] = xx;
+                            ph[d] = atan2(im, re);
+                        }
+                    }
+            }
+        }
+        fft2_free(&p);
+        free(Fg);
+        free(Sf);
+    }
+    /* merge the frequency rows in order with `>=` */
+    for (size_t k = 0; k < N; k++) {
+        double best = 0, ph = 0;
+        int bx = 0, by = 0;
+        for (int yy = 0; yy < iwy; yy++) {
+            double a = pr[N * (size_t)yy + k];
+            if (a >= best) {
+                best = a;
+                bx = px[N * (size_t)yy + k];
+                by = yy;
+                ph = pp[N * (size_t)yy + k];
+            }
+        }
+        r[k] = best;
+        wx[k] = wxl + (double)bx * wxi;
+        wy[k] = wyl + (double)by * wyi;
+        phase[k] = ph;
+    }
+    free(pr);
+    free(pp);
+    free(px);
+
+    /* curvature least squares with the border pixel replicated */
+    double sxx = 0, syy = 0;
+    for (int i = 0; i < winH; i++)
+        for (int j = 0; j < winW; j++) {
+            double y = (double)(i - sy), x = (double)(j - sx);
+            sxx += x * x * g[(size_t)i * winW + j];
+            syy += y * y * g[(size_t)i * winW + j];
+        }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int i = 0; i < H; i++)
+        for (int j = 0; j < W; j++) {
+            double ax = 0, ay = 0;
+            for (int a = 0; a < winH; a++) {
+                const int m = a - sy;
+                int yi = i - m;
+                yi = yi < 0 ? 0 : (yi > H - 1 ? H - 1 : yi);
+                for (int c = 0; c < winW; c++) {
+                    const int n = c - sx;
+                    int xi = j - n;
+                    xi = xi < 0 ? 0 : (xi > W - 1 ? W - 1 : xi);
+                    const double gv = g[(size_t)a * winW + c];
+                    ax += gv * (double)n * wx[(size_t)yi * W + xi];
+                    ay += gv * (double)m * wy[(size_t)yi * W + xi];
+                }
+            }
+            const size_t k = (size_t)i * W + j;
+            cxx[k] = -ax / sxx;
+            cyy[k] = -ay / syy;
+            double pc = phase[k] - 0.5 * atan(sigx * sigx * cxx[k]) - 0.5 * atan(sigy * sigy * cyy[k]);
+            phase_comp[k] = atan2(sin(pc), cos(pc));
+            b[k] = r[k] * pow((1 + sigx * sigx * sigx * sigx * cxx[k] * cxx[k]) * 0.25 / M_PI / (sigx * sigx), 0.25) *
+                   pow((1 + sigy * sigy * sigy * sigy * cyy[k] * cyy[k]) * 0.25 / M_PI / (sigy * sigy), 0.25);
+        }
+    free(g);
+    free(Ff);
+    return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Small dense solves.                                                      */
 /* ------------------------------------------------------------------------ */

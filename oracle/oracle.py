@@ -63,6 +63,7 @@ def lib():
             L.or_aia_phi_solve.argtypes = [c_int, c_int, dp, dp, dp, dp]
             L.or_aia.argtypes = [c_int, c_int, dp, dp, c_int, c_double, dp, ip, dp]
             L.or_unwrap2.argtypes = [c_int, c_int, dp, c_int, c_int]
+            L.or_wfr2.argtypes = [c_int, c_int, dp] + [c_double] * 8 + [dp] * 8 + [c_int]
             _lib = L
     return _lib
 
@@ -137,6 +138,25 @@ def wff2(f, sigx, wxl, wxh, wxi, sigy, wyl, wyh, wyi, thr, nthreads=0, ky=None):
     if rc:
         raise MemoryError("oracle allocation failed")
     return out, thr_used.value
+
+
+WFR_FIELDS = ("wx", "wy", "phase", "phase_comp", "b", "r", "cxx", "cyy")
+
+
+def wfr2(f, sigx, wxl, wxh, wxi, sigy, wyl, wyh, wyi, nthreads=0):
+    """WFR2 (windowed Fourier ridges) of complex H x W ``f``
+    (WFT/WFT2_CPU.cpp:391-694).  Returns a dict of the eight H x W result
+    maps of WFT2_HostResults: wx, wy, phase, phase_comp, b, r, cxx, cyy."""
+    a = _c128(f)
+    H, W = a.shape
+    out = {k: np.zeros((H, W), np.float64) for k in WFR_FIELDS}
+    rc = lib().or_wfr2(W, H, _dp(a.view(np.float64)), sigx, wxl, wxh, wxi, sigy, wyl, wyh, wyi,
+                       *[_dp(out[k]) for k in WFR_FIELDS], int(nthreads))
+    if rc == -1:
+        raise ValueError("FFT padding is out of range [4096]")
+    if rc:
+        raise MemoryError("oracle allocation failed")
+    return out
 
 
 def dpra_ls(img, phiref, r=1, nthreads=0, raw=False):

@@ -95,6 +95,26 @@ int main(int argc, char **argv)
             save(dir + "/wff_f32.c64", out);
             std::cout << "WFT2_CUDAF time_ms=" << t << "\n";
         }
+        // ---- WFT2_CUDAF (WFR) on the same device field: the ridge maps
+        {
+            auto f = load<float>(dir + "/field.c64", 2 * N);
+            WFT_FPA::WFT::WFT2_DeviceResultsF z;
+            WFT_FPA::WFT::WFT2_CUDAF wfr(W, H, WFT_FPA::WFT::WFT_TYPE::WFR, (float)sigma, (float)wl, (float)wh,
+                                         (float)wi, (float)sigma, (float)wl, (float)wh, (float)wi, 0.f, z);
+            cuFloatComplex *d_f = nullptr;
+            cudaMalloc((void **)&d_f, sizeof(cuFloatComplex) * N);
+            cudaMemcpy(d_f, f.data(), sizeof(cuFloatComplex) * N, cudaMemcpyHostToDevice);
+            double t = 0;
+            wfr(d_f, z, t);
+            const float *maps[8] = {z.m_d_wx, z.m_d_wy, z.m_d_phase, z.m_d_phase_comp,
+                                    z.m_d_b,  z.m_d_r,  z.m_d_cxx,   z.m_d_cyy};
+            std::vector<float> out(8 * N);
+            for (int k = 0; k < 8; k++)
+                cudaMemcpy(out.data() + k * N, maps[k], sizeof(float) * N, cudaMemcpyDeviceToHost);
+            cudaFree(d_f);
+            save(dir + "/wfr_f32.f32", out);
+            std::cout << "WFT2_CUDAF(WFR) time_ms=" << t << "\n";
+        }
         // ---- AIA_CUDAF on BMP files read through cv::imread
         {
             std::vector<cv::Mat> v;
@@ -116,7 +136,7 @@ int main(int argc, char **argv)
         int caught = 0;
         try {
             WFT_FPA::WFT::WFT2_DeviceResultsF z;
-            WFT_FPA::WFT::WFT2_CUDAF bad(64, 64, WFT_FPA::WFT::WFT_TYPE::WFR, z);
+            WFT_FPA::WFT::WFT2_CUDAF bad(4090, 16, WFT_FPA::WFT::WFT_TYPE::WFR, z);
         } catch (const std::runtime_error &) {
             caught++;
         }

@@ -1,6 +1,6 @@
-"""The reference's C++ class interfaces (DPRA_CUDAF, DPRA_CUDA, WFT2_CUDAF,
-AIA_CUDAF) driven from a compiled C++ program (tests/cpp/test_classes.cpp)
-and checked against the FP64 oracle."""
+"""The reference's C++ class interfaces (DPRA_CUDAF, DPRA_CUDA, WFT2_CUDAF
+with WFT_TYPE::WFF and WFR, AIA_CUDAF) driven from a compiled C++ program
+(tests/cpp/test_classes.cpp) and checked against the FP64 oracle."""
 import os
 import struct
 import subprocess
@@ -58,6 +58,15 @@ def test_reference_class_interfaces(tmp_path, oracle, synth):
     wf = np.fromfile(os.path.join(d, "wff_f32.c64"), np.complex64).reshape(H, W)
     ref, _ = oracle.wff2(field.astype(np.complex128), *wp.tuple())
     assert np.abs(wf - ref).max() < 1e-4 * np.abs(ref).max()
+    # WFT2_CUDAF with WFT_TYPE::WFR: the ridge maps against the oracle's WFR2
+    wr = np.fromfile(os.path.join(d, "wfr_f32.f32"), np.float32).reshape(8, H, W)
+    ow = oracle.wfr2(field.astype(np.complex128), wpar[0], wpar[1], wpar[2], wpar[3], wpar[0], wpar[1], wpar[2],
+                     wpar[3])
+    got = dict(zip(oracle.WFR_FIELDS, wr))
+    assert np.abs(got["r"] - ow["r"]).max() < 1e-4 * ow["r"].max()
+    same = (got["wx"] == ow["wx"].astype(np.float32)) & (got["wy"] == ow["wy"].astype(np.float32))
+    assert same.mean() > 0.99
+    assert np.abs(np.angle(np.exp(1j * (got["phase"] - ow["phase"]))))[same].max() < 1e-3
     # AIA_CUDAF on BMPs read by the class layer's imread
     img1 = np.fromfile(os.path.join(d, "aia_img1.u8"), np.uint8).reshape(256, 256)
     assert np.array_equal(img1, g["frames"][0])
