@@ -365,6 +365,33 @@ def surrogate_accuracy(glsu, torch, dfr, phi0, wp, params, dil, nframes):
             "tiles_probed": probed, "tiles_recomputed": flagged}
 
 
+def wfr_measure(glsu, torch, phi0, size, seed):
+    """WFR2 (windowed Fourier ridges) with the reference's WFR defaults
+    (sigma 10, 161 x 161 frequencies on [-2, 2] step 0.025, counted in float as
+    WFT2_CUDAF does) on the fringe field exp(j phi0) + noise at size^2, FP32:
+    device time of one run (after one warm-up) and the FP32-pipe fraction of
+    its algorithmic FMAs (per frequency and pixel, 2 (2s+1) for the column
+    filter; per wx and pixel, 2 (2s+1) for the row filter)."""
+    rng = np.random.default_rng(seed)
+    f = np.exp(1j * phi0) + 0.05 * (rng.standard_normal(phi0.shape) + 1j * rng.standard_normal(phi0.shape))
+    df = torch.from_numpy(f.astype(np.complex64)).cuda()
+    maps = {k: torch.empty((size, size), dtype=torch.float32, device="cuda") for k in glsu.WFR_FIELDS}
+    ptrs = {k: v.data_ptr() for k, v in maps.items()}
+    p = glsu.default_params(glsu.WFT_WFR)
+    w = glsu.WFR2(size, size, "f32", p)
+    w.run(df.data_ptr(), ptrs)
+    ms = min(w.run(df.data_ptr(), ptrs) for _ in range(3))
+    w.close()
+    n = glsu.wff_count(p.wxl, p.wxh, p.wxi, glsu.F32)
+    s = int(np.floor(3 * p.sigma_x + 0.5))
+    fma = float(n) * n * size * size * 2 * (2 * s + 1) + float(n) * size * size * 2 * (2 * s + 1)
+    return {"workload": "WFR2 of exp(j phi0) + noise, %dx%d FP32, sigma %g, %dx%d frequencies on [%g, %g] step %g"
+                        % (size, size, p.sigma_x, n, n, p.wxl, p.wxh, p.wxi),
+            "ms": ms, "frames_per_s": 1e3 / ms, "algorithmic_fma": fma,
+            "fp32_tflops": 2 * fma / (ms * 1e-3) / 1e12,
+            "fp32_frac_of_peak_at_2070mhz": 2 * fma / (ms * 1e-3) / (152 * 128 * 2 * 2070e6)}
+
+
 def run_ours(args, rank, world, local):
     import torch
     import glsu
@@ -388,6 +415,8 @@ def run_ours(args, rank, world, local):
     aia.run(list(aframes), None, max_iter=30, max_err=1e-4, seed=seed)  # warm
     _, _, aia_ms, aia_iters, aia_err = aia.run(list(aframes), None, max_iter=30, max_err=1e-4, seed=seed)
     aia.close()
+
+    wfr = wfr_measure(glsu, torch, phi0, size, seed)
 
     stream = torch.cuda.Stream()
     dfr = torch.from_numpy(frames).cuda()
@@ -519,6 +548,7 @@ def run_ours(args, rank, world, local):
                                 "wff_final_update": p_st[3]},
                   "roofline": plain_roof, "clocks": p_clk, "gpu_launches_per_step": PLAIN_LAUNCHES},
         "surrogate": sur,
+        "wfr": wfr,
         "aia": {"frames": 5, "ms": aia_ms, "iterations": aia_iters, "err": aia_err,
                 "ms_per_frame_over_200": aia_ms / 200},
     }
