@@ -187,22 +187,21 @@ inline int sur_layer_offset(int l) { return l == 0 ? 0 : kSurL0Params + (l - 1) 
 
 struct SurConvArgs {
     int B = 0, H = 0, W = 0, dil = 1;
-    const uint16_t *wpack = nullptr;  // [9][4][32][8] BF16 B-operand image of the layer
-    const float *bias = nullptr;      // [32] or null
+    const uint16_t *wpack = nullptr;  // packed BF16 B operand of the layer
+    const float *bias = nullptr;      // [32] (hidden layer) / [2] (last layer) or null
     const uint16_t *mask = nullptr;   // [B][H][W][32]: output zeroed where mask <= 0 (null: none)
-    uint16_t *out = nullptr;          // [B][H][W][32] BF16
+    uint16_t *out = nullptr;          // hidden layer: [B][H][W][32] BF16
     int relu = 1;
     int *err = nullptr;
+    // last layer: y = z + conv + bias; cout = y / |y| (inference) or yout = y (training)
+    const float2 *z = nullptr;
+    float2 *cout = nullptr, *yout = nullptr;
 };
-// Weights of the two CUDA-core layers, passed to their kernels by value
-// (a shared-memory copy read once per FMA made these layers load-bound).
+// Weights of the first (CUDA-core) layer, passed to its kernel by value
+// (a shared-memory copy read once per FMA made it load-bound).
 struct SurL0W {
     float w[32 * 18];  // [co][ci][t], BF16-rounded
     float b[32];
-};
-struct SurL7W {
-    float w[2 * 288];  // [co][ci][t], BF16-rounded
-    float b[2];
 };
 int sur_make_map(CUtensorMap *tm, const void *act, int B, int H, int W, int dil);
 int sur_make_out_map(CUtensorMap *tm, const void *act, int B, int H, int W);
@@ -221,6 +220,9 @@ struct WfrBuffers {
 // Enqueue one WFR2 of d_f (H x W complex) into the eight result maps.
 int enqueue_wfr(WffPlan &P, const WfrBuffers &wb, cudaStream_t s, const void *d_f, const glsu_wfr_results &z);
 int launch_sur_conv(const CUtensorMap &tm, const CUtensorMap &tmo, const SurConvArgs &a, cudaStream_t s);
+// The last layer (32 -> 2, residual, renormalisation) on the tensor cores;
+// tm maps its input activation with the layer's dilation.
+int launch_sur_last(const CUtensorMap &tm, const SurConvArgs &a, cudaStream_t s);
 
 // AIA
 struct AiaDev {

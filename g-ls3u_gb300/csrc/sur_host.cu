@@ -20,20 +20,21 @@ static int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, kS
 // Blocks of the row-walking per-pixel kernels (a block takes whole image rows).
 int SurNet::rows_grid() const { return std::min(B * H, kSurPixBlocks); }
 
-// Blocks of the last layer: one per 128-pixel row segment.
-int SurNet::l7_grid() const { return B * H * ((W + kL7Seg - 1) / kL7Seg); }
-
-int SurNet::launch_l7(const float2 *z, float2 *outp, const float2 *target, float2 *dhp, double *partp)
+int SurNet::last(const float2 *z, float2 *outp, float2 *yp)
 {
-    static int attr = 0;
-    const int smem = sur_l7_smem(dil[7]);
-    if (smem > attr) {
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(sur_l7_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sur_l7_smem(64)));
-        attr = sur_l7_smem(64);
-    }
-    sur_l7_kernel<<<l7_grid(), kL7Seg, smem, stream>>>(a6(), z, B, H, W, dil[7], h_w7, outp, target, dhp, partp);
-    GLSU_CUDA_TRY(cudaGetLastError());
-    return GLSU_OK;
+    SurConvArgs a;
+    a.B = B;
+    a.H = H;
+    a.W = W;
+    a.dil = dil[7];
+    a.wpack = d_pk7;
+    a.bias = d_master + sur_layer_offset(7) + 576;
+    a.relu = 0;
+    a.err = d_err;
+    a.z = z;
+    a.cout = outp;
+    a.yout = yp;
+    return launch_sur_last(map7, a, stream);
 }
 
 int SurNet::init(int batch, int width, int height, const int *dilations, bool train)
@@ -52,14 +53,16 @@ int SurNet::init(int batch, int width, int height, const int *dilations, bool tr
     const size_t abytes = n * 32 * sizeof(uint16_t);
     auto A = [&](void **p, size_t bytes) { return cudaMalloc(p, bytes) == cudaSuccess; };
     bool ok = A((void **)&d_master, kSurParams * 4) && A((void **)&d_pk_fwd, 6 * 9216 * 2) &&
-              A((void **)&d_pk_bwd, 6 * 9216 * 2) && A((void **)&d_w0r, 576 * 4) && A((void **)&d_w7r, 576 * 4) &&
+              A((void **)&d_pk_bwd, 6 * 9216 * 2) && A((void **)&d_pk7, kSurPk7Bytes) &&
+              A((void **)&d_w0r, 576 * 4) && A((void **)&d_w7r, 576 * 4) &&
               A((void **)&d_err, sizeof(int));
     const int nact = training ? 7 : 2;
     for (int k = 0; k < nact && ok; k++) ok = A((void **)&d_act[k], abytes);
     if (training && ok) {
         ok = A((void **)&d_g[0], abytes) && A((void **)&d_g[1], abytes) && A((void **)&d_dh, n * 8) &&
              A((void **)&d_out, n * 8) && A((void **)&d_grad, kSurParams * 4) && A((void **)&d_m, kSurParams * 4) &&
-             A((void **)&d_v, kSurParams * 4) && A((void **)&d_lpart, (size_t)l7_grid() * 8) &&
+             A((void **)&d_v, kSurParams * 4) && A((void **)&d_lpart, (size_t)kSurPixBlocks * 8) &&
+             A((void **)&d_y, n * 8) &&
              A((void **)&d_loss, 8);
         nb32 = sur_dw32_blocks(B, H, W);
         nbs = (int)((n + kSurSmallPix - 1) / kSurSmallPix);
@@ -83,27 +86,27 @@ int SurNet::init(int batch, int width, int height, const int *dilations, bool tr
             GLSU_TRY(sur_make_out_map(&map_bwd_out[l], d_g[(7 - l) & 1], B, H, W));
         }
     }
+    GLSU_TRY(sur_make_map(&map7, a6(), B, H, W, dil[7]));
     return pack();
 }
 
 void SurNet::release()
 {
-    void *ps[] = {d_master, d_pk_fwd, d_pk_bwd, d_w0r, d_w7r, d_err, d_g[0], d_g[1], d_dh, d_out, d_grad, d_m,
-                  d_v, d_lpart, d_loss, d_part};
+    void *ps[] = {d_master, d_pk_fwd, d_pk_bwd, d_pk7, d_w0r, d_w7r, d_err, d_g[0], d_g[1], d_dh, d_out, d_y,
+                  d_grad, d_m, d_v, d_lpart, d_loss, d_part};
     for (void *p : ps) cudaFree(p);
     for (int k = 0; k < 7; k++) cudaFree(d_act[k]);
 }
 
 int SurNet::pack()
 {
-    sur_pack_kernel<<<(6 * 9216 + 255) / 256, 256, 0, stream>>>(d_master, d_pk_fwd, d_pk_bwd, d_w0r, d_w7r);
+    GLSU_CUDA_TRY(cudaMemsetAsync(d_pk7, 0, kSurPk7Bytes, stream));  // the zero-padded outputs 2..15
+    sur_pack_kernel<<<(6 * 9216 + 255) / 256, 256, 0, stream>>>(d_master, d_pk_fwd, d_pk_bwd, d_w0r, d_w7r,
+                                                                d_pk7);
     GLSU_CUDA_TRY(cudaGetLastError());
-    // layers 0 and 7 take their weights as kernel parameters
-    const int off7 = sur_layer_offset(7);
+    // layer 0 takes its weights as kernel parameters
     GLSU_CUDA_TRY(cudaMemcpyAsync(h_w0.w, d_w0r, sizeof(h_w0.w), cudaMemcpyDeviceToHost, stream));
     GLSU_CUDA_TRY(cudaMemcpyAsync(h_w0.b, d_master + 576, sizeof(h_w0.b), cudaMemcpyDeviceToHost, stream));
-    GLSU_CUDA_TRY(cudaMemcpyAsync(h_w7.w, d_w7r, sizeof(h_w7.w), cudaMemcpyDeviceToHost, stream));
-    GLSU_CUDA_TRY(cudaMemcpyAsync(h_w7.b, d_master + off7 + 576, sizeof(h_w7.b), cudaMemcpyDeviceToHost, stream));
     GLSU_CUDA_TRY(cudaStreamSynchronize(stream));
     return GLSU_OK;
 }
@@ -169,7 +172,7 @@ const uint16_t *SurNet::a6() const { return training ? d_act[6] : d_act[0]; }
 int SurNet::forward(const void *d_z, void *d_outp, cudaEvent_t *ev)
 {
     GLSU_TRY(hidden((const float2 *)d_z, ev));
-    return launch_l7((const float2 *)d_z, (float2 *)d_outp, nullptr, nullptr, nullptr);
+    return last((const float2 *)d_z, (float2 *)d_outp, nullptr);
 }
 
 int SurNet::backward(const void *d_z, const void *d_target)
@@ -178,8 +181,10 @@ int SurNet::backward(const void *d_z, const void *d_target)
     const float2 *z = (const float2 *)d_z;
     GLSU_TRY(hidden(z));
     const int g = rows_grid();
-    GLSU_TRY(launch_l7(z, d_out, (const float2 *)d_target, d_dh, d_lpart));
-    sur_sum_kernel<<<1, 32, 0, stream>>>(d_lpart, l7_grid(), d_loss);
+    GLSU_TRY(last(z, nullptr, d_y));
+    sur_l7_loss_kernel<<<kSurPixBlocks, 256, 0, stream>>>(d_y, (const float2 *)d_target, (size_t)B * H * W, d_out,
+                                                          d_dh, d_lpart);
+    sur_sum_kernel<<<1, 32, 0, stream>>>(d_lpart, kSurPixBlocks, d_loss);
     // layer 7: weight gradient and dL/da6 (masked)
     sur_dw_small_kernel<2, 32><<<nbs, 256, 0, stream>>>(d_dh, d_act[6], B, H, W, dil[7], kSurSmallPix, d_part);
     sur_reduce_kernel<<<(kSurL7Params + 255) / 256, 256, 0, stream>>>(d_part, nbs, kSurL7Params,
@@ -388,7 +393,7 @@ extern "C" int glsu_sur_conv32(const void *d_in, void *d_out, int batch, int wid
     if (rc == GLSU_OK) {
         cudaMemcpyAsync(d_master, master.data(), kSurParams * 4, cudaMemcpyHostToDevice, s);
         cudaMemsetAsync(d_err, 0, 4, s);
-        sur_pack_kernel<<<(6 * 9216 + 255) / 256, 256, 0, s>>>(d_master, d_pk, d_pkb, d_w0r, d_w7r);
+        sur_pack_kernel<<<(6 * 9216 + 255) / 256, 256, 0, s>>>(d_master, d_pk, d_pkb, d_w0r, d_w7r, nullptr);
         SurConvArgs a;
         a.B = batch;
         a.H = height;

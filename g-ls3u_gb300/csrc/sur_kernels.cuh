@@ -55,15 +55,36 @@
 namespace glsu {
 
 constexpr int kSurSlots = 8;     // input-row ring of the tensor-core conv (TMA loads in flight)
-constexpr int kSurRows = 8;      // output rows per work item = TMEM accumulators (32 columns each)
-constexpr int kSurTmemCols = kSurRows * 32;
-constexpr int kSurWBytes = 9 * 4 * 32 * 16;  // packed B operand of one layer
-// packed B operand: [dx][K half kc][8-channel chunk h][96 rows][8 channels],
-// row n = 32 * (2 - dy) + output channel
-constexpr int kSurBRows = 96;
-constexpr int kSurBHalf = kSurBRows * 16;      // bytes between the two 8-channel chunks of one K = 16 step
-constexpr int kSurBStep = 2 * kSurBHalf;       // bytes of one (dx, kc) operand
-constexpr int kSurStageBytes = 32 * 64;        // one epilogue warp's output tile
+constexpr int kSurRows = 8;      // output rows per work item = TMEM accumulators
+constexpr int kSurWBytes = 9 * 4 * 32 * 16;  // packed B operand of a 32 -> 32 layer
+constexpr int kSurStageBytes = 32 * 64;      // one epilogue warp's output tile
+
+// Geometry of a tensor-core layer with NOUT output channels per accumulator:
+// 32 for the hidden layers, 16 for the last layer (its 2 outputs padded with
+// zero weights to the smallest N of an M = 128 MMA).  The packed B operand
+// is [dx][K half kc][8-channel chunk h][3 NOUT rows][8 channels], row
+// n = NOUT (2 - dy) + output channel.
+template <int NOUT> struct SurTc {
+    static constexpr int BROWS = 3 * NOUT;
+    static constexpr int BHALF = BROWS * 16;  // bytes between the two 8-channel chunks of one K = 16 step
+    static constexpr int BSTEP = 2 * BHALF;   // bytes of one (dx, kc) operand
+    static constexpr int WBYTES = 6 * BSTEP;  // 3 dx x 2 kc operands (a 1024-byte multiple)
+    static constexpr int TMEM_COLS = kSurRows * NOUT;
+    static constexpr int STAGE = NOUT == 32 ? 4 * kSurStageBytes : 0;
+    static constexpr int NBIAS = NOUT == 32 ? 32 : 2;
+};
+static_assert(SurTc<32>::WBYTES == kSurWBytes && SurTc<16>::WBYTES % 1024 == 0, "B operand layout");
+constexpr int kSurPk7Bytes = SurTc<16>::WBYTES;  // packed B operand of the last layer
+
+// out = y / |y| with the same rounding wherever it is evaluated (the last
+// layer's epilogue in inference, the loss kernel in training).
+__device__ __forceinline__ void sur_unit(float yr, float yi, float &orr, float &oii, float &inv)
+{
+    const float nrm = __fsqrt_rn(__fadd_rn(__fmul_rn(yr, yr), __fmul_rn(yi, yi)));
+    inv = nrm > 1e-20f ? __fdiv_rn(1.f, nrm) : 0.f;
+    orr = __fmul_rn(yr, inv);
+    oii = __fmul_rn(yi, inv);
+}
 
 __device__ __forceinline__ float bf2f(uint16_t v) { return __uint_as_float((uint32_t)v << 16); }
 
@@ -115,18 +136,23 @@ __device__ __forceinline__ SurItem sur_item(const SurConvArgs &a, int item)
 // (blockIdx.x, + gridDim.x, ...); input rows are numbered across items and
 // each accumulator completes one phase of its two mbarriers per item (a
 // block that an item leaves unused gets an empty phase), which keeps the
-// mbarrier parities consistent.
+// mbarrier parities consistent.  NOUT = 32: a hidden layer (ReLU / mask,
+// BF16 NHWC by TMA store through tmo); NOUT = 16: the last layer (y = z +
+// conv + bias from the first two accumulator columns; out = y / |y| into
+// a.cout, or y itself into a.yout).
+template <int NOUT>
 __global__ void __launch_bounds__(256, 1) sur_conv_tc_kernel(const __grid_constant__ CUtensorMap tm,
                                                              const __grid_constant__ CUtensorMap tmo, SurConvArgs a,
                                                              int nitems)
 {
+    using L = SurTc<NOUT>;
     extern __shared__ __align__(1024) unsigned char sm[];
     const int BW = 128 + 2 * a.dil;
     const int slot_bytes = (BW * 64 + 1023) & ~1023;
     unsigned char *wsm = sm;
-    unsigned char *slots = sm + kSurWBytes;
+    unsigned char *slots = sm + L::WBYTES;
     unsigned char *stage = slots + kSurSlots * slot_bytes;  // [4 warps][32 px][64 B], 64-byte swizzle
-    uint64_t *full = reinterpret_cast<uint64_t *>(stage + 4 * kSurStageBytes);
+    uint64_t *full = reinterpret_cast<uint64_t *>(stage + L::STAGE);
     uint64_t *sfree = full + kSurSlots;
     uint64_t *accf = sfree + kSurSlots;  // [kSurRows] accumulator complete
     uint64_t *acce = accf + kSurRows;    // [kSurRows] accumulator drained and refilled with the bias
@@ -147,10 +173,10 @@ __global__ void __launch_bounds__(256, 1) sur_conv_tc_kernel(const __grid_consta
         mbar_init(drain, 1);
         fence_mbar_init();
     }
-    if (warp == 0) tmem_alloc(tslot, kSurTmemCols);
-    for (int e = tid; e < kSurWBytes / 16; e += 256)
+    if (warp == 0) tmem_alloc(tslot, L::TMEM_COLS);
+    for (int e = tid; e < L::WBYTES / 16; e += 256)
         reinterpret_cast<uint4 *>(wsm)[e] = reinterpret_cast<const uint4 *>(a.wpack)[e];
-    if (tid < 32) bias_s[tid] = a.bias ? a.bias[tid] : 0.f;
+    if (tid < 32) bias_s[tid] = (a.bias && tid < L::NBIAS) ? a.bias[tid] : 0.f;
     fence_proxy_async_smem();  // the weight image was written by generic stores
     tc_fence_before();
     __syncthreads();
@@ -198,19 +224,19 @@ __global__ void __launch_bounds__(256, 1) sur_conv_tc_kernel(const __grid_consta
                 if (!ok) break;
                 tc_fence_after();
                 const int klo = max(0, j - 2), khi = min(it.nout - 1, j);
-                const uint32_t id = khi == klo       ? umma_idesc_bf16(128, 32)
-                                    : khi == klo + 1 ? umma_idesc_bf16(128, 64)
-                                                     : umma_idesc_bf16(128, 96);
-                const uint32_t d = tmem + (uint32_t)(klo * 32);
+                const uint32_t id = khi == klo       ? umma_idesc_bf16(128, NOUT)
+                                    : khi == klo + 1 ? umma_idesc_bf16(128, 2 * NOUT)
+                                                     : umma_idesc_bf16(128, 3 * NOUT);
+                const uint32_t d = tmem + (uint32_t)(klo * NOUT);
                 const uint32_t srow = sbase + (uint32_t)(s * slot_bytes);
-                const uint32_t brow = wbase + (uint32_t)((2 - j + klo) * 32 * 16);
+                const uint32_t brow = wbase + (uint32_t)((2 - j + klo) * NOUT * 16);
 #pragma unroll
                 for (int dx = 0; dx < 3; dx++) {
 #pragma unroll
                     for (int kc = 0; kc < 2; kc++) {
                         const uint32_t astart = srow + (uint32_t)(dx * a.dil * 64 + kc * 32);
                         const uint64_t ad = umma_desc_sw64(astart, 0);
-                        const uint64_t bd = umma_desc(brow + (uint32_t)((dx * 2 + kc) * kSurBStep), kSurBHalf, 128);
+                        const uint64_t bd = umma_desc(brow + (uint32_t)((dx * 2 + kc) * L::BSTEP), L::BHALF, 128);
                         umma_bf16(d, ad, bd, id, 1u);
                     }
                 }
@@ -226,7 +252,51 @@ __global__ void __launch_bounds__(256, 1) sur_conv_tc_kernel(const __grid_consta
         if (!ok) atomicExch(a.err, GLSU_ERR_TIMEOUT);
         umma_commit(drain);  // every MMA has completed before TMEM is released
         mbar_wait_bounded(drain, 0);
-    } else if (warp >= 4) {
+    } else if (warp >= 4 && NOUT == 16) {
+        // ---- last-layer epilogue: y = z + h, out = y / |y|; refill with the bias ----
+        const int q = warp - 4;
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+        float bias[16];
+#pragma unroll
+        for (int c = 0; c < 16; c++) bias[c] = bias_s[c];
+        for (int b = 0; b < kSurRows; b++) tmem_st16(lane_base + b * NOUT, bias);
+        tc_fence_before();
+        for (int b = 0; b < kSurRows; b++) mbar_arrive(&acce[b]);
+        uint32_t li = 0;
+        bool ok = true;
+        for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+            const SurItem it = sur_item(a, item);
+            if (it.nout <= 0) continue;
+            const int x = it.x0 + q * 32 + lane;
+            for (int k = 0; k < kSurRows; k++) {
+                if (!__all_sync(0xffffffffu, mbar_wait_bounded(&accf[k], li & 1))) {
+                    if (lane == 0) atomicExch(a.err, GLSU_ERR_TIMEOUT);
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                float h[2] = {0.f, 0.f};
+                if (k < it.nout) {
+                    tmem_ld2(lane_base + k * NOUT, h);
+                    tmem_st16(lane_base + k * NOUT, bias);
+                }
+                tc_fence_before();
+                mbar_arrive(&acce[k]);
+                if (k >= it.nout || x >= a.W) continue;
+                const size_t p = ((size_t)it.b * a.H + it.r + (size_t)(it.kbeg + k) * a.dil) * a.W + x;
+                const float2 zv = a.z[p];
+                const float yr = __fadd_rn(zv.x, h[0]), yi = __fadd_rn(zv.y, h[1]);
+                if (a.yout) {
+                    a.yout[p] = make_float2(yr, yi);
+                } else {
+                    float orr, oii, inv;
+                    sur_unit(yr, yi, orr, oii, inv);
+                    a.cout[p] = make_float2(orr, oii);
+                }
+            }
+            li++;
+        }
+    } else if (warp >= 4 && NOUT == 32) {
         // ---- epilogue: TMEM -> ReLU, mask -> BF16 NHWC; refill with the bias ----
         const int q = warp - 4;
         const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
@@ -299,15 +369,15 @@ __global__ void __launch_bounds__(256, 1) sur_conv_tc_kernel(const __grid_consta
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, kSurTmemCols);
+    if (warp == 0) tmem_dealloc(tmem, L::TMEM_COLS);
 }
 
-int sur_conv_smem_bytes(int dil)
+template <int NOUT> static int sur_conv_smem_bytes(int dil)
 {
     const int BW = 128 + 2 * dil;
     const int slot_bytes = (BW * 64 + 1023) & ~1023;
-    return kSurWBytes + kSurSlots * slot_bytes + 4 * kSurStageBytes + (2 * kSurSlots + 2 * kSurRows + 1) * 8 + 32 * 4 +
-           16;
+    return SurTc<NOUT>::WBYTES + kSurSlots * slot_bytes + SurTc<NOUT>::STAGE +
+           (2 * kSurSlots + 2 * kSurRows + 1) * 8 + 32 * 4 + 16;
 }
 
 int sur_conv_items(int B, int H, int W, int dil)
@@ -347,23 +417,24 @@ int sur_make_out_map(CUtensorMap *tm, const void *act, int B, int H, int W)
     return sur_make_map_box(tm, act, B, H, W, 32);
 }
 
-int launch_sur_conv(const CUtensorMap &tm, const CUtensorMap &tmo, const SurConvArgs &a, cudaStream_t s)
+template <int NOUT>
+static int launch_sur_conv_t(const CUtensorMap &tm, const CUtensorMap &tmo, const SurConvArgs &a, cudaStream_t s)
 {
     static int attr_bytes = 0, sms = 0, regs = 0;
-    const int smem = sur_conv_smem_bytes(a.dil);
+    const int smem = sur_conv_smem_bytes<NOUT>(a.dil);
     if (smem > attr_bytes) {
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(sur_conv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           sur_conv_smem_bytes(64)));
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(sur_conv_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+        GLSU_CUDA_TRY(cudaFuncSetAttribute(sur_conv_tc_kernel<NOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           sur_conv_smem_bytes<NOUT>(64)));
+        GLSU_CUDA_TRY(cudaFuncSetAttribute(sur_conv_tc_kernel<NOUT>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                            (int)cudaSharedmemCarveoutMaxShared));
-        attr_bytes = sur_conv_smem_bytes(64);
+        attr_bytes = sur_conv_smem_bytes<NOUT>(64);
     }
     if (!sms) {
         int dev = 0;
         GLSU_CUDA_TRY(cudaGetDevice(&dev));
         GLSU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         cudaFuncAttributes fa;
-        GLSU_CUDA_TRY(cudaFuncGetAttributes(&fa, sur_conv_tc_kernel));
+        GLSU_CUDA_TRY(cudaFuncGetAttributes(&fa, sur_conv_tc_kernel<NOUT>));
         regs = std::max(1, fa.numRegs);
     }
     // persistent: as many CTAs as are resident at once, each walking a
@@ -373,13 +444,24 @@ int launch_sur_conv(const CUtensorMap &tm, const CUtensorMap &tmo, const SurConv
     const int warp_regs = (regs * 32 + 255) / 256 * 256;
     const int by_regs = 65536 / (8 * warp_regs);
     const int by_smem = (228 * 1024) / (smem + 1024);
-    const int by_tmem = 512 / kSurTmemCols;
+    const int by_tmem = 512 / SurTc<NOUT>::TMEM_COLS;
     const int per_sm = std::max(1, std::min(std::min(by_regs, by_smem), by_tmem));
     const int items = sur_conv_items(a.B, a.H, a.W, a.dil);
     const int grid = std::min(items, per_sm * sms);
-    sur_conv_tc_kernel<<<grid, 256, smem, s>>>(tm, tmo, a, items);
+    sur_conv_tc_kernel<NOUT><<<grid, 256, smem, s>>>(tm, tmo, a, items);
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
+}
+
+int launch_sur_conv(const CUtensorMap &tm, const CUtensorMap &tmo, const SurConvArgs &a, cudaStream_t s)
+{
+    return launch_sur_conv_t<32>(tm, tmo, a, s);
+}
+
+int launch_sur_last(const CUtensorMap &tm, const SurConvArgs &a, cudaStream_t s)
+{
+    if (!a.z || (!a.cout && !a.yout)) return fail(GLSU_ERR_INVALID, "last surrogate layer without input or output");
+    return launch_sur_conv_t<16>(tm, tm, a, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -420,90 +502,43 @@ __global__ void __launch_bounds__(256) sur_l0_kernel(const float2 *__restrict__ 
         }
 }
 
-// Last layer, residual, renormalisation: out = y/|y|, y = z + conv7(a6).
-// One CTA per 128-pixel segment of an image row: the three input rows
-// y - d, y, y + d (columns x0 - d .. x0 + 127 + d, zero outside the image)
-// are staged in shared memory by coalesced 16-byte loads, with an 80-byte
-// pixel stride so that the per-pixel 16-byte reads are free of bank
-// conflicts; one thread per pixel, weights in the parameter bank.  With a
-// target (training): per pixel loss wgt |out - t|^2, wgt = min(|target|, 1),
-// t = target/|target|, the gradient dL/dh7 of the mean loss into dh, and per
-// block loss sums into part.
-constexpr int kL7Seg = 128;
-constexpr int kL7Pix = 5;  // uint4 per staged pixel: 4 of data, 1 of padding
-
-int sur_l7_smem(int dil) { return 3 * (kL7Seg + 2 * dil) * kL7Pix * 16; }
-
-__global__ void __launch_bounds__(kL7Seg) sur_l7_kernel(const uint16_t *__restrict__ a6,
-                                                        const float2 *__restrict__ z, int B, int H, int W, int dil,
-                                                        const __grid_constant__ SurL7W wp, float2 *__restrict__ out,
-                                                        const float2 *__restrict__ target, float2 *__restrict__ dh,
-                                                        double *__restrict__ part)
+// Training loss of the last layer's output: from y = z + conv7(a6) (written
+// by the tensor-core last layer), out = y / |y| (the same rounding as the
+// inference epilogue), per pixel loss wgt |out - t|^2 with wgt = min(|target|,
+// 1) and t = target / |target|, the gradient dL/dh7 of the mean loss into dh
+// and per-block loss sums (fixed order) into part.
+__global__ void __launch_bounds__(256) sur_l7_loss_kernel(const float2 *__restrict__ yv,
+                                                          const float2 *__restrict__ target, size_t n,
+                                                          float2 *__restrict__ out, float2 *__restrict__ dh,
+                                                          double *__restrict__ part)
 {
-    extern __shared__ __align__(16) uint4 st7[];
-    __shared__ double red[kL7Seg];
-    const int nseg = (W + kL7Seg - 1) / kL7Seg;
-    const int row = blockIdx.x / nseg, seg = blockIdx.x - row * nseg;
-    const int y = row % H;
-    const size_t img = (size_t)(row - y) * W;
-    const int x0 = seg * kL7Seg, SW = kL7Seg + 2 * dil, tid = threadIdx.x;
-    for (int e = tid; e < 3 * SW * 4; e += kL7Seg) {
-        const int r = e / (SW * 4), rem = e - r * SW * 4, px = rem >> 2, c = rem & 3;
-        const int yy = y + (r - 1) * dil, xx = x0 - dil + px;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (yy >= 0 && yy < H && xx >= 0 && xx < W)
-            v = reinterpret_cast<const uint4 *>(a6 + (img + (size_t)yy * W + xx) * 32)[c];
-        st7[(r * SW + px) * kL7Pix + c] = v;
-    }
-    __syncthreads();
-    const int x = x0 + tid;
+    __shared__ double red[256];
+    const int tid = threadIdx.x;
+    const double inv_n = 1.0 / (double)n;
     double lsum = 0;
-    if (x < W) {
-        float h0 = wp.b[0], h1 = wp.b[1];
-#pragma unroll
-        for (int t = 0; t < 9; t++) {
-            const uint4 *sp = st7 + ((t / 3) * SW + tid + (t % 3) * dil) * kL7Pix;
-#pragma unroll
-            for (int c = 0; c < 4; c++) {
-                float av[8];
-                unpack8(sp[c], av);
-#pragma unroll
-                for (int i = 0; i < 8; i++) {
-                    h0 = fmaf(wp.w[(8 * c + i) * 9 + t], av[i], h0);
-                    h1 = fmaf(wp.w[288 + (8 * c + i) * 9 + t], av[i], h1);
-                }
-            }
-        }
-        const size_t p = img + (size_t)y * W + x;
-        const float2 xv = z[p];
-        const float yr = xv.x + h0, yi = xv.y + h1;
-        const float nrm = sqrtf(yr * yr + yi * yi);
-        const float inv = nrm > 1e-20f ? 1.f / nrm : 0.f;
-        const float orr = yr * inv, oii = yi * inv;
+    for (size_t p = (size_t)blockIdx.x * 256 + tid; p < n; p += (size_t)gridDim.x * 256) {
+        const float2 y = yv[p];
+        float orr, oii, inv;
+        sur_unit(y.x, y.y, orr, oii, inv);
         out[p] = make_float2(orr, oii);
-        if (target) {
-            const double inv_n = 1.0 / ((double)B * H * W);
-            const float2 tv = target[p];
-            const float tn = sqrtf(tv.x * tv.x + tv.y * tv.y);
-            const float wgt = fminf(tn, 1.f);
-            const float ti = tn > 1e-20f ? 1.f / tn : 0.f;
-            const float er = orr - tv.x * ti, ei = oii - tv.y * ti;
-            lsum = (double)(wgt * (er * er + ei * ei)) * inv_n;
-            // d out: 2 wgt e / n; through out = y/|y|: (g - out (out.g)) / |y|
-            const float gr = (float)(2.0 * inv_n) * wgt * er, gi = (float)(2.0 * inv_n) * wgt * ei;
-            const float dot = orr * gr + oii * gi;
-            dh[p] = make_float2((gr - orr * dot) * inv, (gi - oii * dot) * inv);
-        }
+        const float2 tv = target[p];
+        const float tn = sqrtf(tv.x * tv.x + tv.y * tv.y);
+        const float wgt = fminf(tn, 1.f);
+        const float ti = tn > 1e-20f ? 1.f / tn : 0.f;
+        const float er = orr - tv.x * ti, ei = oii - tv.y * ti;
+        lsum += (double)(wgt * (er * er + ei * ei)) * inv_n;
+        // d out: 2 wgt e / n; through out = y/|y|: (g - out (out.g)) / |y|
+        const float gr = (float)(2.0 * inv_n) * wgt * er, gi = (float)(2.0 * inv_n) * wgt * ei;
+        const float dot = orr * gr + oii * gi;
+        dh[p] = make_float2((gr - orr * dot) * inv, (gi - oii * dot) * inv);
     }
-    if (target) {
-        red[tid] = lsum;
+    red[tid] = lsum;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (tid < s) red[tid] += red[tid + s];
         __syncthreads();
-        for (int s = kL7Seg / 2; s > 0; s >>= 1) {
-            if (tid < s) red[tid] += red[tid + s];
-            __syncthreads();
-        }
-        if (tid == 0) part[blockIdx.x] = red[0];
     }
+    if (tid == 0) part[blockIdx.x] = red[0];
 }
 
 // dL/da6 through layer 7, masked by ReLU'(a6): g6[p][ci] = [a6 > 0] *
@@ -716,27 +751,35 @@ __global__ void sur_adam_kernel(float *__restrict__ w, const float *__restrict__
 
 __device__ __forceinline__ float bf16_round(float f) { return __bfloat162float(__float2bfloat16_rn(f)); }
 
-// Element index in the packed B operand of one layer: tap t = 3 dy + dx, K
-// index k (input channel of the layer), N index n (output channel):
-// [dx][kc = k / 16][h = (k / 8) % 2][row 32 (2 - dy) + n][k % 8].
-__device__ __forceinline__ int sur_bpack_index(int t, int k, int n)
+// Element index in the packed B operand (layout of SurTc<NOUT>): tap
+// t = 3 dy + dx, K index k (input channel of the layer), N index n (output
+// channel): [dx][kc = k / 16][h = (k / 8) % 2][row NOUT (2 - dy) + n][k % 8].
+template <int NOUT> __device__ __forceinline__ int sur_bpack_index(int t, int k, int n)
 {
     const int dy = t / 3, dx = t % 3;
-    return ((dx * 2 + k / 16) * 2 + (k / 8) % 2) * kSurBRows * 8 + (32 * (2 - dy) + n) * 8 + k % 8;
+    return ((dx * 2 + k / 16) * 2 + (k / 8) % 2) * SurTc<NOUT>::BROWS * 8 + (NOUT * (2 - dy) + n) * 8 + k % 8;
 }
 
 // From the FP32 master parameters (per layer W[co][ci][3][3] then b[co]):
 //   pk_fwd[l] with B[n = co][k = ci] and pk_bwd[l] with B[n = ci][k = co] of
 //   the flipped tap 8 - t (the transposed, flipped kernel of the
-//   backward-data pass) for the six tensor-core layers; BF16-rounded FP32
-//   copies of layers 0 and 7.
+//   backward-data pass) for the six tensor-core layers; pk7 (if not null,
+//   zeroed beforehand) with B[n = co < 2][k = ci] of the last layer; BF16-
+//   rounded FP32 copies of layers 0 and 7.
 __global__ void sur_pack_kernel(const float *__restrict__ master, uint16_t *__restrict__ pk_fwd,
-                                uint16_t *__restrict__ pk_bwd, float *__restrict__ w0r, float *__restrict__ w7r)
+                                uint16_t *__restrict__ pk_bwd, float *__restrict__ w0r, float *__restrict__ w7r,
+                                uint16_t *__restrict__ pk7)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < 576) w0r[i] = bf16_round(master[i]);
     const int off7 = kSurL0Params + 6 * kSurL32Params;
-    if (i < 576) w7r[i] = bf16_round(master[off7 + i]);
+    if (i < 576) {
+        w7r[i] = bf16_round(master[off7 + i]);
+        if (pk7) {
+            const __nv_bfloat16 h = __float2bfloat16_rn(master[off7 + i]);
+            pk7[sur_bpack_index<16>(i % 9, (i / 9) % 32, i / 288)] = *reinterpret_cast<const uint16_t *>(&h);
+        }
+    }
     if (i >= 6 * 9216) return;
     const int l = i / 9216, e = i % 9216;
     const int co = e / 288, ci = (e / 9) % 32, t = e % 9;
@@ -744,9 +787,9 @@ __global__ void sur_pack_kernel(const float *__restrict__ master, uint16_t *__re
     const __nv_bfloat16 h = __float2bfloat16_rn(wv);
     const uint16_t bits = *reinterpret_cast<const uint16_t *>(&h);
     // forward: B[n = 32 (2 - dy) + co][k = ci] of tap t = 3 dy + dx
-    pk_fwd[(size_t)l * 9216 + sur_bpack_index(t, ci, co)] = bits;
+    pk_fwd[(size_t)l * 9216 + sur_bpack_index<32>(t, ci, co)] = bits;
     // backward data: B[n = 32 (2 - dy') + ci][k = co] of the flipped tap t' = 8 - t
-    pk_bwd[(size_t)l * 9216 + sur_bpack_index(8 - t, co, ci)] = bits;
+    pk_bwd[(size_t)l * 9216 + sur_bpack_index<32>(8 - t, co, ci)] = bits;
 }
 
 // Gather training crops: x[b] = pool_x[idx[b]][oy:oy+h, ox:ox+w] (complex),

@@ -12,23 +12,24 @@ struct SurNet {
     bool training = false;
     cudaStream_t stream = nullptr;
     // parameters: FP32 master, BF16 operand images of layers 1..6 (forward and
-    // transposed/flipped for backward-data), BF16-rounded layers 0 and 7
+    // transposed/flipped for backward-data) and of layer 7, BF16-rounded
+    // layers 0 and 7
     float *d_master = nullptr;
-    uint16_t *d_pk_fwd = nullptr, *d_pk_bwd = nullptr;
+    uint16_t *d_pk_fwd = nullptr, *d_pk_bwd = nullptr, *d_pk7 = nullptr;
     float *d_w0r = nullptr, *d_w7r = nullptr;
-    SurL0W h_w0;  // host copies of layers 0 and 7 (kernel-parameter weights)
-    SurL7W h_w7;
+    SurL0W h_w0;  // host copy of layer 0 (kernel-parameter weights)
     // activations [B][H][W][32] BF16: training keeps a0..a6, inference ping-pongs two
     uint16_t *d_act[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     // training
     uint16_t *d_g[2] = {nullptr, nullptr};  // gradients w.r.t. pre-activations
-    float2 *d_dh = nullptr, *d_out = nullptr;
+    float2 *d_dh = nullptr, *d_out = nullptr, *d_y = nullptr;  // y = z + h7 before the renormalisation
     float *d_grad = nullptr, *d_m = nullptr, *d_v = nullptr, *d_part = nullptr;
     double *d_lpart = nullptr, *d_loss = nullptr;
     int nb32 = 0, nbs = 0, adam_t = 0;
     int *d_err = nullptr;
     CUtensorMap map_fwd[7], map_bwd[7];        // conv inputs (box 128 + 2d)
     CUtensorMap map_fwd_out[7], map_bwd_out[7];  // conv outputs (32-pixel tiles)
+    CUtensorMap map7;                            // the last layer's input a6
 
     int init(int batch, int width, int height, const int *dilations, bool train);
     void release();
@@ -45,8 +46,8 @@ struct SurNet {
     int adam(float lr, float b1, float b2, float eps);
     int check_error();
     int rows_grid() const;
-    int l7_grid() const;
-    int launch_l7(const float2 *z, float2 *outp, const float2 *target, float2 *dhp, double *partp);
+    // the last layer on the tensor cores: out = y/|y| into outp, or y into yp
+    int last(const float2 *z, float2 *outp, float2 *yp);
 };
 
 }  // namespace glsu
