@@ -269,26 +269,49 @@ __global__ void __launch_bounds__(kDpraTX *kDpraTY)
         pr[7 * NE + e] = ff_mul(di, ds);
     }
     __syncthreads();
-    for (int e = tid; e < 8 * NH; e += kDpraTX * kDpraTY) {
-        const int k = e / NH, rem = e - k * NH, r = rem / kDpraTX, c = rem - r * kDpraTX;
-        const ff *src = pr + k * NE + r * SW + c;
-        ff acc = {0.f, 0.f};
+    // box sums as running sums over segments of kSeg outputs: the first sum
+    // of a segment in full, each next one by adding the entering value and
+    // subtracting the leaving one (about 2 float-float additions per output
+    // instead of 2R + 1); horizontal sums of every halo row, then vertical
+    // sums into ps (the products are not read again)
+    constexpr int kSeg = 8;
+    constexpr int NSX = kDpraTX / kSeg, NSY = kDpraTY / kSeg;
+    for (int e = tid; e < 8 * G::SH * NSX; e += kDpraTX * kDpraTY) {
+        const int sg = e % NSX, rest = e / NSX, r = rest % G::SH, k = rest / G::SH;
+        const ff *src = pr + k * NE + r * SW + sg * kSeg;
+        ff *dst = hs + k * NH + r * kDpraTX + sg * kSeg;
+        ff acc = src[0];
 #pragma unroll
-        for (int dx = 0; dx <= 2 * R; dx++) acc = ff_add(acc, src[dx]);
-        hs[e] = acc;
+        for (int dx = 1; dx <= 2 * R; dx++) acc = ff_add(acc, src[dx]);
+        dst[0] = acc;
+#pragma unroll
+        for (int c = 1; c < kSeg; c++) {
+            acc = ff_sub(ff_add(acc, src[c + 2 * R]), src[c - 1]);
+            dst[c] = acc;
+        }
+    }
+    __syncthreads();
+    ff *ps = pr;  // [8][kDpraTY][kDpraTX]
+    for (int e = tid; e < 8 * kDpraTX * NSY; e += kDpraTX * kDpraTY) {
+        const int c = e % kDpraTX, rest = e / kDpraTX, sg = rest % NSY, k = rest / NSY;
+        const ff *src = hs + k * NH + sg * kSeg * kDpraTX + c;
+        ff *dst = ps + (k * kDpraTY + sg * kSeg) * kDpraTX + c;
+        ff acc = src[0];
+#pragma unroll
+        for (int dy = 1; dy <= 2 * R; dy++) acc = ff_add(acc, src[dy * kDpraTX]);
+        dst[0] = acc;
+#pragma unroll
+        for (int y = 1; y < kSeg; y++) {
+            acc = ff_sub(ff_add(acc, src[(y + 2 * R) * kDpraTX]), src[(y - 1) * kDpraTX]);
+            dst[y * kDpraTX] = acc;
+        }
     }
     __syncthreads();
     const int gx = x0 + tx, gy = y0 + ty;
     if (gx >= W || gy >= H) return;
     ff P[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-        const ff *src = hs + k * NH + ty * kDpraTX + tx;
-        ff acc = {0.f, 0.f};
-#pragma unroll
-        for (int dy = 0; dy <= 2 * R; dy++) acc = ff_add(acc, src[dy * kDpraTX]);
-        P[k] = acc;
-    }
+    for (int k = 0; k < 8; k++) P[k] = ps[(k * kDpraTY + ty) * kDpraTX + tx];
     const int m0 = max(gy - R, 0), m1 = min(gy + R, H - 1);
     const int n0 = max(gx - R, 0), n1 = min(gx + R, W - 1);
     const float cnt = (float)((m1 - m0 + 1) * (n1 - n0 + 1));
