@@ -93,8 +93,14 @@ struct glsu_dpra {
     cudaStream_t s_in = nullptr, s_out = nullptr;
     void *d_seq_img1 = nullptr, *d_ring[2] = {nullptr, nullptr};
     cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
-    // surrogate form: network output, probes, per-tile fallback
+    // surrogate form: network output, probes, per-tile fallback.  The
+    // probes' exact WFF2 sweep runs on s_probe concurrently with the network
+    // (fork after the LS stage, join before the residuals); ev_p time it.
     SurNet *sur = nullptr;
+    cudaStream_t s_probe = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_p[2] = {nullptr, nullptr};
+    bool probe_overlap = true;
+    int overlap_conv_ctas = 0;  // cap of tensor-core CTAs per SM while the probe sweep runs beside them (0: none)
     void *d_filt = nullptr;  // complex H*W: the filtered field (surrogate, then fallback tiles)
     int sur_tile = 0, sur_patch = 0, sur_ntx = 0, sur_nty = 0;
     double sur_tol = 0;
@@ -524,6 +530,17 @@ static void dpra_surrogate_release(glsu_dpra *h)
         delete h->sur;
         h->sur = nullptr;
     }
+    if (h->s_probe) {
+        cudaStreamSynchronize(h->s_probe);
+        cudaStreamDestroy(h->s_probe);
+        h->s_probe = nullptr;
+    }
+    cudaEvent_t *evs[] = {&h->ev_fork, &h->ev_join, &h->ev_p[0], &h->ev_p[1]};
+    for (cudaEvent_t *e : evs)
+        if (*e) {
+            cudaEventDestroy(*e);
+            *e = nullptr;
+        }
     cudaFree(h->d_filt);
     cudaFree(h->probe.partial);
     cudaFree(h->probe.sites);
@@ -535,20 +552,40 @@ static void dpra_surrogate_release(glsu_dpra *h)
     h->probe = ProbeOut();
 }
 
-// Surrogate form of one frame after the LS stage (d_z): network -> probes ->
-// plain WFF2 on flagged tiles -> phase update.  Stage events: ev[0] before
-// the network, ev[6] after its layer 0, ev[7] after its six tensor-core
-// layers, ev[1] after the network, ev[2] after the probes, ev[3] after
-// fallback and update.
+// Surrogate form of one frame after the LS stage (d_z): the exact WFF2 probe
+// sweep forks onto s_probe and runs beside the network; the residuals join
+// behind it, then plain WFF2 on flagged tiles and the phase update.  Stage
+// events: ev[0] before the network, ev[6] after its layer 0, ev[7] after its
+// six tensor-core layers, ev[1] after the network, ev[2] after the join and
+// the residuals, ev[3] after fallback and update; ev_p around the sweep.
 static int dpra_surrogate_frame(glsu_dpra *h, cudaEvent_t *ev)
 {
+    const bool probe = h->sur_tol > 0;
+    const bool overlap = probe && h->probe_overlap;
+    if (overlap) {
+        GLSU_CUDA_TRY(cudaEventRecord(h->ev_fork, h->stream));
+        GLSU_CUDA_TRY(cudaStreamWaitEvent(h->s_probe, h->ev_fork, 0));
+        if (ev) GLSU_CUDA_TRY(cudaEventRecord(h->ev_p[0], h->s_probe));
+        GLSU_TRY(h->wff.enqueue_probe_sweep(h->s_probe, h->d_z, h->sur_tile, h->sur_patch, (uint32_t)h->frames_done,
+                                            h->probe));
+        if (ev) GLSU_CUDA_TRY(cudaEventRecord(h->ev_p[1], h->s_probe));
+        GLSU_CUDA_TRY(cudaEventRecord(h->ev_join, h->s_probe));
+    }
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[0], h->stream));
     h->sur->stream = h->stream;
+    h->sur->conv_ctas_per_sm = overlap ? h->overlap_conv_ctas : 0;
     GLSU_TRY(h->sur->forward(h->d_z, h->d_filt, ev ? ev + 6 : nullptr));
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[1], h->stream));
-    if (h->sur_tol > 0) {
-        GLSU_TRY(h->wff.enqueue_probe(h->stream, h->d_z, h->d_filt, h->sur_tile, h->sur_patch,
-                                      (uint32_t)h->frames_done, h->sur_tol, h->probe));
+    if (probe) {
+        if (overlap) {
+            GLSU_CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
+        } else {
+            if (ev) GLSU_CUDA_TRY(cudaEventRecord(h->ev_p[0], h->stream));
+            GLSU_TRY(h->wff.enqueue_probe_sweep(h->stream, h->d_z, h->sur_tile, h->sur_patch,
+                                                (uint32_t)h->frames_done, h->probe));
+            if (ev) GLSU_CUDA_TRY(cudaEventRecord(h->ev_p[1], h->stream));
+        }
+        GLSU_TRY(h->wff.enqueue_probe_resid(h->stream, h->d_filt, h->sur_tol, h->probe));
         if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[2], h->stream));
         TileMask m;
         m.flags = h->probe.flags;
@@ -565,6 +602,16 @@ static int dpra_surrogate_frame(glsu_dpra *h, cudaEvent_t *ev)
     GLSU_TRY(launch_dpra_update(h->prec, h->d_filt, h->d_phi[GLSU_PHI_REF], h->unwrap ? nullptr : h->d_phi[GLSU_DPHI_REF],
                                 h->d_phi[GLSU_PHI_CURR], h->d_phi[GLSU_DPHI], h->W * h->H, h->stream));
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[3], h->stream));
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_set_probe_overlap(glsu_dpra *h, int enable, int conv_ctas_per_sm)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    if (conv_ctas_per_sm < 0) return fail(GLSU_ERR_INVALID, "negative CTA cap");
+    GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->probe_overlap = enable != 0;
+    h->overlap_conv_ctas = conv_ctas_per_sm;
     return GLSU_OK;
 }
 
@@ -604,6 +651,11 @@ extern "C" int glsu_dpra_set_surrogate(glsu_dpra *h, const float *h_params, cons
             cudaMalloc(&h->probe.rows, nt * h->wff.nfx * probe_rows_elems(s_inst) * sizeof(float2)) != cudaSuccess)
             rc = fail(GLSU_ERR_ALLOC, "allocation failed");
         if (rc == GLSU_OK) rc = h->wff.alloc_tile_list();
+        if (rc == GLSU_OK && (cudaStreamCreateWithFlags(&h->s_probe, cudaStreamNonBlocking) != cudaSuccess ||
+                              cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+                              cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+                              cudaEventCreate(&h->ev_p[0]) != cudaSuccess || cudaEventCreate(&h->ev_p[1]) != cudaSuccess))
+            rc = fail(GLSU_ERR_CUDA, "probe stream or event creation failed");
         if (rc == GLSU_OK && (cudaMemset(h->probe.counts, 0, 2 * sizeof(int)) != cudaSuccess ||
                               cudaMemset(h->probe.resid, 0, nt * sizeof(float)) != cudaSuccess))
             rc = fail(GLSU_ERR_CUDA, "memset failed");
@@ -869,6 +921,12 @@ extern "C" int glsu_dpra_stage_times(glsu_dpra *h, float *ms, int n)
     // surrogate form: the network split into layer 0, layers 1-6, layer 7
     const cudaEvent_t net[4] = {h->ev[0], h->ev[6], h->ev[7], h->ev[1]};
     for (int j = 0; j < 3 && k < n; j++, k++) GLSU_CUDA_TRY(cudaEventElapsedTime(&ms[k], net[j], net[j + 1]));
+    // and the probe sweep on its own (beside the network when overlapped)
+    if (k < n && h->sur_tol > 0) {
+        GLSU_CUDA_TRY(cudaStreamSynchronize(h->s_probe));
+        GLSU_CUDA_TRY(cudaEventElapsedTime(&ms[k], h->ev_p[0], h->ev_p[1]));
+        k++;
+    }
     return k;
 }
 

@@ -148,6 +148,12 @@ struct WffPlan {
     // |WFF2| >= 0.1, flag when above tol.
     int enqueue_probe(cudaStream_t s, const void *d_f, const void *d_cmp, int tile, int P, uint32_t seed,
                       double tol, const ProbeOut &o);
+    // The same in two parts: the exact patches (row and column passes) on
+    // one stream, then the residuals and flags (after the sweep, e.g. on
+    // another stream behind an event).
+    int enqueue_probe_sweep(cudaStream_t s, const void *d_f, int tile, int P, uint32_t seed, const ProbeOut &o);
+    int enqueue_probe_resid(cudaStream_t s, const void *d_cmp, double tol, const ProbeOut &o);
+    int probe_parts = 0, probe_P = 0, probe_ntiles = 0;  // set by the last sweep
 
     // Column sweep by shared-memory FFTs (FP32 form; see wff_colfft.cu).
     int method = GLSU_METHOD_AUTO;  // GLSU_METHOD_AUTO / DIRECT / FFT
@@ -196,6 +202,7 @@ struct SurConvArgs {
     // last layer: y = z + conv + bias; cout = y / |y| (inference) or yout = y (training)
     const float2 *z = nullptr;
     float2 *cout = nullptr, *yout = nullptr;
+    int max_ctas_per_sm = 0;  // 0: as many as fit; else a cap (room for a concurrent kernel)
 };
 // Weights of the first (CUDA-core) layer, passed to its kernel by value
 // (a shared-memory copy read once per FMA made it load-bound).

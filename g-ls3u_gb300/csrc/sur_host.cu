@@ -34,6 +34,7 @@ int SurNet::last(const float2 *z, float2 *outp, float2 *yp)
     a.z = z;
     a.cout = outp;
     a.yout = yp;
+    a.max_ctas_per_sm = conv_ctas_per_sm;
     return launch_sur_last(map7, a, stream);
 }
 
@@ -161,6 +162,7 @@ int SurNet::hidden(const float2 *z, cudaEvent_t *ev)
         a.out = training ? d_act[l] : d_act[l & 1];
         a.relu = 1;
         a.err = d_err;
+        a.max_ctas_per_sm = conv_ctas_per_sm;
         GLSU_TRY(launch_sur_conv(map_fwd[l], map_fwd_out[l], a, stream));
     }
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[1], stream));

@@ -445,7 +445,8 @@ static int launch_sur_conv_t(const CUtensorMap &tm, const CUtensorMap &tmo, cons
     const int by_regs = 65536 / (8 * warp_regs);
     const int by_smem = (228 * 1024) / (smem + 1024);
     const int by_tmem = 512 / SurTc<NOUT>::TMEM_COLS;
-    const int per_sm = std::max(1, std::min(std::min(by_regs, by_smem), by_tmem));
+    int per_sm = std::max(1, std::min(std::min(by_regs, by_smem), by_tmem));
+    if (a.max_ctas_per_sm > 0) per_sm = std::min(per_sm, a.max_ctas_per_sm);
     const int items = sur_conv_items(a.B, a.H, a.W, a.dil);
     const int grid = std::min(items, per_sm * sms);
     sur_conv_tc_kernel<NOUT><<<grid, 256, smem, s>>>(tm, tmo, a, items);

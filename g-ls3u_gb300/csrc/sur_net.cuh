@@ -26,6 +26,7 @@ struct SurNet {
     float *d_grad = nullptr, *d_m = nullptr, *d_v = nullptr, *d_part = nullptr;
     double *d_lpart = nullptr, *d_loss = nullptr;
     int nb32 = 0, nbs = 0, adam_t = 0;
+    int conv_ctas_per_sm = 0;  // cap of the tensor-core layers' CTAs per SM (0: none)
     int *d_err = nullptr;
     CUtensorMap map_fwd[7], map_bwd[7];        // conv inputs (box 128 + 2d)
     CUtensorMap map_fwd_out[7], map_bwd_out[7];  // conv outputs (32-pixel tiles)

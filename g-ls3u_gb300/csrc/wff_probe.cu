@@ -331,9 +331,7 @@ static int sm_count()
     return n;
 }
 
-template <int S>
-static int launch_probe(const WffPlan &Pl, ProbeArgs a, cudaStream_t s, const ProbeOut &o, const void *d_cmp,
-                        double tol)
+template <int S> static int launch_probe_sweep(WffPlan &Pl, ProbeArgs a, cudaStream_t s)
 {
     using G = ProbeGeom<S>;
     static bool attr = false;
@@ -362,14 +360,14 @@ static int launch_probe(const WffPlan &Pl, ProbeArgs a, cudaStream_t s, const Pr
     wff_probe_kernel<S><<<dim3(ntiles, Pl.nfx, a.nsplit), G::THREADS, G::SMEM, s>>>(
         a, probe_taps<S>(Pl.gy, Pl.sy, Pl.inv_norm), probe_taps<S>(Pl.gy, Pl.sy, 1.0),
         probe_taps<S>(Pl.gx, Pl.sx, Pl.scale * Pl.inv_norm));
-    wff_probe_resid_kernel<<<ntiles, 64, 0, s>>>(o.partial, o.sites, Pl.nfx * a.nsplit, G::P, a.W, a.H,
-                                                 (const float2 *)d_cmp, (float)tol, o.resid, o.flags, o.counts);
     GLSU_CUDA_TRY(cudaGetLastError());
+    Pl.probe_parts = Pl.nfx * a.nsplit;
+    Pl.probe_P = G::P;
+    Pl.probe_ntiles = ntiles;
     return GLSU_OK;
 }
 
-int WffPlan::enqueue_probe(cudaStream_t s, const void *d_f, const void *d_cmp, int tile, int P, uint32_t seed,
-                           double tol, const ProbeOut &o)
+int WffPlan::enqueue_probe_sweep(cudaStream_t s, const void *d_f, int tile, int P, uint32_t seed, const ProbeOut &o)
 {
     if (prec != GLSU_F32) return fail(GLSU_ERR_UNSUPPORTED, "the WFF2 probe runs in FP32");
     const int S = std::max(sxi, syi);
@@ -398,11 +396,27 @@ int WffPlan::enqueue_probe(cudaStream_t s, const void *d_f, const void *d_cmp, i
     a.rows = o.rows;
     if (!o.rows || !o.partial || !o.sites) return fail(GLSU_ERR_INVALID, "probe buffers not allocated");
     switch (S) {
-    case 12: return launch_probe<12>(*this, a, s, o, d_cmp, tol);
-    case 20: return launch_probe<20>(*this, a, s, o, d_cmp, tol);
-    case 30: return launch_probe<30>(*this, a, s, o, d_cmp, tol);
-    default: return launch_probe<45>(*this, a, s, o, d_cmp, tol);
+    case 12: return launch_probe_sweep<12>(*this, a, s);
+    case 20: return launch_probe_sweep<20>(*this, a, s);
+    case 30: return launch_probe_sweep<30>(*this, a, s);
+    default: return launch_probe_sweep<45>(*this, a, s);
     }
+}
+
+int WffPlan::enqueue_probe_resid(cudaStream_t s, const void *d_cmp, double tol, const ProbeOut &o)
+{
+    if (probe_parts <= 0) return fail(GLSU_ERR_INVALID, "probe residual without a probe sweep");
+    wff_probe_resid_kernel<<<probe_ntiles, 64, 0, s>>>(o.partial, o.sites, probe_parts, probe_P, W, H,
+                                                       (const float2 *)d_cmp, (float)tol, o.resid, o.flags, o.counts);
+    GLSU_CUDA_TRY(cudaGetLastError());
+    return GLSU_OK;
+}
+
+int WffPlan::enqueue_probe(cudaStream_t s, const void *d_f, const void *d_cmp, int tile, int P, uint32_t seed,
+                           double tol, const ProbeOut &o)
+{
+    GLSU_TRY(enqueue_probe_sweep(s, d_f, tile, P, seed, o));
+    return enqueue_probe_resid(s, d_cmp, tol, o);
 }
 
 }  // namespace glsu

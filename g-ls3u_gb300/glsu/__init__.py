@@ -162,6 +162,7 @@ def lib() -> ctypes.CDLL:
             "glsu_sur_conv32": ([c_void_p, c_void_p, c_int, c_int, c_int, c_int, fltp, fltp, c_int, c_void_p,
                                  c_void_p], c_int),
             "glsu_dpra_set_surrogate": ([c_void_p, fltp, intp, c_int, c_int, c_double], c_int),
+            "glsu_dpra_set_probe_overlap": ([c_void_p, c_int, c_int], c_int),
             "glsu_dpra_surrogate_stats": ([c_void_p, ctypes.POINTER(ctypes.c_longlong),
                                            ctypes.POINTER(ctypes.c_longlong), fltp, intp], c_int),
             "glsu_dpra_lsq_device": ([c_void_p, c_void_p], c_int),
@@ -454,11 +455,16 @@ class DPRA:
         check(lib().glsu_dpra_stage_timing(self._h, int(enable)))
 
     def stage_times(self):
-        """Stage times (ms) of the last frame: 4 stages, plus the network's
-        layer 0 / tensor-core layers / layer 7 split in the surrogate form."""
-        ms = (ctypes.c_float * 7)()
-        n = check(lib().glsu_dpra_stage_times(self._h, ms, 7))
+        """Stage times (ms) of the last frame: 4 stages, plus in the surrogate
+        form the network's layer 0 / tensor-core layers / layer 7 split and
+        the probe sweep on its own stream."""
+        ms = (ctypes.c_float * 8)()
+        n = check(lib().glsu_dpra_stage_times(self._h, ms, 8))
         return list(ms[:n])
+
+    def set_probe_overlap(self, enable: bool = True, conv_ctas_per_sm: int = 0):
+        """Surrogate form: probe sweep beside the network on a second stream."""
+        check(lib().glsu_dpra_set_probe_overlap(self._h, int(enable), int(conv_ctas_per_sm)))
 
 
 class AIA:

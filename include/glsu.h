@@ -234,10 +234,12 @@ int glsu_dpra_set_method(glsu_dpra *h, int method);
 int glsu_dpra_stage_timing(glsu_dpra *h, int enable);
 /* Device times (ms) of the stages of the last frame.  Plain form: [0] LS
  * solve, [1] WFF row pass, [2] WFF column sweep, [3] WFF final row pass +
- * phase update.  Surrogate form: [0] LS solve, [1] network, [2] WFF2 probes,
- * [3] fallback + phase update, then the network split into [4] layer 0,
- * [5] the six tensor-core layers, [6] layer 7.  Returns the number of
- * stages written (at most n). */
+ * phase update.  Surrogate form: [0] LS solve, [1] network, [2] from the end
+ * of the network to the probe residuals (with the probe sweep overlapped:
+ * only the part of the sweep the network did not hide), [3] fallback + phase
+ * update, then the network split into [4] layer 0, [5] the six tensor-core
+ * layers, [6] layer 7, and [7] the probe sweep on its own stream.  Returns the
+ * number of stages written (at most n). */
 int glsu_dpra_stage_times(glsu_dpra *h, float *ms, int n);
 
 /* ---- spatial unwrapping: MatLab/fp_unwrapping.m ------------------------- */
@@ -324,6 +326,13 @@ int glsu_dpra_set_surrogate(glsu_dpra *h, const float *h_params, const int *dila
 /* Cumulative probe counts; h_resid (optional, one float per tile, tiles
  * row-major) gets the last frame's residuals and h_sites (optional, two ints
  * per tile) the (row, col) of the last frame's probe patches.  Synchronous. */
+/* Surrogate form: run the probes' exact WFF2 sweep on a second stream beside
+ * the network (enable != 0, the default) with the network's tensor-core
+ * layers capped at conv_ctas_per_sm CTAs per SM (0, the default: no cap; 1
+ * reserves room on each SM for a probe CTA), or after it on one stream.
+ * Measured at 1024^2: 0.580 ms a frame overlapped without a cap, 0.582 with
+ * a cap of 2, 0.660 with a cap of 1, 0.613 on one stream. */
+int glsu_dpra_set_probe_overlap(glsu_dpra *h, int enable, int conv_ctas_per_sm);
 int glsu_dpra_surrogate_stats(glsu_dpra *h, long long *tiles_probed, long long *tiles_flagged, float *h_resid,
                               int *h_sites);
 
