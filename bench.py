@@ -65,7 +65,7 @@ PLAIN_LAUNCHES, SUR_LAUNCHES = 4, 15
 SUR_CONV_BYTES_PER_PX, SUR_CONV_FLOPS_PER_PX = 128, 2 * 288 * 32
 # DRAM bytes (read + write) of one sur_conv_tc_kernel launch at 1024x1024,
 # from the ncu capture summarised in profiles/sur_conv_tc_kernel_1024.md
-SUR_CONV_TRAFFIC_1024 = 67.349760e6 + 18.997248e6
+SUR_CONV_TRAFFIC_1024 = 67.170304e6 + 21.358592e6
 SIZE = 1024
 RADIUS = 3
 WFF = (10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)
@@ -274,7 +274,7 @@ def timed_frames(glsu, torch, d, dfr, nfr, args, stream, flush, world, local):
     update), L2 flushed before each frame outside the events; max over ranks.
     The timed frames run without the handle's stage events (they cost about
     17 us a frame); STAGE_FRAMES further frames of the sequence, run with the
-    events, give the per-stage split."""
+    events and with the stages one after another, give the per-stage split."""
     d.stage_timing(False)
     for k in range(args.warmup):
         d.per_frame_device(dfr[k % nfr].data_ptr(), glsu.F32)
@@ -297,6 +297,11 @@ def timed_frames(glsu, torch, d, dfr, nfr, args, stream, flush, world, local):
     clk = clocks.stop()
     barrier(world)
     max_ms = reduce_max(sum(a.elapsed_time(b) for a, b in evs), world)
+    # the stage split with the stages one after another (surrogate form: the
+    # probe sweep not overlapped), so that each kernel is timed on its own
+    overlap = hasattr(d, "set_probe_overlap") and getattr(d, "_surrogate", False)
+    if overlap:
+        d.set_probe_overlap(False)
     d.stage_timing(True)
     stage = None
     for k in range(STAGE_FRAMES):
@@ -307,6 +312,8 @@ def timed_frames(glsu, torch, d, dfr, nfr, args, stream, flush, world, local):
         st = np.array(d.stage_times())
         stage = st if stage is None else stage + st
     d.stage_timing(False)
+    if overlap:
+        d.set_probe_overlap(True)
     return world * args.steps / (max_ms / 1e3), max_ms, stage / STAGE_FRAMES, clk
 
 
@@ -459,12 +466,12 @@ def run_ours(args, rank, world, local):
         acc = surrogate_accuracy(glsu, torch, dfr, phi0, wp, params, dil, min(6, nfr - 1))
         sur = {"frames_per_s": s_val, "ms_per_step": s_ms / args.steps, "speedup_vs_plain": s_val / p_val,
                "e2e_frames_per_s": s_e2e,
-               "stages_ms": {"dpra_ls": s_st[0], "network": s_st[1], "probe_tail_and_residuals": s_st[2],
+               "stages_ms": {"dpra_ls": s_st[0], "network": s_st[1], "wff2_probe_and_residuals": s_st[2],
                              "fallback_and_update": s_st[3]},
                "network_ms": {"layer0": s_st[4], "tensor_core_layers_1_6": s_st[5], "layer7": s_st[6]},
                "wff2_probe_sweep_ms": s_st[7],
-               "probe_overlap": "the probe sweep runs on a second stream beside the network; "
-                                "probe_tail_and_residuals is the part of it the network does not hide",
+               "probe_overlap": "in the timed frames the probe sweep runs on a second stream beside the "
+                                "network; the stage split is taken with the stages one after another",
                "fallback_fraction_timed": flagged / probed if probed else None,
                "probe": {"tile": SUR_TILE, "patch": SUR_PATCH, "tol_rad": SUR_TOL},
                "dilations": dil, "params": int(params.size),

@@ -428,12 +428,14 @@ class DPRA:
         plain WFF2.  ``params=None`` restores the plain form."""
         if params is None:
             check(lib().glsu_dpra_set_surrogate(self._h, None, None, 0, 0, 0.0))
+            self._surrogate = False
             return
         p = np.ascontiguousarray(params, np.float32)
         d = np.ascontiguousarray(dilations, np.int32)
         check(lib().glsu_dpra_set_surrogate(self._h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
                                             d.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), tile, patch,
                                             float(tol)))
+        self._surrogate = tol > 0
 
     def surrogate_stats(self, ntiles: int = 0):
         """(tiles probed, tiles recomputed by the plain WFF2[, last residuals,
