@@ -229,10 +229,15 @@ __device__ __forceinline__ void dpra_solve_ff(const ff *P, float mi, float cnt, 
 }
 
 template <int R> struct FfGeom {
-    static constexpr int SW = kDpraTX + 2 * R, SH = kDpraTY + 2 * R, NE = SW * SH, NH = SH * kDpraTX;
+    static constexpr int SW = kDpraTX + 2 * R, SH = kDpraTY + 2 * R;
+    // odd row strides (in float-float elements): the running-sum passes walk
+    // rows with consecutive threads, which then meet distinct bank pairs
+    static constexpr int SWP = SW | 1, HSP = kDpraTX + 1;
+    static constexpr int NE = SWP * SH, NH = SH * HSP;
     // per halo element 8 float-float values (C-1, S, I-I_t and the five
     // products), per horizontal sum 8 float-float
     static constexpr size_t SMEM = sizeof(ff) * (8 * (size_t)NE + 8 * (size_t)NH);
+    static_assert(NE >= kDpraTX * kDpraTY, "the vertical sums reuse the product buffer");
 };
 
 template <typename IMG, int R>
@@ -241,17 +246,17 @@ __global__ void __launch_bounds__(kDpraTX *kDpraTY)
                       int H)
 {
     using G = FfGeom<R>;
-    constexpr int SW = G::SW, NE = G::NE, NH = G::NH;
+    constexpr int SW = G::SW, SWP = G::SWP, HSP = G::HSP, NE = G::NE, NH = G::NH;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    ff *pr = reinterpret_cast<ff *>(smem_raw);  // [8][NE]: C-1, S, I-I_t, CC, SS, CS, IC, IS
-    ff *hs = pr + 8 * NE;                       // [8][NH] horizontal sums
+    ff *pr = reinterpret_cast<ff *>(smem_raw);  // [8][SH][SWP]: C-1, S, I-I_t, CC, SS, CS, IC, IS
+    ff *hs = pr + 8 * NE;                       // [8][SH][HSP] horizontal sums
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kDpraTX + tx;
     const int x0 = blockIdx.x * kDpraTX, y0 = blockIdx.y * kDpraTY;
     const size_t cid = (size_t)min(y0 + kDpraTY / 2, H - 1) * W + min(x0 + kDpraTX / 2, W - 1);
     const float phit = phiref[cid];
     const float mi = (float)img[cid];
-    for (int e = tid; e < NE; e += kDpraTX * kDpraTY) {
-        const int r = e / SW, c = e - r * SW;
+    for (int e0 = tid; e0 < G::SH * SW; e0 += kDpraTX * kDpraTY) {
+        const int r = e0 / SW, c = e0 - r * SW, e = r * SWP + c;
         const int gy = y0 - R + r, gx = x0 - R + c;
         ff dc = {0.f, 0.f}, ds = {0.f, 0.f}, di = {0.f, 0.f};
         if (gy >= 0 && gy < H && gx >= 0 && gx < W) {
@@ -277,9 +282,9 @@ __global__ void __launch_bounds__(kDpraTX *kDpraTY)
     constexpr int kSeg = 8;
     constexpr int NSX = kDpraTX / kSeg, NSY = kDpraTY / kSeg;
     for (int e = tid; e < 8 * G::SH * NSX; e += kDpraTX * kDpraTY) {
-        const int sg = e % NSX, rest = e / NSX, r = rest % G::SH, k = rest / G::SH;
-        const ff *src = pr + k * NE + r * SW + sg * kSeg;
-        ff *dst = hs + k * NH + r * kDpraTX + sg * kSeg;
+        const int r = e % G::SH, rest = e / G::SH, sg = rest % NSX, k = rest / NSX;
+        const ff *src = pr + k * NE + r * SWP + sg * kSeg;
+        ff *dst = hs + k * NH + r * HSP + sg * kSeg;
         ff acc = src[0];
 #pragma unroll
         for (int dx = 1; dx <= 2 * R; dx++) acc = ff_add(acc, src[dx]);
@@ -294,15 +299,15 @@ __global__ void __launch_bounds__(kDpraTX *kDpraTY)
     ff *ps = pr;  // [8][kDpraTY][kDpraTX]
     for (int e = tid; e < 8 * kDpraTX * NSY; e += kDpraTX * kDpraTY) {
         const int c = e % kDpraTX, rest = e / kDpraTX, sg = rest % NSY, k = rest / NSY;
-        const ff *src = hs + k * NH + sg * kSeg * kDpraTX + c;
+        const ff *src = hs + k * NH + sg * kSeg * HSP + c;
         ff *dst = ps + (k * kDpraTY + sg * kSeg) * kDpraTX + c;
         ff acc = src[0];
 #pragma unroll
-        for (int dy = 1; dy <= 2 * R; dy++) acc = ff_add(acc, src[dy * kDpraTX]);
+        for (int dy = 1; dy <= 2 * R; dy++) acc = ff_add(acc, src[dy * HSP]);
         dst[0] = acc;
 #pragma unroll
         for (int y = 1; y < kSeg; y++) {
-            acc = ff_sub(ff_add(acc, src[(y + 2 * R) * kDpraTX]), src[(y - 1) * kDpraTX]);
+            acc = ff_sub(ff_add(acc, src[(y + 2 * R) * HSP]), src[(y - 1) * HSP]);
             dst[y * kDpraTX] = acc;
         }
     }
