@@ -111,6 +111,36 @@ def test_mixed_tiles_come_from_the_right_path(glsu, synth):
     print("tol %.3f: %d of %d tiles recomputed" % (tol, flagged.sum(), len(resid)))
 
 
+def test_probe_overlap_gives_the_serial_result(glsu, synth):
+    """The probe sweep on its own stream beside the network (the default), on
+    one stream after it, and beside it with the handle on a caller's stream:
+    the same phases bit for bit and the same tile decisions."""
+    torch = _torch()
+    p = _params(glsu)
+    frames, phi0, _ = synth.sequence(H, W, 4, seed=21)
+    res = []
+    for mode in ("overlap", "serial", "user_stream"):
+        d = glsu.DPRA(phi0.astype(np.float32), 1, 3, "f32", glsu.WffParams(*WP))
+        d.set_surrogate(p, DIL, TILE, PATCH, 0.3)
+        if mode == "serial":
+            d.set_probe_overlap(False)
+        if mode == "user_stream":
+            st = torch.cuda.Stream()
+            d.set_stream(st.cuda_stream)
+        out = []
+        for f in frames[1:]:
+            dphi, _ = d.per_frame(f)
+            out.append(dphi)
+            d.update_ref_phi()
+        out.append(np.asarray(d.surrogate_stats()))
+        d.close()
+        res.append(out)
+    for other in res[1:]:
+        for a, b in zip(res[0], other):
+            assert np.array_equal(a, b)
+    print("probed, recomputed:", res[0][-1])
+
+
 def test_surrogate_form_rejects_fp64_and_bad_patches(glsu):
     d = glsu.DPRA(np.zeros((32, 32)), 1, 1, "f64", glsu.WffParams(*WP))
     with pytest.raises(glsu.GlsuError) as e:
