@@ -101,6 +101,18 @@ struct glsu_dpra {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_p[2] = {nullptr, nullptr};
     bool probe_overlap = true;
     int overlap_conv_ctas = 0;  // cap of tensor-core CTAs per SM while the probe sweep runs beside them (0: none)
+    // CUDA-graph replay of the per-frame work (opt-in): one executable graph
+    // per (input buffer, image type, parity of the exchanged phase buffers)
+    struct FrameGraph {
+        const void *in = nullptr;
+        int type = -1, parity = -1;
+        cudaGraphExec_t exec = nullptr;
+    };
+    bool use_graph = false;
+    int phi_parity = 0;  // flips with every exchange of the reference / current buffers
+    FrameGraph graphs[4];
+    int graph_next = 0;
+    bool graph_warm = false;  // one eager frame ran since the graphs were last dropped
     void *d_filt = nullptr;  // complex H*W: the filtered field (surrogate, then fallback tiles)
     int sur_tile = 0, sur_patch = 0, sur_ntx = 0, sur_nty = 0;
     double sur_tol = 0;
@@ -406,9 +418,25 @@ extern "C" int glsu_wff_set_method(glsu_wff *h, int method)
     return set_method(h->plan, method);
 }
 
+// Executable frame graphs capture the handle's configuration and buffers:
+// every change of either drops them.
+static void dpra_drop_graphs(glsu_dpra *h)
+{
+    bool any = false;
+    for (auto &g : h->graphs) any = any || g.exec;
+    if (any && h->stream) cudaStreamSynchronize(h->stream);  // no replay of them still in flight
+    for (auto &g : h->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = glsu_dpra::FrameGraph();
+    }
+    h->graph_next = 0;
+    h->graph_warm = false;
+}
+
 extern "C" int glsu_dpra_set_method(glsu_dpra *h, int method)
 {
     if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    dpra_drop_graphs(h);
     return set_method(h->wff, method);
 }
 
@@ -477,6 +505,7 @@ extern "C" int glsu_dpra_destroy(glsu_dpra *h)
 {
     if (!h) return GLSU_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    dpra_drop_graphs(h);
     h->wff.release();
     cudaFree(h->d_img);
     cudaFree(h->d_z);
@@ -507,6 +536,7 @@ extern "C" int glsu_dpra_destroy(glsu_dpra *h)
 extern "C" int glsu_dpra_set_stream(glsu_dpra *h, void *stream)
 {
     if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    dpra_drop_graphs(h);
     if (h->own_stream && h->stream) {
         cudaStreamSynchronize(h->stream);
         cudaStreamDestroy(h->stream);
@@ -548,6 +578,7 @@ static void dpra_surrogate_release(glsu_dpra *h)
     cudaFree(h->probe.flags);
     cudaFree(h->probe.counts);
     cudaFree(h->probe.rows);
+    cudaFree(h->probe.seed);
     h->d_filt = nullptr;
     h->probe = ProbeOut();
 }
@@ -608,6 +639,7 @@ static int dpra_surrogate_frame(glsu_dpra *h, cudaEvent_t *ev)
 extern "C" int glsu_dpra_set_probe_overlap(glsu_dpra *h, int enable, int conv_ctas_per_sm)
 {
     if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    dpra_drop_graphs(h);
     if (conv_ctas_per_sm < 0) return fail(GLSU_ERR_INVALID, "negative CTA cap");
     GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
     h->probe_overlap = enable != 0;
@@ -619,6 +651,7 @@ extern "C" int glsu_dpra_set_surrogate(glsu_dpra *h, const float *h_params, cons
                                        int patch, double tol)
 {
     if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    dpra_drop_graphs(h);
     GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
     dpra_surrogate_release(h);
     if (!h_params) return GLSU_OK;
@@ -648,7 +681,8 @@ extern "C" int glsu_dpra_set_surrogate(glsu_dpra *h, const float *h_params, cons
             cudaMalloc(&h->probe.resid, nt * sizeof(float)) != cudaSuccess ||
             cudaMalloc(&h->probe.flags, nt * sizeof(int)) != cudaSuccess ||
             cudaMalloc(&h->probe.counts, 2 * sizeof(int)) != cudaSuccess ||
-            cudaMalloc(&h->probe.rows, nt * h->wff.nfx * probe_rows_elems(s_inst) * sizeof(float2)) != cudaSuccess)
+            cudaMalloc(&h->probe.rows, nt * h->wff.nfx * probe_rows_elems(s_inst) * sizeof(float2)) != cudaSuccess ||
+            cudaMalloc(&h->probe.seed, sizeof(uint32_t)) != cudaSuccess)
             rc = fail(GLSU_ERR_ALLOC, "allocation failed");
         if (rc == GLSU_OK) rc = h->wff.alloc_tile_list();
         if (rc == GLSU_OK && (cudaStreamCreateWithFlags(&h->s_probe, cudaStreamNonBlocking) != cudaSuccess ||
@@ -657,6 +691,7 @@ extern "C" int glsu_dpra_set_surrogate(glsu_dpra *h, const float *h_params, cons
                               cudaEventCreate(&h->ev_p[0]) != cudaSuccess || cudaEventCreate(&h->ev_p[1]) != cudaSuccess))
             rc = fail(GLSU_ERR_CUDA, "probe stream or event creation failed");
         if (rc == GLSU_OK && (cudaMemset(h->probe.counts, 0, 2 * sizeof(int)) != cudaSuccess ||
+                              cudaMemset(h->probe.seed, 0, sizeof(uint32_t)) != cudaSuccess ||
                               cudaMemset(h->probe.resid, 0, nt * sizeof(float)) != cudaSuccess))
             rc = fail(GLSU_ERR_CUDA, "memset failed");
     }
@@ -684,10 +719,10 @@ extern "C" int glsu_dpra_surrogate_stats(glsu_dpra *h, long long *tiles_probed, 
     return GLSU_OK;
 }
 
-extern "C" int glsu_dpra_per_frame_device(glsu_dpra *h, const void *d_img, int img_type, void *d_dphi)
+// The device work of one frame on the handle's stream(s): LS, then the plain
+// or surrogate form, then the optional unwrapping.
+static int dpra_enqueue_frame(glsu_dpra *h, const void *d_img, int img_type)
 {
-    if (!h || !d_img) return fail(GLSU_ERR_INVALID, "null argument");
-    GLSU_TRY(dpra_check_type(h, img_type));
     cudaEvent_t *ev = h->timing ? h->ev : nullptr;
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[4], h->stream));
     GLSU_TRY(launch_dpra_ls(h->prec, img_type, d_img, h->d_phi[GLSU_PHI_REF], h->d_z, h->W, h->H, h->r, h->stream,
@@ -700,6 +735,72 @@ extern "C" int glsu_dpra_per_frame_device(glsu_dpra *h, const void *d_img, int i
     if (h->unwrap)
         GLSU_TRY(launch_unwrap(h->prec, h->d_phi[GLSU_DPHI], h->d_phi[GLSU_DPHI_REF], h->W, h->H, h->unwrap_row,
                                h->unwrap_col, h->stream));
+    return GLSU_OK;
+}
+
+// Graph mode: the frame's work captured once per (input buffer, type,
+// parity) and replayed.  Inputs outside the handle's own frame buffers are
+// copied into its first one.
+static int dpra_graph_frame(glsu_dpra *h, const void *d_img, int img_type)
+{
+    const void *in = d_img;
+    if (in != h->d_img && in != h->d_seq_img1) {
+        GLSU_CUDA_TRY(cudaMemcpyAsync(h->d_img, d_img, elem_size(img_type) * (size_t)h->W * h->H,
+                                      cudaMemcpyDeviceToDevice, h->stream));
+        in = h->d_img;
+    }
+    glsu_dpra::FrameGraph *g = nullptr;
+    for (auto &c : h->graphs)
+        if (c.exec && c.in == in && c.type == img_type && c.parity == h->phi_parity) g = &c;
+    if (!g) {
+        g = &h->graphs[h->graph_next];
+        h->graph_next = (h->graph_next + 1) % 4;
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        *g = glsu_dpra::FrameGraph();
+        GLSU_CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = dpra_enqueue_frame(h, in, img_type);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+        if (rc != GLSU_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture of a frame");
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate of a frame");
+        g->in = in;
+        g->type = img_type;
+        g->parity = h->phi_parity;
+        g->exec = exec;
+    }
+    GLSU_CUDA_TRY(cudaGraphLaunch(g->exec, h->stream));
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_set_graph(glsu_dpra *h, int enable)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    dpra_drop_graphs(h);
+    h->use_graph = enable != 0;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_per_frame_device(glsu_dpra *h, const void *d_img, int img_type, void *d_dphi)
+{
+    if (!h || !d_img) return fail(GLSU_ERR_INVALID, "null argument");
+    GLSU_TRY(dpra_check_type(h, img_type));
+    // The first frame after a configuration change runs eagerly, so that
+    // one-time host work (kernel attributes, the automatic threshold) stays
+    // out of the capture; the legacy default stream cannot be captured.
+    if (h->use_graph && !h->timing && h->graph_warm && h->stream) {
+        GLSU_TRY(dpra_graph_frame(h, d_img, img_type));
+    } else {
+        GLSU_TRY(dpra_enqueue_frame(h, d_img, img_type));
+        h->graph_warm = true;
+    }
     h->synced = false;
     h->frames_done++;
     if (d_dphi) {
@@ -745,6 +846,7 @@ extern "C" int glsu_dpra_update_ref_phi(glsu_dpra *h)
     // state without the copies.
     std::swap(h->d_phi[GLSU_PHI_REF], h->d_phi[GLSU_PHI_CURR]);
     std::swap(h->d_phi[GLSU_DPHI_REF], h->d_phi[GLSU_DPHI]);
+    h->phi_parity ^= 1;
     h->synced = true;
     return GLSU_OK;
 }
@@ -772,6 +874,7 @@ extern "C" int glsu_dpra_get(glsu_dpra *h, int which, void *h_out)
 extern "C" int glsu_dpra_set_ls_method(glsu_dpra *h, int method)
 {
     if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    dpra_drop_graphs(h);
     if (method != GLSU_LS_FLOAT_FLOAT && method != GLSU_LS_FP64_SUMS)
         return fail(GLSU_ERR_INVALID, "unknown least-squares method");
     h->ls_method = method;
@@ -887,6 +990,7 @@ extern "C" int glsu_dpra_sequence(glsu_dpra *h, int nframes, const void *h_frame
 extern "C" int glsu_dpra_set_unwrap(glsu_dpra *h, int enable, int start_row, int start_col)
 {
     if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    dpra_drop_graphs(h);
     if (start_row >= h->H || start_col >= h->W) return fail(GLSU_ERR_INVALID, "unwrap start outside the image");
     if (h->W > 4096 || h->H > 4096) return fail(GLSU_ERR_UNSUPPORTED, "unwrap supports sides up to 4096");
     h->unwrap = enable != 0;
@@ -905,6 +1009,7 @@ extern "C" int glsu_unwrap2_device(int precision, void *d_p, int width, int heig
 extern "C" int glsu_dpra_stage_timing(glsu_dpra *h, int enable)
 {
     if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    dpra_drop_graphs(h);
     h->timing = enable != 0;
     return GLSU_OK;
 }

@@ -88,6 +88,8 @@ struct ProbeOut {
     int *flags = nullptr;       // [ntiles] residual > tolerance
     int *counts = nullptr;      // [2] cumulative: tiles probed, tiles flagged
     float2 *rows = nullptr;     // [ntiles][nfx][probe_rows_elems]: row-filtered input of each (tile, wx)
+    uint32_t *seed = nullptr;   // frame counter on the device: the patch positions' hash seed (null: the
+                                // seed argument of the sweep)
 };
 
 // ---------------------------------------------------------------------------

@@ -70,6 +70,7 @@ struct ProbeArgs {
     float2 *partial;  // [ntiles][nfx * nsplit][P*P]
     int2 *sites;
     float2 *rows;     // [ntiles][nfx][RYP][RXP]: R of each (tile, wx)
+    const uint32_t *seed_dev;  // not null: the seed is read here (a frame counter on the device)
 };
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x)
@@ -107,6 +108,7 @@ __global__ void __launch_bounds__(ProbeGeom<S>::RTHREADS) wff_probe_rows_kernel(
     float2 *es = fs + CR * FXS;  // [FX] e^{-j wx x}
     const int t = blockIdx.x, i = blockIdx.y, tid = threadIdx.x;
     const int rl = tid % CR, seg = tid / CR;
+    if (a.seed_dev) a.seed = *a.seed_dev;
     const int2 site = probe_site(a, t);
     const int py = site.x, px = site.y;
     const float2 *exi = a.ex + (size_t)i * (a.pitch + 2 * kPhasorPad) + kPhasorPad;
@@ -167,6 +169,7 @@ __global__ void __launch_bounds__(ProbeGeom<S>::THREADS) wff_probe_kernel(ProbeA
     const int t = blockIdx.x, i = blockIdx.y, part = blockIdx.z, tid = threadIdx.x;
     const int lane = tid & 31, w = tid >> 5, cg = w % G::NCG, rg = w / G::NCG;
     const int col = cg * 32 + lane;
+    if (a.seed_dev) a.seed = *a.seed_dev;
     const int2 site = probe_site(a, t);
     if (i == 0 && part == 0 && tid == 0) a.sites[t] = site;
     const int py = site.x, px = site.y;
@@ -266,7 +269,7 @@ __global__ void __launch_bounds__(64) wff_probe_resid_kernel(const float2 *__res
                                                              const int2 *__restrict__ sites, int nparts, int P,
                                                              int W, int H, const float2 *__restrict__ cmp, float tol,
                                                              float *__restrict__ resid, int *__restrict__ flags,
-                                                             int *__restrict__ counts)
+                                                             int *__restrict__ counts, uint32_t *__restrict__ seed)
 {
     __shared__ float s_se[2];
     __shared__ int s_n[2];
@@ -307,6 +310,8 @@ __global__ void __launch_bounds__(64) wff_probe_resid_kernel(const float2 *__res
         flags[t] = r > tol ? 1 : 0;
         atomicAdd(&counts[0], 1);
         if (r > tol) atomicAdd(&counts[1], 1);
+        // the sweep kernels of this frame have read the seed: advance it for the next frame
+        if (t == 0 && seed) atomicAdd(seed, 1u);
     }
 }
 
@@ -394,6 +399,7 @@ int WffPlan::enqueue_probe_sweep(cudaStream_t s, const void *d_f, int tile, int 
     a.partial = o.partial;
     a.sites = o.sites;
     a.rows = o.rows;
+    a.seed_dev = o.seed;
     if (!o.rows || !o.partial || !o.sites) return fail(GLSU_ERR_INVALID, "probe buffers not allocated");
     switch (S) {
     case 12: return launch_probe_sweep<12>(*this, a, s);
@@ -407,7 +413,8 @@ int WffPlan::enqueue_probe_resid(cudaStream_t s, const void *d_cmp, double tol, 
 {
     if (probe_parts <= 0) return fail(GLSU_ERR_INVALID, "probe residual without a probe sweep");
     wff_probe_resid_kernel<<<probe_ntiles, 64, 0, s>>>(o.partial, o.sites, probe_parts, probe_P, W, H,
-                                                       (const float2 *)d_cmp, (float)tol, o.resid, o.flags, o.counts);
+                                                       (const float2 *)d_cmp, (float)tol, o.resid, o.flags, o.counts,
+                                                       o.seed);
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
 }

@@ -163,6 +163,7 @@ def lib() -> ctypes.CDLL:
                                  c_void_p], c_int),
             "glsu_dpra_set_surrogate": ([c_void_p, fltp, intp, c_int, c_int, c_double], c_int),
             "glsu_dpra_set_probe_overlap": ([c_void_p, c_int, c_int], c_int),
+            "glsu_dpra_set_graph": ([c_void_p, c_int], c_int),
             "glsu_dpra_surrogate_stats": ([c_void_p, ctypes.POINTER(ctypes.c_longlong),
                                            ctypes.POINTER(ctypes.c_longlong), fltp, intp], c_int),
             "glsu_dpra_lsq_device": ([c_void_p, c_void_p], c_int),
@@ -463,6 +464,10 @@ class DPRA:
         ms = (ctypes.c_float * 8)()
         n = check(lib().glsu_dpra_stage_times(self._h, ms, 8))
         return list(ms[:n])
+
+    def set_graph(self, enable: bool = True):
+        """Replay each frame's device work as a captured CUDA graph."""
+        check(lib().glsu_dpra_set_graph(self._h, int(enable)))
 
     def set_probe_overlap(self, enable: bool = True, conv_ctas_per_sm: int = 0):
         """Surrogate form: probe sweep beside the network on a second stream."""

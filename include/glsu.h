@@ -230,6 +230,13 @@ int glsu_dpra_device_ptr(glsu_dpra *h, int which, void **d_ptr);
 int glsu_dpra_set_unwrap(glsu_dpra *h, int enable, int start_row, int start_col);
 /* Column-sweep method of the handle's WFF2 (GLSU_METHOD_*). */
 int glsu_dpra_set_method(glsu_dpra *h, int method);
+/* Graph mode (off by default): from the second frame on, the device work of
+ * a frame is captured once as a CUDA graph (per input buffer, image type and
+ * parity of the exchanged reference buffers) and replayed, which takes the
+ * host's per-launch cost out of each frame; device-pointer inputs outside the
+ * handle's own buffers are first copied into its frame buffer.  Results are
+ * identical to the eager path.  Stage timing runs eagerly. */
+int glsu_dpra_set_graph(glsu_dpra *h, int enable);
 /* Record CUDA events between the stages of each frame (off by default). */
 int glsu_dpra_stage_timing(glsu_dpra *h, int enable);
 /* Device times (ms) of the stages of the last frame.  Plain form: [0] LS

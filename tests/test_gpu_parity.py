@@ -356,3 +356,53 @@ def test_dpra_with_unwrapping_matches_matlab_semantics(glsu, oracle, synth):
         assert np.abs(dphi - ref).max() < 1e-9
         d.update_ref_phi()
     d.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("surrogate", [False, True])
+@pytest.mark.parametrize("rr", [1, 2])
+def test_graph_mode_equals_eager(glsu, synth, surrogate, rr):
+    """Frames replayed from captured CUDA graphs (host frames, device frames at
+    arbitrary addresses, u8 and f32) give the eager path's phases bit for bit,
+    across reference updates and a configuration change."""
+    import torch
+    from glsu import train_surrogate as T
+    H, W = 96, 136
+    frames, phi0, _ = synth.sequence(H, W, 7, seed=8)
+    wp = glsu.WffParams(4.0, -0.5, 0.5, 0.25, 4.0, -0.5, 0.5, 0.25, 0.2)
+    params, dil = T.init_params(3, scale_last=1.0), [1, 2, 4, 8, 16, 8, 4, 1]
+    out = []
+    for graph in (False, True):
+        d = glsu.DPRA(phi0.astype(np.float32), rr, 2, "f32", wp)
+        if surrogate:
+            d.set_surrogate(params, dil, 64, 8, 0.1)
+        d.set_graph(graph)
+        res = []
+        dev = torch.from_numpy(frames.astype(np.float32)).cuda()
+        for k, f in enumerate(frames[1:], start=1):
+            if k == 4:
+                d.set_ls_method(glsu.LS_FP64_SUMS)  # drops the captured graphs
+            if k % 3 == 0:
+                dphi, _ = d.per_frame(np.clip(f * 255, 0, 255).astype(np.uint8))
+            elif k % 3 == 1:
+                dphi, _ = d.per_frame(f.astype(np.float32))
+            else:
+                d.per_frame_device(dev[k].data_ptr(), glsu.F32)
+                dphi = d.get(glsu.DPHI)
+            res.append((dphi.copy(), d.get(glsu.PHI_CURR).copy()))
+            if k % rr == 0:
+                d.update_ref_phi()
+        # the sequence API: pageable (per frame) and page-locked (pipelined,
+        # two input slots) buffers
+        seq, _ = d.sequence(frames[1:4].astype(np.float32))
+        res.append((seq, d.get(glsu.PHI_REF).copy()))
+        pin_in = torch.from_numpy(frames[1:5].astype(np.float32)).pin_memory()
+        pin_out = torch.empty((4, H, W), dtype=torch.float32).pin_memory()
+        d.sequence_ptr(4, pin_in.data_ptr(), glsu.F32, pin_out.data_ptr())
+        res.append((pin_out.numpy().copy(), d.get(glsu.PHI_REF).copy()))
+        if surrogate:
+            res.append((np.asarray(d.surrogate_stats()), np.zeros(1)))
+        d.close()
+        out.append(res)
+    for (a1, b1), (a2, b2) in zip(*out):
+        assert np.array_equal(a1, a2) and np.array_equal(b1, b2)
