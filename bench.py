@@ -122,6 +122,8 @@ def workload_config(size):
         "dpra_window": 2 * RADIUS + 1,
         "wff": {"sigma": WFF[0], "wl": WFF[1], "wh": WFF[2], "wi": WFF[3], "thr": WFF[8], "n_freq": NFX * NFY},
         "surrogate": {"tile": SUR_TILE, "probe_patch": SUR_PATCH, "tol_rad": SUR_TOL},
+        "frame_launch": "each handle in graph mode: a frame's kernels (both streams of the surrogate form) "
+                        "captured once as a CUDA graph and replayed; the stage-split frames run eagerly",
         "l2": "flushed before every timed step (256 MiB device write outside the timed events)",
         "e2e_path": "glsu_dpra_sequence over K consecutive pinned host frames after W warm-up frames on a "
                     "fresh handle (H2D, D2H on their own streams, overlapped with neighbouring frames); L2 "
@@ -432,12 +434,14 @@ def run_ours(args, rank, world, local):
     # ---- plain form: DPRA LS -> WFF2 -> update
     dp = glsu.DPRA(phi0.astype(np.float32), 1, RADIUS, "f32", wp)
     dp.set_stream(stream.cuda_stream)
+    dp.set_graph(True)
     p_val, p_ms, p_st, p_clk = timed_frames(glsu, torch, dp, dfr, nfr, args, stream, flush, world, local)
     dp.close()
 
     def plain_handle():
         h = glsu.DPRA(phi0.astype(np.float32), 1, RADIUS, "f32", wp)
         h.set_stream(stream.cuda_stream)
+        h.set_graph(True)
         return h
 
     p_e2e = e2e_sequence(glsu, torch, plain_handle, frames, args, stream, flush, world)
@@ -453,6 +457,7 @@ def run_ours(args, rank, world, local):
         ds = glsu.DPRA(phi0.astype(np.float32), 1, RADIUS, "f32", wp)
         ds.set_stream(stream.cuda_stream)
         ds.set_surrogate(params, dil, SUR_TILE, SUR_PATCH, SUR_TOL)
+        ds.set_graph(True)
         s_val, s_ms, s_st, s_clk = timed_frames(glsu, torch, ds, dfr, nfr, args, stream, flush, world, local)
         probed, flagged = ds.surrogate_stats()
         ds.close()
