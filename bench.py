@@ -342,18 +342,24 @@ def e2e_sequence(glsu, torch, make_handle, frames, args, stream, flush, world):
 
 
 def surrogate_accuracy(glsu, torch, dfr, phi0, wp, params, dil, nframes):
-    """Teacher-forced phase error of the surrogate form against the plain FP32
-    WFF2 of the same least-squares output (per frame, all pixels), and of the
-    raw least-squares phase (no filtering) for comparison."""
+    """Teacher-forced phase error of the surrogate form (per frame, all pixels)
+    against the FP64 G-LS3U frame from the same reference phase (FP64 DPRA
+    least squares and FP64 WFF2: the oracle's arithmetic, which the FP64
+    kernels match to 1e-11 rad), against the plain FP32 WFF2 of the same
+    least-squares output, and of the raw least-squares phase (no filtering)."""
     size = dfr.shape[-1]
     d = glsu.DPRA(phi0.astype(np.float32), 1, RADIUS, "f32", wp)
     d.set_surrogate(params, dil, SUR_TILE, SUR_PATCH, SUR_TOL)
     w = glsu.WFF2(size, size, "f32", wp)
     z = torch.empty((size, size), dtype=torch.complex64, device="cuda")
     ref = torch.empty_like(z)
-    rm, mx, rid = [], [], []
+    rm, mx, rid, rm64, mx64 = [], [], [], [], []
     for k in range(1, nframes + 1):
         pref = d.get(glsu.PHI_REF).astype(np.float64)
+        d64 = glsu.DPRA(pref, 1, RADIUS, "f64", wp)
+        d64.per_frame_device(dfr[k].data_ptr(), glsu.F32)
+        pc64 = d64.get(glsu.PHI_CURR)
+        d64.close()
         d.per_frame_device(dfr[k].data_ptr(), glsu.F32)
         d.lsq_device(z.data_ptr())
         torch.cuda.synchronize()
@@ -365,11 +371,16 @@ def surrogate_accuracy(glsu, torch, dfr, phi0, wp, params, dil, nframes):
         rm.append(float(np.sqrt(np.mean(e ** 2))))
         mx.append(float(np.abs(e).max()))
         rid.append(float(np.sqrt(np.mean(eid ** 2))))
+        e64 = np.angle(np.exp(1j * (pc - pc64)))
+        rm64.append(float(np.sqrt(np.mean(e64 ** 2))))
+        mx64.append(float(np.abs(e64).max()))
         d.update_ref_phi()
     probed, flagged = d.surrogate_stats()
     d.close()
     w.close()
-    return {"rmse_per_frame": rm, "rmse": float(np.sqrt(np.mean(np.square(rm)))), "max_abs": max(mx),
+    return {"rmse_vs_fp64": float(np.sqrt(np.mean(np.square(rm64)))), "max_abs_vs_fp64": max(mx64),
+            "rmse_vs_fp64_per_frame": rm64,
+            "rmse_per_frame": rm, "rmse": float(np.sqrt(np.mean(np.square(rm)))), "max_abs": max(mx),
             "rmse_without_network": float(np.sqrt(np.mean(np.square(rid)))), "frames": nframes,
             "tiles_probed": probed, "tiles_recomputed": flagged}
 
@@ -480,8 +491,8 @@ def run_ours(args, rank, world, local):
                "fallback_fraction_timed": flagged / probed if probed else None,
                "probe": {"tile": SUR_TILE, "patch": SUR_PATCH, "tol_rad": SUR_TOL},
                "dilations": dil, "params": int(params.size),
-               "accuracy_vs_plain_fp32": acc,
-               "rmse_target_rad": 0.02, "meets_rmse_target": acc["rmse"] <= 0.02}
+               "accuracy": acc,
+               "rmse_target_rad": 0.02, "meets_rmse_target": acc["rmse_vs_fp64"] <= 0.02}
 
     # ---- rooflines
     peaks = {}

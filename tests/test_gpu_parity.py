@@ -190,6 +190,70 @@ def test_glsu_sequence_256_matches_oracle(glsu, oracle, synth, prec):
     assert all(s_["pc_max"] < tol and s_["dp_max"] < tol and s_["pc_rms_all"] < tol for s_ in st)
 
 
+_FREE_RUN = {}
+
+
+def _oracle_free_run(oracle, frames, phi0, owp):
+    """The oracle's own free-running recursion from phi0 (dphi per frame)."""
+    key = phi0.tobytes()
+    if key not in _FREE_RUN:
+        pref, dref = phi0.astype(np.float64), np.zeros(phi0.shape)
+        out = []
+        for fr in frames:
+            opc, odp, _, _ = oracle.glsu_frame(fr.astype(np.float64), pref, dref, 3, owp)
+            out.append(odp)
+            pref, dref = opc, odp
+        _FREE_RUN[key] = np.stack(out)
+    return _FREE_RUN[key]
+
+
+def _drift(a, b):
+    """Per-frame RMS of the wrapped difference (all pixels)."""
+    e = np.angle(np.exp(1j * (a - b)))
+    return np.sqrt(np.mean(e ** 2, axis=(1, 2)))
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_glsu_sequence_256_free_running_drift(glsu, oracle, synth, prec):
+    """The whole 20-frame 256x256 sequence of the FP64 reference workload
+    (DPRA 7x7, WFF2 sigma 10, 21x21 frequencies, threshold 0.2, reference
+    update every frame), free running on the GPU and in the oracle.
+
+    The recursion feeds each frame's phase back as the next reference, and
+    on this generator it amplifies any perturbation about 2.5x per frame
+    (a 1e-9 rad perturbation of phi0 alone reaches 0.3 rad RMS after 20
+    frames in the oracle itself).  So the drift is judged against the
+    oracle's own sensitivity: FP64 within 10x of what a 4e-16 relative
+    perturbation of phi0 causes in the oracle; FP32, started from the FP32
+    phi0 that the reference's float interface passes, no more than what
+    that rounding of phi0 alone causes in the oracle.  The first frame meets
+    the per-frame tolerances (1e-10 / 1e-3 rad)."""
+    frames, phi0, _ = synth.sequence(256, 256, 20, seed=0)
+    wp = glsu.WffParams(10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)
+    owp = oracle.WffParams(*wp.tuple())
+    dt = np.float32 if prec == "f32" else np.float64
+    d = glsu.DPRA(phi0.astype(dt), 1, 3, prec, wp)
+    gpu, _ = d.sequence(frames.astype(dt))
+    d.close()
+    gpu = gpu.astype(np.float64)
+    base = _oracle_free_run(oracle, frames, phi0, owp)
+    fmt = lambda c: " ".join("%.2g" % v for v in c)
+    if prec == "f64":
+        rng = np.random.default_rng(1)
+        pert = _oracle_free_run(oracle, frames, phi0 * (1 + 4e-16 * rng.standard_normal(phi0.shape)), owp)
+        got, sens = _drift(gpu, base), _drift(pert, base)
+        print("free-running f64 drift vs oracle: %s\n  oracle, phi0 perturbed 4e-16: %s" % (fmt(got), fmt(sens)))
+        assert got[0] < F64_PHASE_TOL
+        assert np.all(got <= 10 * sens + 1e-13)
+    else:
+        o32 = _oracle_free_run(oracle, frames, phi0.astype(np.float32).astype(np.float64), owp)
+        got, sens = _drift(gpu, o32), _drift(o32, base)
+        print("free-running f32 drift vs oracle from the same phi0: %s\n  oracle, phi0 rounded to FP32: %s\n"
+              "  f32 vs oracle from the FP64 phi0: %s" % (fmt(got), fmt(sens), fmt(_drift(gpu, base))))
+        assert got[0] < F32_PHASE_TOL
+        assert np.all(got <= sens)
+
+
 def test_reference_update_rate_semantics(glsu, oracle, synth):
     frames, phi0, _ = synth.sequence(48, 40, 5, seed=9)
     wp = glsu.WffParams(3.0, -0.5, 0.5, 0.25, 3.0, -0.5, 0.5, 0.25, 0.1)
