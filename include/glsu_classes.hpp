@@ -5,6 +5,7 @@
 //   WFT_FPA::WFT::WFT2_DeviceResults[F]        WFT/WFT.h:92-135 (owns m_d_filtered and the WFR maps)
 //   DPRA::DPRA_CUDAF                            DPRA/dpra_cudaf.h:21-46
 //   DPRA::DPRA_CUDA  (empty in the reference)   DPRA/dpra_cuda.h:9-14; interface of DPRA_CPU, dpra_cpu.h:30-64
+//   DPRA::DPRA_HYBRIDF / DPRA_HYBRID            DPRA/dpra_hybridf.h:15-40, DPRA/dpra_hybrid.h:15-40
 //   AIA::AIA_CUDAF                              AIA/aia_cudaf.h:15-38
 // Aliases WFF2_CUDAF / WFF2_CUDA name the WFF-only use.
 //
@@ -179,6 +180,7 @@ class DPRA_CUDAF {
     // Current (wrapped) phase, which the reference does not expose.
     void get_phi_curr(std::vector<float> &phi) const;
     glsu_dpra *handle() const { return h_; }
+    int ref_update_rate() const { return rr_; }
 
   private:
     glsu_dpra *h_ = nullptr;
@@ -205,6 +207,54 @@ class DPRA_CUDA {
   private:
     glsu_dpra *h_ = nullptr;
     int w_, hgt_, rr_;
+};
+
+// DPRA::DPRA_HYBRIDF / DPRA_HYBRID (DPRA/dpra_hybridf.h:15-40,
+// DPRA/dpra_hybrid.h:15-40).  The reference builds the window sums on the GPU,
+// copies them to the host, solves the 3x3 systems there with LAPACKE_dsysv on
+// iNumThreads OpenMP threads and filters on the GPU again
+// (DPRA/dpra_hybrid.cpp:182-270).  Here the whole frame stays on the GPU: the
+// classes are the DPRA_CUDAF / DPRA_CUDA path with the same hard-wired 3x3
+// window and WFF parameters (DPRA/dpra_hybrid.cpp:34-36), so iNumThreads is
+// accepted and unused and the results equal those classes' bit for bit.
+class DPRA_HYBRIDF : public DPRA_CUDAF {
+  public:
+    DPRA_HYBRIDF() = delete;
+    DPRA_HYBRIDF(const DPRA_HYBRIDF &) = delete;
+    DPRA_HYBRIDF &operator=(const DPRA_HYBRIDF &) = delete;
+    DPRA_HYBRIDF(const float *v_Phi0, const int iWidth, const int iHeight, const int irefUpdateRate = 1,
+                 const int iNumThreads = 1)
+        : DPRA_CUDAF(v_Phi0, iWidth, iHeight, irefUpdateRate)
+    {
+        (void)iNumThreads;
+    }
+    using DPRA_CUDAF::operator();
+    // frames as cv::Mat (DPRA_CUDAF's takes cv::cuda::HostMem); DPRA_CPU::operator() loop
+    void operator()(const std::vector<cv::Mat> &f, std::vector<std::vector<float>> &dPhi_Sum, double &time)
+    {
+        time = 0;
+        std::vector<float> d;
+        for (size_t i = 0; i < f.size(); i++) {
+            double t = 0;
+            dpra_per_frame(f[i], d, t);
+            time += t;
+            dPhi_Sum.push_back(d);
+            if (i % ref_update_rate() == 0) update_ref_phi();
+        }
+    }
+};
+
+class DPRA_HYBRID : public DPRA_CUDA {
+  public:
+    DPRA_HYBRID() = delete;
+    DPRA_HYBRID(const DPRA_HYBRID &) = delete;
+    DPRA_HYBRID &operator=(const DPRA_HYBRID &) = delete;
+    DPRA_HYBRID(const double *v_Phi0, const int iWidth, const int iHeight, const int irefUpdateRate = 1,
+                const int iNumThreads = 1)
+        : DPRA_CUDA(v_Phi0, iWidth, iHeight, irefUpdateRate)
+    {
+        (void)iNumThreads;
+    }
 };
 
 }  // namespace DPRA

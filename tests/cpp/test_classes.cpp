@@ -1,5 +1,5 @@
 // Driver for the C++ class tests: uses the reference's class names and
-// signatures (DPRA_CUDAF, DPRA_CUDA, WFT2_CUDAF, WFF2_CUDA, AIA_CUDAF) the way
+// signatures (DPRA_CUDAF, DPRA_CUDA, DPRA_HYBRID[F], WFT2_CUDAF, WFF2_CUDA, AIA_CUDAF) the way
 // the reference's own tests and GUI do, on inputs written by
 // tests/test_cpp_classes.py, and writes the results back as raw files.
 //
@@ -77,6 +77,30 @@ int main(int argc, char **argv)
             for (auto &d : dphi) all.insert(all.end(), d.begin(), d.end());
             save(dir + "/dpra_f64_dphi.f64", all);
             std::cout << "DPRA_CUDA frames=" << dphi.size() << " time_ms=" << t << "\n";
+        }
+        // ---- DPRA_HYBRIDF / DPRA_HYBRID (reference signatures, iNumThreads) against
+        //      DPRA_CUDAF / DPRA_CUDA with the same hard-wired window and WFF parameters
+        {
+            std::vector<std::vector<float>> a, b;
+            double t = 0;
+            {
+                DPRA::DPRA_HYBRIDF hy(phi0f.data(), W, H, rr, 4);
+                hy(mats, a, t);
+            }
+            {
+                DPRA::DPRA_CUDAF cu(phi0f.data(), W, H, rr);
+                cu(mats, b, t);
+            }
+            std::vector<std::vector<double>> c, e;
+            {
+                DPRA::DPRA_HYBRID hy(phi0d.data(), W, H, rr, 4);
+                hy(mats, c, t);
+            }
+            {
+                DPRA::DPRA_CUDA cu(phi0d.data(), W, H, rr);
+                cu(mats, e, t);
+            }
+            std::cout << "DPRA_HYBRID equal=" << (a == b && c == e && a.size() == (size_t)nf) << "\n";
         }
         // ---- WFT2_CUDAF (WFF) on a device buffer, as DPRA_CUDAF uses it
         {

@@ -1,4 +1,4 @@
-"""The reference's C++ class interfaces (DPRA_CUDAF, DPRA_CUDA, WFT2_CUDAF
+"""The reference's C++ class interfaces (DPRA_CUDAF, DPRA_CUDA, DPRA_HYBRID[F], WFT2_CUDAF
 with WFT_TYPE::WFF and WFR, AIA_CUDAF) driven from a compiled C++ program
 (tests/cpp/test_classes.cpp) and checked against the FP64 oracle."""
 import os
@@ -45,6 +45,7 @@ def test_reference_class_interfaces(tmp_path, oracle, synth):
     print(out.stdout, out.stderr)
     assert out.returncode == 0
     assert "errors_caught=2" in out.stdout
+    assert "DPRA_HYBRID equal=1" in out.stdout
 
     wp = oracle.WffParams(wpar[0], wpar[1], wpar[2], wpar[3], wpar[0], wpar[1], wpar[2], wpar[3], wpar[4])
     # DPRA_CUDA (FP64): every frame against the oracle sequence
