@@ -451,6 +451,7 @@ def run_ours(args, rank, world, local):
     dp.set_stream(stream.cuda_stream)
     dp.set_graph(True)
     p_val, p_ms, p_st, p_clk = timed_frames(glsu, torch, dp, dfr, nfr, args, stream, flush, world, local)
+    p_tuning = dp.tuning()
     dp.close()
 
     def plain_handle():
@@ -580,7 +581,8 @@ def run_ours(args, rank, world, local):
         "plain": {"frames_per_s": p_val, "ms_per_step": p_ms / args.steps, "e2e_frames_per_s": p_e2e,
                   "stages_ms": {"dpra_ls": p_st[0], "wff_rows": p_st[1], "wff_column_sweep": p_st[2],
                                 "wff_final_update": p_st[3]},
-                  "roofline": plain_roof, "clocks": p_clk, "gpu_launches_per_step": PLAIN_LAUNCHES},
+                  "roofline": plain_roof, "clocks": p_clk, "gpu_launches_per_step": PLAIN_LAUNCHES,
+                  "column_sweep_autotune": p_tuning},
         "surrogate": sur,
         "wfr": wfr,
         "aia": {"frames": 5, "ms": aia_ms, "iterations": aia_iters, "err": aia_err,

@@ -241,6 +241,7 @@ extern "C" int glsu_wff_create(glsu_wff **out, int precision, int width, int hei
     if (rc == GLSU_OK) rc = h->plan.upload_tables(h->stream);
     if (rc == GLSU_OK) rc = h->plan.make_tensor_map();
     if (rc == GLSU_OK) rc = h->plan.init_colfft();
+    if (rc == GLSU_OK) rc = h->plan.autotune(h->stream);
     if (rc == GLSU_OK && (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess))
         rc = fail(GLSU_ERR_CUDA, "cudaEventCreate failed");
     if (rc != GLSU_OK) {
@@ -402,20 +403,47 @@ extern "C" int glsu_wff_threshold(glsu_wff *h, double *thr)
     return GLSU_OK;
 }
 
-static int set_method(WffPlan &P, int method)
+static int set_method(WffPlan &P, int method, cudaStream_t s)
 {
     if (method != GLSU_METHOD_AUTO && method != GLSU_METHOD_DIRECT && method != GLSU_METHOD_FFT)
         return fail(GLSU_ERR_INVALID, "unknown column-sweep method");
     if (method == GLSU_METHOD_FFT && P.fft_L == 0)
         return fail(GLSU_ERR_UNSUPPORTED, "no shared-memory FFT plan for this handle (FP64, or no transform length)");
+    GLSU_CUDA_TRY(cudaStreamSynchronize(s));
     P.method = method;
+    if (method == GLSU_METHOD_AUTO && !P.tuned) return P.autotune(s);
     return GLSU_OK;
+}
+
+static void get_tuning(const WffPlan &P, glsu_wff_tuning *t)
+{
+    t->method = P.column_method() == GLSU_METHOD_FFT && P.fft_L > 0 ? GLSU_METHOD_FFT : GLSU_METHOD_DIRECT;
+    t->fft_length = P.fft_L;
+    t->fft_columns = P.fft_nc;
+    t->fft_radix_order = P.fft_order;
+    t->tuned = P.tuned ? 1 : 0;
+    t->ms_direct = P.tune_ms_direct;
+    t->ms_fft = P.tune_ms_fft;
 }
 
 extern "C" int glsu_wff_set_method(glsu_wff *h, int method)
 {
     if (!h) return fail(GLSU_ERR_INVALID, "null handle");
-    return set_method(h->plan, method);
+    return set_method(h->plan, method, h->stream);
+}
+
+extern "C" int glsu_wff_get_tuning(const glsu_wff *h, glsu_wff_tuning *t)
+{
+    if (!h || !t) return fail(GLSU_ERR_INVALID, "null argument");
+    get_tuning(h->plan, t);
+    return GLSU_OK;
+}
+
+extern "C" int glsu_wff_set_fft_plan(glsu_wff *h, int columns_per_cta, int radix_order)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return h->plan.set_fft_plan(columns_per_cta, radix_order);
 }
 
 // Executable frame graphs capture the handle's configuration and buffers:
@@ -437,7 +465,14 @@ extern "C" int glsu_dpra_set_method(glsu_dpra *h, int method)
 {
     if (!h) return fail(GLSU_ERR_INVALID, "null handle");
     dpra_drop_graphs(h);
-    return set_method(h->wff, method);
+    return set_method(h->wff, method, h->stream);
+}
+
+extern "C" int glsu_dpra_get_tuning(const glsu_dpra *h, glsu_wff_tuning *t)
+{
+    if (!h || !t) return fail(GLSU_ERR_INVALID, "null argument");
+    get_tuning(h->wff, t);
+    return GLSU_OK;
 }
 
 extern "C" int glsu_wff_padded_size(const glsu_wff *h, int *pw, int *ph)
@@ -474,6 +509,7 @@ extern "C" int glsu_dpra_create(glsu_dpra **out, int precision, const void *h_ph
     if (rc == GLSU_OK) rc = h->wff.upload_tables(h->stream);
     if (rc == GLSU_OK) rc = h->wff.make_tensor_map();
     if (rc == GLSU_OK) rc = h->wff.init_colfft();
+    if (rc == GLSU_OK) rc = h->wff.autotune(h->stream);
     const size_t N = (size_t)width * height;
     const size_t es = precision == GLSU_F32 ? 4 : 8;
     if (rc == GLSU_OK) {

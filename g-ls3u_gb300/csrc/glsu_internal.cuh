@@ -161,14 +161,29 @@ struct WffPlan {
     int method = GLSU_METHOD_AUTO;  // GLSU_METHOD_AUTO / DIRECT / FFT
     int fft_L = 0, fft_nst = 0;     // fft_L == 0: no FFT plan, the direct kernel runs
     int fft_radix[12];
+    int fft_nc = 0;                 // columns per CTA of the FFT sweep (4 or 2)
+    int fft_order = 0;              // radix order of the stages (see fft_factor)
     void *d_khat = nullptr;         // nfy x fft_L spectra of the modulated windows
     void *d_tw = nullptr;           // fft_L twiddles e^{-2 pi i t / L}
     int init_colfft();
     void release_colfft();
-    // The FFT sweep runs when asked for: on GB300 the direct kernel is faster
-    // at the benchmark sizes (5.5 vs 9.1 ms at 1024^2 with 21x21 frequencies).
-    bool use_colfft() const { return fft_L > 0 && d_khat != nullptr && method == GLSU_METHOD_FFT; }
+    // FFT plan variant: nc columns per CTA, radix order; GLSU_ERR_UNSUPPORTED
+    // where it does not fit (the plan is then unchanged).
+    int set_fft_plan(int nc, int order);
+
+    // Autotuner (wff_colfft.cu): with GLSU_METHOD_AUTO the column sweep is
+    // the candidate (direct kernel or FFT plan variant) measured fastest for
+    // this shape, timed once per shape and process.
+    bool tuned = false;
+    int auto_method = GLSU_METHOD_DIRECT;
+    float tune_ms_direct = 0, tune_ms_fft = 0;
+    int autotune(cudaStream_t s);
+    int column_method() const { return method == GLSU_METHOD_AUTO ? auto_method : method; }
+    bool use_colfft() const { return fft_L > 0 && d_khat != nullptr && column_method() == GLSU_METHOD_FFT; }
 };
+
+// The column sweep of a full-frame run (FFT or direct, as the plan selects).
+int launch_column_sweep(WffPlan &P, cudaStream_t s);
 
 int launch_colfft(const WffPlan &P, cudaStream_t s);
 

@@ -18,7 +18,11 @@
 // two shared buffers laid out [L][NC] (NC columns per CTA, column index
 // fastest) with one float2 of padding per 16 elements against bank
 // conflicts on the strided writes of the early stages.
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "glsu_internal.cuh"
@@ -280,14 +284,28 @@ __global__ void __launch_bounds__(kFftThreads, 1) wff_colfft_kernel(const float2
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-static int factor(int n, int *rad)
+// Stage radices of a length-n transform in one of three orders (the tuner's
+// radix-plan knob): 0 = 8, 4, 2 then 5, 3; 1 = 4, 2 then 5, 3 (no radix 8);
+// 2 = 5, 3 first, then 8, 4, 2.  Returns the stage count, or -1 when n has a
+// prime factor above 5.
+static int factor(int n, int *rad, int order = 0)
 {
     int ns = 0;
-    while (n % 8 == 0) { rad[ns++] = 8; n /= 8; }
-    while (n % 4 == 0) { rad[ns++] = 4; n /= 4; }
-    while (n % 2 == 0) { rad[ns++] = 2; n /= 2; }
-    while (n % 5 == 0) { rad[ns++] = 5; n /= 5; }
-    while (n % 3 == 0) { rad[ns++] = 3; n /= 3; }
+    auto take = [&](int r) {
+        while (n % r == 0 && ns < 12) {
+            rad[ns++] = r;
+            n /= r;
+        }
+    };
+    if (order == 2) {
+        take(5);
+        take(3);
+    }
+    if (order != 1) take(8);
+    take(4);
+    take(2);
+    take(5);
+    take(3);
     return n == 1 ? ns : -1;
 }
 
@@ -311,6 +329,12 @@ static int choose_length(int need, ColFftPlan *out)
 }
 
 static int colfft_nc(int L) { return L <= 1600 ? 4 : 2; }
+static bool colfft_fits(int L, int nc, int pitch)
+{
+    const int nel = L * nc;
+    return (nc == 4 || nc == 2) && (size_t)nel <= (size_t)kFftThreads * 13 && pitch % nc == 0 &&
+           sizeof(float2) * 2 * (size_t)(nel + (nel >> 4) + 1) <= 112 * 1024;
+}
 
 int WffPlan::init_colfft()
 {
@@ -318,9 +342,11 @@ int WffPlan::init_colfft()
     ColFftPlan p;
     if (choose_length(H + 2 * sy, &p)) return GLSU_OK;  // no suitable length: direct kernel
     const int nc = colfft_nc(p.L);
-    if ((size_t)p.L * nc > (size_t)kFftThreads * 13 || pitch % nc) return GLSU_OK;  // registers per thread
+    if (!colfft_fits(p.L, nc, pitch)) return GLSU_OK;  // registers per thread, shared memory
     fft_L = p.L;
     fft_nst = p.nst;
+    fft_nc = nc;
+    fft_order = 0;
     for (int s = 0; s < p.nst; s++) fft_radix[s] = p.radix[s];
     // H_k = DFT of h_k(m) = gy(m) e^{j wy_k m}, m in [-sy, sy] placed circularly
     std::vector<float> kh(2 * (size_t)nfy * p.L), tw(2 * (size_t)p.L);
@@ -346,6 +372,21 @@ int WffPlan::init_colfft()
         return fail(GLSU_ERR_ALLOC, "cudaMalloc of the column FFT tables failed");
     GLSU_CUDA_TRY(cudaMemcpy(d_khat, kh.data(), kh.size() * sizeof(float), cudaMemcpyHostToDevice));
     GLSU_CUDA_TRY(cudaMemcpy(d_tw, tw.data(), tw.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return GLSU_OK;
+}
+
+int WffPlan::set_fft_plan(int nc, int order)
+{
+    if (fft_L == 0) return fail(GLSU_ERR_UNSUPPORTED, "no shared-memory FFT plan for this handle");
+    if (order < 0 || order > 2 || !colfft_fits(fft_L, nc, pitch))
+        return fail(GLSU_ERR_UNSUPPORTED, "FFT plan variant does not fit this transform length");
+    int rad[12];
+    const int ns = factor(fft_L, rad, order);
+    if (ns < 1 || ns > 12) return fail(GLSU_ERR_UNSUPPORTED, "transform length does not factor in that order");
+    fft_nc = nc;
+    fft_order = order;
+    fft_nst = ns;
+    for (int k = 0; k < ns; k++) fft_radix[k] = rad[k];
     return GLSU_OK;
 }
 
@@ -384,7 +425,7 @@ template <int NC, int MAXE> static int launch_colfft_t(const WffPlan &P, cudaStr
 
 int launch_colfft(const WffPlan &P, cudaStream_t s)
 {
-    const int nc = colfft_nc(P.fft_L);
+    const int nc = P.fft_nc;
     const int per = (P.fft_L * nc + kFftThreads - 1) / kFftThreads;  // elements owned per thread
     if (nc == 4) {
         if (per <= 3) return launch_colfft_t<4, 3>(P, s);
@@ -394,6 +435,99 @@ int launch_colfft(const WffPlan &P, cudaStream_t s)
     }
     if (per <= 10) return launch_colfft_t<2, 10>(P, s);
     return launch_colfft_t<2, 13>(P, s);
+}
+
+// ---------------------------------------------------------------------------
+// autotuner
+// ---------------------------------------------------------------------------
+// Candidates: the direct column kernel, and the FFT sweep with 4 or 2
+// columns per CTA and each radix order.  Each is launched once (warm-up),
+// then twice between CUDA events on the plan's own buffers; the kernels have
+// no data-dependent control flow, so the buffers' contents do not matter.
+// The FFT is taken only when at least 10% faster than the direct kernel, so
+// that near ties keep the direct kernel, and the other FFT variants are
+// tried only when the default one is within 1.5x of it.  Results are kept
+// per shape for the process, so every handle of a shape runs the same
+// kernels.  GLSU_AUTOTUNE=0 in the environment skips the timing (the direct
+// kernel).
+namespace {
+struct TuneKey {
+    int v[9];
+    bool operator<(const TuneKey &o) const { return std::lexicographical_compare(v, v + 9, o.v, o.v + 9); }
+};
+struct TuneResult {
+    int method, nc, order;
+    float ms_direct, ms_fft;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneResult> g_tune;
+}  // namespace
+
+int WffPlan::autotune(cudaStream_t s)
+{
+    tuned = true;
+    auto_method = GLSU_METHOD_DIRECT;
+    tune_ms_direct = tune_ms_fft = 0;
+    if (prec != GLSU_F32 || fft_L == 0 || d_khat == nullptr || mask.flags) return GLSU_OK;
+    const char *env = std::getenv("GLSU_AUTOTUNE");
+    if (env && env[0] == '0') return GLSU_OK;
+    const TuneKey key{{W, H, pitch, sx, sy, nfx, nfy, fft_L, (int)(1000 * p.wyl + 0.5)}};
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it == g_tune.end()) {
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+            if (e0) cudaEventDestroy(e0);
+            return fail(GLSU_ERR_CUDA, "cudaEventCreate failed");
+        }
+        const int saved = method;
+        int rc = GLSU_OK;
+        auto time_it = [&](int m, float *ms) {
+            method = m;
+            for (int k = 0; k < 3 && rc == GLSU_OK; k++) {
+                if (k == 1 && cudaEventRecord(e0, s) != cudaSuccess) rc = fail(GLSU_ERR_CUDA, "cudaEventRecord");
+                if (rc == GLSU_OK) rc = launch_column_sweep(*this, s);
+            }
+            if (rc == GLSU_OK && (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                                  cudaEventElapsedTime(ms, e0, e1) != cudaSuccess))
+                rc = fail(GLSU_ERR_CUDA, "timing a column-sweep candidate failed");
+            *ms *= 0.5f;
+        };
+        TuneResult r{GLSU_METHOD_DIRECT, fft_nc, fft_order, 0.f, 0.f};
+        time_it(GLSU_METHOD_DIRECT, &r.ms_direct);
+        float best = -1.f;
+        const int nc0 = fft_nc;
+        for (int nc : {nc0, 6 - nc0}) {
+            for (int order = 0; order < 3 && rc == GLSU_OK; order++) {
+                if (set_fft_plan(nc, order) != GLSU_OK) continue;
+                float ms = 0;
+                time_it(GLSU_METHOD_FFT, &ms);
+                if (rc == GLSU_OK && (best < 0 || ms < best)) {
+                    best = ms;
+                    r.nc = nc;
+                    r.order = order;
+                }
+                if (nc == nc0 && order == 0 && ms > 1.5f * r.ms_direct) break;
+            }
+            if (best > 1.5f * r.ms_direct) break;
+        }
+        set_error(std::string());  // variants that did not fit leave no message
+        method = saved;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (rc != GLSU_OK) {
+            set_fft_plan(nc0, 0);
+            return rc;
+        }
+        r.ms_fft = best;
+        if (best > 0 && best < 0.9f * r.ms_direct) r.method = GLSU_METHOD_FFT;
+        it = g_tune.emplace(key, r).first;
+    }
+    const TuneResult &r = it->second;
+    auto_method = r.method;
+    tune_ms_direct = r.ms_direct;
+    tune_ms_fft = r.ms_fft;
+    return set_fft_plan(r.nc, r.order);
 }
 
 }  // namespace glsu

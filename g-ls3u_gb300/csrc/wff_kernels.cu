@@ -787,6 +787,23 @@ static int launch_final(const WffPlan &P, void *d_out, const void *phiref, const
     return GLSU_OK;
 }
 
+template <typename T> static int launch_cols_any(WffPlan &P, cudaStream_t s)
+{
+    if (sizeof(T) == 4 && P.use_colfft() && !P.mask.flags) return launch_colfft(P, s);
+    switch (P.syi) {
+    case 12: return launch_cols<T, 12>(P, s);
+    case 20: return launch_cols<T, 20>(P, s);
+    case 30: return launch_cols<T, 30>(P, s);
+    case 45: return launch_cols<T, 45>(P, s);
+    default: return launch_cols<T, 60>(P, s);
+    }
+}
+
+int launch_column_sweep(WffPlan &P, cudaStream_t s)
+{
+    return P.prec == GLSU_F32 ? launch_cols_any<float>(P, s) : launch_cols_any<double>(P, s);
+}
+
 template <typename T>
 static int enqueue_t(WffPlan &P, cudaStream_t s, const void *d_f, void *d_out, int mode, const void *phiref,
                      const void *dphiref, void *phicurr, void *dphi, cudaEvent_t *ev)
@@ -803,17 +820,7 @@ static int enqueue_t(WffPlan &P, cudaStream_t s, const void *d_f, void *d_out, i
     }
     if (rc) return rc;
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[1], s));
-    if (sizeof(T) == 4 && P.use_colfft() && !P.mask.flags) {
-        rc = launch_colfft(P, s);
-    } else {
-        switch (P.syi) {
-        case 12: rc = launch_cols<T, 12>(P, s); break;
-        case 20: rc = launch_cols<T, 20>(P, s); break;
-        case 30: rc = launch_cols<T, 30>(P, s); break;
-        case 45: rc = launch_cols<T, 45>(P, s); break;
-        default: rc = launch_cols<T, 60>(P, s); break;
-        }
-    }
+    rc = launch_cols_any<T>(P, s);
     if (rc) return rc;
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[2], s));
 #define GLSU_FINAL(SS)                                                                              \

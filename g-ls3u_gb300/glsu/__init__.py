@@ -57,6 +57,15 @@ class WfrResultsC(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in WFR_FIELDS]
 
 
+class WffTuningC(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int), ("fft_length", ctypes.c_int), ("fft_columns", ctypes.c_int),
+                ("fft_radix_order", ctypes.c_int), ("tuned", ctypes.c_int), ("ms_direct", ctypes.c_float),
+                ("ms_fft", ctypes.c_float)]
+
+    def asdict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class WffParamsC(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in
                 ("sigma_x", "wxl", "wxh", "wxi", "sigma_y", "wyl", "wyh", "wyi", "thr")]
@@ -124,6 +133,9 @@ def lib() -> ctypes.CDLL:
             "glsu_wff_threshold": ([c_void_p, dblp], c_int),
             "glsu_wff_set_method": ([c_void_p, c_int], c_int),
             "glsu_dpra_set_method": ([c_void_p, c_int], c_int),
+            "glsu_wff_get_tuning": ([c_void_p, ctypes.POINTER(WffTuningC)], c_int),
+            "glsu_dpra_get_tuning": ([c_void_p, ctypes.POINTER(WffTuningC)], c_int),
+            "glsu_wff_set_fft_plan": ([c_void_p, c_int, c_int], c_int),
             "glsu_dpra_set_unwrap": ([c_void_p, c_int, c_int, c_int], c_int),
             "glsu_unwrap2_device": ([c_int, c_void_p, c_int, c_int, c_int, c_int, c_void_p], c_int),
             "glsu_wff_padded_size": ([c_void_p, intp, intp], c_int),
@@ -316,6 +328,16 @@ class WFF2:
         """Column-sweep method: METHOD_AUTO, METHOD_DIRECT or METHOD_FFT."""
         check(lib().glsu_wff_set_method(self._h, method))
 
+    def tuning(self) -> dict:
+        """The autotuner's choice for this shape (method, FFT plan, timings)."""
+        t = WffTuningC()
+        check(lib().glsu_wff_get_tuning(self._h, ctypes.byref(t)))
+        return t.asdict()
+
+    def set_fft_plan(self, columns_per_cta: int, radix_order: int):
+        """Force an FFT plan variant (4 or 2 columns per CTA; radix order 0, 1 or 2)."""
+        check(lib().glsu_wff_set_fft_plan(self._h, columns_per_cta, radix_order))
+
     @property
     def threshold(self) -> float:
         t = ctypes.c_double(0)
@@ -414,6 +436,12 @@ class DPRA:
     def set_method(self, method: int):
         """Column-sweep method of the WFF2: METHOD_AUTO, METHOD_DIRECT or METHOD_FFT."""
         check(lib().glsu_dpra_set_method(self._h, method))
+
+    def tuning(self) -> dict:
+        """The autotuner's choice for this handle's WFF2 shape."""
+        t = WffTuningC()
+        check(lib().glsu_dpra_get_tuning(self._h, ctypes.byref(t)))
+        return t.asdict()
 
     def set_ls_method(self, method: int):
         """FP32 least-squares arithmetic: LS_FLOAT_FLOAT (default) or LS_FP64_SUMS."""

@@ -54,8 +54,8 @@ extern "C" {
 /* Column-sweep method of the WFF2 (glsu_wff_set_method / glsu_dpra_set_method):
  * DIRECT convolves the columns with the truncated window; FFT (FP32 form
  * only) does the same in the frequency domain of each column with
- * shared-memory transforms; AUTO picks DIRECT, the faster of the two on
- * GB300 at the sizes measured. */
+ * shared-memory transforms; AUTO (the default) runs whichever the
+ * autotuner measured faster for the handle's shape (glsu_wff_tuning). */
 #define GLSU_METHOD_AUTO 0
 #define GLSU_METHOD_DIRECT 1
 #define GLSU_METHOD_FFT 2
@@ -120,6 +120,29 @@ int glsu_wff_threshold(glsu_wff *h, double *thr);
  * rounding.  GLSU_METHOD_FFT fails with GLSU_ERR_UNSUPPORTED where no
  * transform plan exists (FP64 handles). */
 int glsu_wff_set_method(glsu_wff *h, int method);
+/* Column-sweep autotuner.  With GLSU_METHOD_AUTO (the default) the handle
+ * runs the column sweep measured fastest for its shape: the direct kernel,
+ * or the shared-memory FFT sweep with 4 or 2 columns per CTA and one of
+ * three radix orders (0: 8,4,2,5,3; 1: 4,2,5,3; 2: 5,3,8,4,2).  The first
+ * handle of a shape in the process times the candidates at creation (a few
+ * launches each); later handles of that shape reuse the choice.  The FFT is
+ * taken only when at least 10% faster.  Setting GLSU_AUTOTUNE=0 in the
+ * environment skips the timing: AUTO is then the direct kernel.  The methods
+ * agree to FP32 rounding, not bit for bit. */
+typedef struct {
+    int method;          /* GLSU_METHOD_DIRECT or GLSU_METHOD_FFT: the sweep that runs */
+    int fft_length;      /* transform length of the FFT plan (0: no FFT plan) */
+    int fft_columns;     /* columns per CTA of the FFT sweep */
+    int fft_radix_order; /* radix order of the FFT stages (see above) */
+    int tuned;           /* 1: the autotuner resolved AUTO for this shape */
+    float ms_direct;     /* measured column-sweep time of the direct kernel (0: not timed) */
+    float ms_fft;        /* best measured time of the FFT sweep (0: not timed) */
+} glsu_wff_tuning;
+int glsu_wff_get_tuning(const glsu_wff *h, glsu_wff_tuning *t);
+/* Force an FFT plan variant (the autotuner's knobs); GLSU_ERR_UNSUPPORTED
+ * where it does not fit.  Takes effect when the FFT sweep runs. */
+int glsu_wff_set_fft_plan(glsu_wff *h, int columns_per_cta, int radix_order);
+
 /* FFT-padded plane of the reference's formulation (kept for API parity). */
 int glsu_wff_padded_size(const glsu_wff *h, int *padded_width, int *padded_height);
 
@@ -230,6 +253,8 @@ int glsu_dpra_device_ptr(glsu_dpra *h, int which, void **d_ptr);
 int glsu_dpra_set_unwrap(glsu_dpra *h, int enable, int start_row, int start_col);
 /* Column-sweep method of the handle's WFF2 (GLSU_METHOD_*). */
 int glsu_dpra_set_method(glsu_dpra *h, int method);
+/* The handle's column-sweep tuning (see glsu_wff_get_tuning). */
+int glsu_dpra_get_tuning(const glsu_dpra *h, glsu_wff_tuning *t);
 /* Graph mode (off by default): from the second frame on, the device work of
  * a frame is captured once as a CUDA graph (per input buffer, image type and
  * parity of the exchanged reference buffers) and replayed, which takes the

@@ -102,6 +102,83 @@ def test_column_method_switch(glsu):
     w.close()
 
 
+@pytest.mark.parametrize("case", [0, 2, 4])
+def test_wff_fft_plan_variants_match_oracle(glsu, oracle, case):
+    """Every FFT plan variant the autotuner may pick (4 or 2 columns per CTA,
+    radix orders 0, 1, 2) within the FP32 tolerance of the oracle."""
+    shape, p = WFF_CASES[case]
+    f = field(shape, case)
+    ref, _ = oracle.wff2(f.astype(np.complex64).astype(np.complex128), *p)
+    torch = _torch()
+    t = torch.from_numpy(np.ascontiguousarray(f, np.complex64)).cuda()
+    out = torch.empty_like(t)
+    w = glsu.WFF2(shape[1], shape[0], "f32", glsu.WffParams(*p))
+    w.set_method(glsu.METHOD_FFT)
+    ran = 0
+    for nc in (4, 2):
+        for order in (0, 1, 2):
+            try:
+                w.set_fft_plan(nc, order)
+            except glsu.GlsuError as e:
+                assert e.code == glsu.ERR_UNSUPPORTED
+                continue
+            w.run(t.data_ptr(), out.data_ptr())
+            perr, rel = compare(out.cpu().numpy(), ref)
+            print("fft plan case %d nc %d order %d: phase err %.3g, rel %.3g" % (case, nc, order, perr, rel))
+            assert perr < F32_PHASE_TOL and rel < 1e-4
+            ran += 1
+    w.close()
+    assert ran >= 3
+
+
+def test_autotuner_choices(glsu, oracle):
+    """METHOD_AUTO resolves to the column sweep measured fastest for the
+    shape, once per shape and process.  With the reference's DPRA WFF
+    parameters (sigma 20, 7x7 frequencies) the FFT sweep wins by about 3x
+    and is picked; with sigma 10 and 21x21 frequencies the direct kernel
+    wins by about 1.7x and is picked, with results bit for bit those of an
+    explicit METHOD_DIRECT handle."""
+    import os
+    torch = _torch()
+    dp = glsu.dpra_default_params()
+    f = field((512, 512), 3)
+    w = glsu.WFF2(512, 512, "f32", dp)
+    tu = w.tuning()
+    print("tuning, DPRA defaults 512^2:", tu)
+    assert tu["tuned"] == 1 and tu["method"] == glsu.METHOD_FFT and 0 < tu["ms_fft"] < tu["ms_direct"]
+    t = torch.from_numpy(np.ascontiguousarray(f, np.complex64)).cuda()
+    out = torch.empty_like(t)
+    w.run(t.data_ptr(), out.data_ptr())
+    w2 = glsu.WFF2(512, 512, "f32", dp)  # the same shape: the process's choice, not timed again
+    assert w2.tuning() == tu
+    w2.close()
+    w.close()
+    ref, _ = oracle.wff2(f.astype(np.complex64).astype(np.complex128), *dp.tuple())
+    perr, rel = compare(out.cpu().numpy(), ref)
+    assert perr < F32_PHASE_TOL and rel < 1e-4
+
+    p10 = glsu.WffParams(10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)
+    f = field((256, 256), 4)
+    a, _, _ = wff_gpu(glsu, f, "f32", p10)
+    b, _, _ = wff_gpu(glsu, f, "f32", p10, glsu.METHOD_DIRECT)
+    w = glsu.WFF2(256, 256, "f32", p10)
+    tu = w.tuning()
+    w.close()
+    print("tuning, sigma 10 21x21 256^2:", tu)
+    assert tu["method"] == glsu.METHOD_DIRECT and tu["ms_direct"] < tu["ms_fft"]
+    assert np.array_equal(a, b)
+
+    # GLSU_AUTOTUNE=0: no timing, AUTO is the direct kernel (a shape not seen before)
+    os.environ["GLSU_AUTOTUNE"] = "0"
+    try:
+        d = glsu.DPRA(np.zeros((200, 136), np.float32), 1, 1, "f32", dp)
+        tu = d.tuning()
+        d.close()
+    finally:
+        del os.environ["GLSU_AUTOTUNE"]
+    assert tu["method"] == glsu.METHOD_DIRECT and tu["ms_direct"] == 0 and tu["ms_fft"] == 0
+
+
 def test_wff_threshold_is_kept_after_first_call(glsu, oracle):
     torch = _torch()
     p = glsu.WffParams(4.0, -1, 1, 0.5, 4.0, -1, 1, 0.5, -1)
