@@ -113,6 +113,7 @@ struct glsu_dpra {
     FrameGraph graphs[4];
     int graph_next = 0;
     bool graph_warm = false;  // one eager frame ran since the graphs were last dropped
+    int batch_index = 0;      // frames run through glsu_dpra_batch_step
     void *d_filt = nullptr;  // complex H*W: the filtered field (surrogate, then fallback tiles)
     int sur_tile = 0, sur_patch = 0, sur_ntx = 0, sur_nty = 0;
     double sur_tol = 0;
@@ -1020,6 +1021,39 @@ extern "C" int glsu_dpra_sequence(glsu_dpra *h, int nframes, const void *h_frame
         if (i % h->rr == 0) GLSU_TRY(glsu_dpra_update_ref_phi(h));
     }
     if (time_ms) *time_ms = total;
+    return GLSU_OK;
+}
+
+// Batched form: one frame of each of n independent sequences (handles of any
+// sizes, windows and parameters), each enqueued on its handle's own stream so
+// that the frames are in flight together; the host returns after
+// enqueueing.  Each handle follows the sequence rule: after its i-th batched
+// frame the reference is updated when i % rr == 0.
+extern "C" int glsu_dpra_batch_step(glsu_dpra *const *handles, int n, const void *const *d_frames, int img_type)
+{
+    if (!handles || !d_frames || n < 0) return fail(GLSU_ERR_INVALID, "bad argument");
+    for (int i = 0; i < n; i++) {
+        glsu_dpra *h = handles[i];
+        if (!h || !d_frames[i]) continue;  // this sequence has ended
+        if (!h->stream) return fail(GLSU_ERR_INVALID, "batched handles need their own streams, not the legacy one");
+        for (int j = 0; j < i; j++)
+            if (handles[j] == h) return fail(GLSU_ERR_INVALID, "a handle appears twice in one batch step");
+        GLSU_TRY(glsu_dpra_per_frame_device(h, d_frames[i], img_type, nullptr));
+        if (h->batch_index++ % h->rr == 0) GLSU_TRY(glsu_dpra_update_ref_phi(h));
+    }
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_batch_wait(glsu_dpra *const *handles, int n)
+{
+    if (!handles || n < 0) return fail(GLSU_ERR_INVALID, "bad argument");
+    for (int i = 0; i < n; i++) {
+        glsu_dpra *h = handles[i];
+        if (!h) continue;
+        GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+        GLSU_TRY(h->wff.check_device_error(h->stream));
+        if (h->sur) GLSU_TRY(h->sur->check_error());
+    }
     return GLSU_OK;
 }
 

@@ -134,6 +134,8 @@ def lib() -> ctypes.CDLL:
             "glsu_wff_set_method": ([c_void_p, c_int], c_int),
             "glsu_dpra_set_method": ([c_void_p, c_int], c_int),
             "glsu_wff_get_tuning": ([c_void_p, ctypes.POINTER(WffTuningC)], c_int),
+            "glsu_dpra_batch_step": ([ctypes.POINTER(c_void_p), c_int, ctypes.POINTER(c_void_p), c_int], c_int),
+            "glsu_dpra_batch_wait": ([ctypes.POINTER(c_void_p), c_int], c_int),
             "glsu_dpra_get_tuning": ([c_void_p, ctypes.POINTER(WffTuningC)], c_int),
             "glsu_wff_set_fft_plan": ([c_void_p, c_int, c_int], c_int),
             "glsu_dpra_set_unwrap": ([c_void_p, c_int, c_int, c_int], c_int),
@@ -500,6 +502,23 @@ class DPRA:
     def set_probe_overlap(self, enable: bool = True, conv_ctas_per_sm: int = 0):
         """Surrogate form: probe sweep beside the network on a second stream."""
         check(lib().glsu_dpra_set_probe_overlap(self._h, int(enable), int(conv_ctas_per_sm)))
+
+
+def _handle_array(handles):
+    return (ctypes.c_void_p * len(handles))(*[h._h.value for h in handles])
+
+
+def dpra_batch_step(handles, d_frames, img_type: int):
+    """One frame of each of several DPRA sequences (handles of any sizes), each
+    on its handle's stream, in flight together; d_frames[i] is a device
+    pointer, or 0 / None for a sequence that has ended.  Returns without
+    waiting: call dpra_batch_wait."""
+    fs = (ctypes.c_void_p * len(handles))(*[f or None for f in d_frames])
+    check(lib().glsu_dpra_batch_step(_handle_array(handles), len(handles), fs, img_type))
+
+
+def dpra_batch_wait(handles):
+    check(lib().glsu_dpra_batch_wait(_handle_array(handles), len(handles)))
 
 
 class AIA:

@@ -220,6 +220,17 @@ int glsu_dpra_per_frame(glsu_dpra *h, const void *h_img, int img_type, void *h_d
 int glsu_dpra_per_frame_device(glsu_dpra *h, const void *d_img, int img_type, void *d_dphi);
 /* DPRA_CUDAF::update_ref_phi: phi_ref <- phi_curr, dphi_ref <- dphi. */
 int glsu_dpra_update_ref_phi(glsu_dpra *h);
+/* Batched form (no counterpart in the reference): one frame of each of n
+ * independent sequences, handles of any sizes, windows and parameters.
+ * d_frames[i] is handle i's device frame (img_type for all), or NULL when
+ * its sequence has ended.  Each frame is enqueued on its handle's own stream
+ * (so the frames are in flight together; handles in graph mode replay their
+ * graphs) and the call returns without waiting.  Each handle follows the
+ * sequence rule: after its i-th batched frame the reference is updated when
+ * i % rr == 0.  glsu_dpra_batch_wait waits for all of them and reports device
+ * errors.  A handle may appear once per step. */
+int glsu_dpra_batch_step(glsu_dpra *const *handles, int n, const void *const *d_frames, int img_type);
+int glsu_dpra_batch_wait(glsu_dpra *const *handles, int n);
 /* DPRA_CPU::operator() semantics for a block of frames: for frame i, run
  * per_frame, store its dphi, update the reference when i % rr == 0
  * (DPRA/dpra_cpu.cpp:58-89; the CUDA reference's overloads are empty,

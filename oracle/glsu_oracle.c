@@ -71,6 +71,13 @@ int or_fft_lut(int *out, int cap)
 }
 
 /* Index of the first LUT entry >= x, or -1 (WFT/WFT.cpp:10-23). */
+/* Entry i of the size table (used by the FP32 variant, glsu_oracle_f32.c). */
+int or_lut_value(int i)
+{
+    lut_init();
+    return g_lut[i];
+}
+
 int or_first_greater(int x)
 {
     lut_init();
@@ -99,157 +106,11 @@ void or_freq_grid(int W, int H, double *xf, double *yf)
         }
 }
 
-/* ------------------------------------------------------------------------ */
-/* Mixed-radix Stockham FFT (complex double, interleaved re/im).            */
-/* ------------------------------------------------------------------------ */
-typedef struct {
-    int n;
-    int nf;
-    int fac[40];
-    double *w; /* w[2t], w[2t+1] = cos, sin of (-2 pi t / n) */
-} fft_plan;
-
-static int fft_plan_init(fft_plan *p, int n)
-{
-    p->n = n;
-    p->nf = 0;
-    int t = n;
-    while (t % 4 == 0) { p->fac[p->nf++] = 4; t /= 4; }
-    while (t % 2 == 0) { p->fac[p->nf++] = 2; t /= 2; }
-    for (int r = 3; t > 1; r += 2) {
-        if (r > 64) return -1; /* radices above 64 are not supported */
-        while (t % r == 0) { p->fac[p->nf++] = r; t /= r; }
-    }
-    p->w = (double *)malloc(sizeof(double) * 2 * (size_t)n);
-    if (!p->w) return -1;
-    for (int i = 0; i < n; i++) {
-        double a = -2.0 * M_PI * (double)i / (double)n;
-        p->w[2 * i] = cos(a);
-        p->w[2 * i + 1] = sin(a);
-    }
-    return 0;
-}
-
-static void fft_plan_free(fft_plan *p)
-{
-    free(p->w);
-    p->w = NULL;
-}
-
-/* One transform of length p->n.  x and y are 2n-double buffers; the result
- * ends in x.  inverse != 0 computes the unnormalised backward transform. */
-static void fft_exec(const fft_plan *p, double *x, double *y, int inverse)
-{
-    const int n = p->n;
-    if (n == 1) return;
-    const double sgn = inverse ? -1.0 : 1.0; /* sign applied to sin() */
-    double *in = x, *out = y;
-    int Ns = 1;
-    double vr[64], vi[64], tr[64], ti[64];
-    for (int s = 0; s < p->nf; s++) {
-        const int R = p->fac[s];
-        const int nR = n / R;
-        const int tstep = n / (Ns * R);
-        for (int j = 0; j < nR; j++) {
-            const int k = j % Ns;
-            for (int r = 0; r < R; r++) {
-                vr[r] = in[2 * (j + r * nR)];
-                vi[r] = in[2 * (j + r * nR) + 1];
-            }
-            if (Ns > 1) {
-                for (int r = 1; r < R; r++) {
-                    int e = (int)(((long long)r * k * tstep) % n);
-                    double c = p->w[2 * e], sn = sgn * p->w[2 * e + 1];
-                    double a = vr[r] * c - vi[r] * sn;
-                    double b = vr[r] * sn + vi[r] * c;
-                    vr[r] = a;
-                    vi[r] = b;
-                }
-            }
-            if (R == 2) {
-                double ar = vr[0] + vr[1], ai = vi[0] + vi[1];
-                double br = vr[0] - vr[1], bi = vi[0] - vi[1];
-                tr[0] = ar; ti[0] = ai; tr[1] = br; ti[1] = bi;
-            } else if (R == 4) {
-                double s0r = vr[0] + vr[2], s0i = vi[0] + vi[2];
-                double d0r = vr[0] - vr[2], d0i = vi[0] - vi[2];
-                double s1r = vr[1] + vr[3], s1i = vi[1] + vi[3];
-                double d1r = vr[1] - vr[3], d1i = vi[1] - vi[3];
-                /* forward: multiply d1 by -i ; inverse: by +i */
-                double mr = sgn * d1i, mi = -sgn * d1r;
-                tr[0] = s0r + s1r; ti[0] = s0i + s1i;
-                tr[2] = s0r - s1r; ti[2] = s0i - s1i;
-                tr[1] = d0r + mr;  ti[1] = d0i + mi;
-                tr[3] = d0r - mr;  ti[3] = d0i - mi;
-            } else {
-                const int step = n / R;
-                for (int q = 0; q < R; q++) {
-                    double sr = 0, si = 0;
-                    for (int r = 0; r < R; r++) {
-                        int e = (int)(((long long)q * r % R) * step);
-                        double c = p->w[2 * e], sn = sgn * p->w[2 * e + 1];
-                        sr += vr[r] * c - vi[r] * sn;
-                        si += vr[r] * sn + vi[r] * c;
-                    }
-                    tr[q] = sr;
-                    ti[q] = si;
-                }
-            }
-            const int idxD = (j / Ns) * Ns * R + k;
-            for (int r = 0; r < R; r++) {
-                out[2 * (idxD + r * Ns)] = tr[r];
-                out[2 * (idxD + r * Ns) + 1] = ti[r];
-            }
-        }
-        double *t = in; in = out; out = t;
-        Ns *= R;
-    }
-    if (in != x) memcpy(x, in, sizeof(double) * 2 * (size_t)n);
-}
-
-/* 2D transform of an H x W row-major plane, in place. */
-typedef struct {
-    fft_plan row, col;
-    double *buf, *scr; /* 2*max(W,H) each */
-} fft2_plan;
-
-static int fft2_init(fft2_plan *p, int W, int H)
-{
-    if (fft_plan_init(&p->row, W)) return -1;
-    if (fft_plan_init(&p->col, H)) return -1;
-    int m = W > H ? W : H;
-    p->buf = (double *)malloc(sizeof(double) * 2 * (size_t)m);
-    p->scr = (double *)malloc(sizeof(double) * 2 * (size_t)m);
-    return (p->buf && p->scr) ? 0 : -1;
-}
-
-static void fft2_free(fft2_plan *p)
-{
-    fft_plan_free(&p->row);
-    fft_plan_free(&p->col);
-    free(p->buf);
-    free(p->scr);
-}
-
-static void fft2_exec(fft2_plan *p, double *a, int inverse)
-{
-    const int W = p->row.n, H = p->col.n;
-    for (int i = 0; i < H; i++) {
-        double *r = a + 2 * (size_t)i * W;
-        fft_exec(&p->row, r, p->scr, inverse);
-    }
-    for (int j = 0; j < W; j++) {
-        for (int i = 0; i < H; i++) {
-            p->buf[2 * i] = a[2 * ((size_t)i * W + j)];
-            p->buf[2 * i + 1] = a[2 * ((size_t)i * W + j) + 1];
-        }
-        fft_exec(&p->col, p->buf, p->scr, inverse);
-        for (int i = 0; i < H; i++) {
-            a[2 * ((size_t)i * W + j)] = p->buf[2 * i];
-            a[2 * ((size_t)i * W + j) + 1] = p->buf[2 * i + 1];
-        }
-    }
-}
+#define OR_REAL double
+#define OR_FN(name) name
+#include "or_fft_gen.h"
+#undef OR_REAL
+#undef OR_FN
 
 /* Exposed for the oracle's own self-test against numpy.fft. */
 int or_fft1d(int n, double *x, int inverse)

@@ -19,6 +19,7 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _SRC = os.path.join(_HERE, "glsu_oracle.c")
+_SRCS = [_SRC, os.path.join(_HERE, "glsu_oracle_f32.c"), os.path.join(_HERE, "or_fft_gen.h")]
 _OUT_DIR = os.path.join(_HERE, "_build")
 _LIB_PATH = os.path.join(_OUT_DIR, "libglsu_oracle.so")
 _lock = threading.Lock()
@@ -29,10 +30,11 @@ def build(force: bool = False) -> str:
     """Compile the oracle shared library (gcc -O3 -fopenmp) and return its path."""
     os.makedirs(_OUT_DIR, exist_ok=True)
     if (not force and os.path.exists(_LIB_PATH)
-            and os.path.getmtime(_LIB_PATH) >= os.path.getmtime(_SRC)):
+            and os.path.getmtime(_LIB_PATH) >= max(os.path.getmtime(f) for f in _SRCS)):
         return _LIB_PATH
     tmp = _LIB_PATH + ".tmp%d" % os.getpid()
-    cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c11", _SRC, "-o", tmp, "-lm"]
+    cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c11"] + [f for f in _SRCS if f.endswith(".c")] + [
+        "-o", tmp, "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(tmp, _LIB_PATH)
     return _LIB_PATH
@@ -64,6 +66,10 @@ def lib():
             L.or_aia.argtypes = [c_int, c_int, dp, dp, c_int, c_double, dp, ip, dp]
             L.or_unwrap2.argtypes = [c_int, c_int, dp, c_int, c_int]
             L.or_wfr2.argtypes = [c_int, c_int, dp] + [c_double] * 8 + [dp] * 8 + [c_int]
+            fp = ctypes.POINTER(ctypes.c_float)
+            L.orf_dpra_ls.argtypes = [c_int, c_int, c_int, fp, fp, fp, c_int]
+            L.orf_dpra_update.argtypes = [c_int, fp, fp, fp, fp, fp]
+            L.orf_wff2.argtypes = [c_int, c_int, fp] + [c_double] * 9 + [fp, c_int, c_int, c_int]
             _lib = L
     return _lib
 
@@ -274,3 +280,53 @@ def glsu_sequence(frames, phi0, r, wp: WffParams, rr=1, nthreads=0):
         if i % rr == 0:
             phiref, dphiref = pc, dphi
     return np.stack(pcs), np.stack(dps)
+
+
+# ---------------------------------------------------------------------------
+# FP32 variant (glsu_oracle_f32.c): the reference's float CPU classes
+# (DPRA/dpra_cpuf.cpp, WFT/WFT2_CPUf.cpp), for the timed CPU baseline.
+# ---------------------------------------------------------------------------
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def dpra_ls_f32(img, phiref, r=1, nthreads=0):
+    img, phiref = _f32(img), _f32(phiref)
+    H, W = img.shape
+    z = np.empty((H, W), np.complex64)
+    lib().orf_dpra_ls(W, H, r, _fptr(img), _fptr(phiref), _fptr(z.view(np.float32)), nthreads)
+    return z
+
+
+def wff2_f32(f, sigx, wxl, wxh, wxi, sigy, wyl, wyh, wyi, thr, nthreads=0, ky=None):
+    f = np.ascontiguousarray(f, dtype=np.complex64)
+    H, W = f.shape
+    out = np.empty((H, W), np.complex64)
+    ky0, ky1 = ky if ky is not None else (0, -1)
+    rc = lib().orf_wff2(W, H, _fptr(f.view(np.float32)), sigx, wxl, wxh, wxi, sigy, wyl, wyh, wyi, thr,
+                        _fptr(out.view(np.float32)), nthreads, ky0, ky1)
+    if rc:
+        raise RuntimeError("orf_wff2 failed (%d)" % rc)
+    return out
+
+
+def dpra_update_f32(filtered, phiref, dphiref):
+    filtered = np.ascontiguousarray(filtered, dtype=np.complex64)
+    phiref, dphiref = _f32(phiref), _f32(dphiref)
+    pc, dp = np.empty_like(phiref), np.empty_like(phiref)
+    lib().orf_dpra_update(phiref.size, _fptr(filtered.view(np.float32)), _fptr(phiref), _fptr(dphiref), _fptr(pc),
+                          _fptr(dp))
+    return pc, dp
+
+
+def glsu_frame_f32(img, phiref, dphiref, r, wp: WffParams, nthreads=0, ky=None):
+    """One frame of the FP32 CPU variant.  Returns (phicurr, dphi, z, filtered)."""
+    z = dpra_ls_f32(img, phiref, r, nthreads)
+    filt = wff2_f32(z, *wp.tuple(), nthreads=nthreads, ky=ky)
+    pc, dphi = dpra_update_f32(filt, phiref, dphiref)
+    return pc, dphi, z, filt
+

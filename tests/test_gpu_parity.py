@@ -389,6 +389,55 @@ def test_pipelined_sequence_equals_frame_loop(glsu, synth, prec, rr, img):
     assert np.array_equal(seq_np, np.stack(ref))
 
 
+@pytest.mark.parametrize("graph", [False, True])
+def test_batched_uneven_sequences_equal_sequential(glsu, synth, graph):
+    """The batched form: sequences of uneven sizes, window radii 2..4,
+    reference rates 1..3 and lengths, one frame of each per step, each on
+    its handle's stream and in flight together (ended sequences pass no
+    frame), give every sequence's phases bit for bit as its own
+    glsu_dpra_sequence does; FP32, u8 frames; plain and surrogate handles."""
+    torch = _torch()
+    from glsu import train_surrogate as T
+    wp = glsu.WffParams(6.0, -1.0, 1.0, 0.25, 6.0, -1.0, 1.0, 0.25, 0.2)
+    specs = [((64, 48), 2, 1, 5), ((96, 80), 3, 2, 3), ((128, 128), 4, 3, 6), ((80, 120), 3, 1, 4),
+             ((128, 128), 2, 1, 2), ((72, 100), 4, 2, 5)]
+    params = T.init_params(3, scale_last=1.0)
+    seqs, handles, ref = [], [], []
+    for k, ((H, W), r, rr, nf) in enumerate(specs):
+        frames, phi0, _ = synth.sequence(H, W, nf, seed=40 + k)
+        u8 = np.clip(np.round(frames * 255), 0, 255).astype(np.uint8)
+        d = glsu.DPRA(phi0.astype(np.float32), rr, r, "f32", wp)
+        if k == 2:
+            d.set_surrogate(params, [1, 2, 4, 8, 16, 8, 4, 1], 64, 8, 0.1)
+        out, _ = d.sequence(u8)
+        ref.append((out, d.get(glsu.PHI_REF).copy()))
+        d.close()
+        d = glsu.DPRA(phi0.astype(np.float32), rr, r, "f32", wp)
+        if k == 2:
+            d.set_surrogate(params, [1, 2, 4, 8, 16, 8, 4, 1], 64, 8, 0.1)
+        d.set_graph(graph)
+        handles.append(d)
+        seqs.append(torch.from_numpy(u8).cuda())
+    dphi = [[] for _ in specs]
+    for step in range(max(s[3] for s in specs)):
+        ptrs = [seqs[k][step].data_ptr() if step < specs[k][3] else None for k in range(len(specs))]
+        glsu.dpra_batch_step(handles, ptrs, glsu.U8)
+        glsu.dpra_batch_wait(handles)
+        for k in range(len(specs)):
+            if step < specs[k][3]:
+                dphi[k].append(handles[k].get(glsu.DPHI).copy())
+    for k, d in enumerate(handles):
+        assert np.array_equal(np.stack(dphi[k]), ref[k][0]), k
+        assert np.array_equal(d.get(glsu.PHI_REF), ref[k][1]), k
+        d.close()
+    with pytest.raises(glsu.GlsuError):
+        h = glsu.DPRA(np.zeros((16, 16), np.float32), 1, 1, "f32", wp)
+        try:
+            glsu.dpra_batch_step([h, h], [seqs[0][0].data_ptr()] * 2, glsu.U8)
+        finally:
+            h.close()
+
+
 def test_aia_reference_bmp_frames(glsu, oracle):
     """AIA on the reference's own test frames Test/{1,2,3}.bmp with the
     deltas of its tests (uint8 path, as AIA_CUDAF receives cv::Mat CV_8UC1)."""
