@@ -97,9 +97,12 @@ __device__ __forceinline__ int2 probe_site(const ProbeArgs &a, int t)
 // py-2S .. py-2S+RYP-1, demodulated by e^{-j wx x} and filtered along x, for
 // the columns px-S .. px-S+RXP-1 (zero outside the image and beyond RX).  A
 // thread takes 16 adjacent output columns of one row from 16+2S staged
-// inputs, summing the taps in ascending order for each output.
+// inputs, summing the taps in ascending order for each output.  Up to half
+// size 30 the registers are capped for two CTAs per SM: the pass is latency
+// bound, and the second CTA takes it from 49 to about 39 us at 1024^2 (a few
+// bytes of spills); at half size 45 the cap would spill heavily.
 template <int S>
-__global__ void __launch_bounds__(ProbeGeom<S>::RTHREADS) wff_probe_rows_kernel(ProbeArgs a, PTaps<float, S> gxr)
+__global__ void __launch_bounds__(ProbeGeom<S>::RTHREADS, (S <= 30 ? 2 : 1)) wff_probe_rows_kernel(ProbeArgs a, PTaps<float, S> gxr)
 {
     using G = ProbeGeom<S>;
     constexpr int RX = G::RX, RXP = G::RXP, RYP = G::RYP, FX = G::FX, FXS = G::FXS, CR = G::CR, SEG = G::SEG;
