@@ -266,33 +266,45 @@ __global__ void __launch_bounds__(ProbeGeom<S>::THREADS) wff_probe_kernel(ProbeA
     }
 }
 
-// One block of 64 threads per tile: sum the partials (fixed order), RMS
+// One block of 256 threads per tile: sum the partials (fixed order), RMS
 // phase residual of cmp against the exact patch where |WFF2| >= 0.1.
-__global__ void __launch_bounds__(64) wff_probe_resid_kernel(const float2 *__restrict__ partial,
-                                                             const int2 *__restrict__ sites, int nparts, int P,
-                                                             int W, int H, const float2 *__restrict__ cmp, float tol,
-                                                             float *__restrict__ resid, int *__restrict__ flags,
-                                                             int *__restrict__ counts, uint32_t *__restrict__ seed)
+__global__ void __launch_bounds__(256) wff_probe_resid_kernel(const float2 *__restrict__ partial,
+                                                              const int2 *__restrict__ sites, int nparts, int P,
+                                                              int W, int H, const float2 *__restrict__ cmp, float tol,
+                                                              float *__restrict__ resid, int *__restrict__ flags,
+                                                              int *__restrict__ counts, uint32_t *__restrict__ seed)
 {
-    __shared__ float s_se[2];
-    __shared__ int s_n[2];
-    const int t = blockIdx.x, e = threadIdx.x;
-    float se = 0.f;
-    int cnt = 0;
-    if (e < P * P) {
-        float2 v = make_float2(0.f, 0.f);
-        // fixed summation order; unrolled so that several loads are in flight
-#pragma unroll 12
-        for (int i = 0; i < nparts; i++) {
-            const float2 q = partial[((size_t)t * nparts + i) * P * P + e];
+    __shared__ float2 s_part[256];
+    __shared__ float s_se[8];
+    __shared__ int s_n[8];
+    const int t = blockIdx.x, tid = threadIdx.x, PP = P * P;
+    // G threads per patch pixel each sum every G-th part (ascending), then
+    // the G sums are added in order g = 0 .. G-1: a fixed summation order
+    const int G = 256 / PP, e = tid % PP, g = tid / PP;
+    float2 v = make_float2(0.f, 0.f);
+    if (g < G) {
+#pragma unroll 4
+        for (int i = g; i < nparts; i += G) {
+            const float2 q = partial[((size_t)t * nparts + i) * PP + e];
             v.x += q.x;
             v.y += q.y;
         }
-        const int2 s = sites[t];
-        const int y = s.x + e / P, x = s.y + e % P;
-        if (y < H && x < W && v.x * v.x + v.y * v.y >= 0.01f) {
+    }
+    s_part[tid] = v;
+    __syncthreads();
+    float se = 0.f;
+    int cnt = 0;
+    if (tid < PP) {
+        float2 sum = s_part[tid];
+        for (int k = 1; k < G; k++) {
+            sum.x += s_part[k * PP + tid].x;
+            sum.y += s_part[k * PP + tid].y;
+        }
+        const int2 st = sites[t];
+        const int y = st.x + tid / P, x = st.y + tid % P;
+        if (y < H && x < W && sum.x * sum.x + sum.y * sum.y >= 0.01f) {
             const float2 c = cmp[(size_t)y * W + x];
-            const float d = atan2f(c.y * v.x - c.x * v.y, c.x * v.x + c.y * v.y);
+            const float d = atan2f(c.y * sum.x - c.x * sum.y, c.x * sum.x + c.y * sum.y);
             se = d * d;
             cnt = 1;
         }
@@ -301,14 +313,19 @@ __global__ void __launch_bounds__(64) wff_probe_resid_kernel(const float2 *__res
         se += __shfl_down_sync(0xffffffffu, se, o);
         cnt += __shfl_down_sync(0xffffffffu, cnt, o);
     }
-    if ((e & 31) == 0) {
-        s_se[e >> 5] = se;
-        s_n[e >> 5] = cnt;
+    if ((tid & 31) == 0) {
+        s_se[tid >> 5] = se;
+        s_n[tid >> 5] = cnt;
     }
     __syncthreads();
-    if (e == 0) {
-        const int n = s_n[0] + s_n[1];
-        const float r = n ? sqrtf((s_se[0] + s_se[1]) / (float)n) : 0.f;
+    if (tid == 0) {
+        float sse = 0.f;
+        int n = 0;
+        for (int k = 0; k < 8; k++) {
+            sse += s_se[k];
+            n += s_n[k];
+        }
+        const float r = n ? sqrtf(sse / (float)n) : 0.f;
         resid[t] = r;
         flags[t] = r > tol ? 1 : 0;
         atomicAdd(&counts[0], 1);
@@ -415,7 +432,7 @@ int WffPlan::enqueue_probe_sweep(cudaStream_t s, const void *d_f, int tile, int 
 int WffPlan::enqueue_probe_resid(cudaStream_t s, const void *d_cmp, double tol, const ProbeOut &o)
 {
     if (probe_parts <= 0) return fail(GLSU_ERR_INVALID, "probe residual without a probe sweep");
-    wff_probe_resid_kernel<<<probe_ntiles, 64, 0, s>>>(o.partial, o.sites, probe_parts, probe_P, W, H,
+    wff_probe_resid_kernel<<<probe_ntiles, 256, 0, s>>>(o.partial, o.sites, probe_parts, probe_P, W, H,
                                                        (const float2 *)d_cmp, (float)tol, o.resid, o.flags, o.counts,
                                                        o.seed);
     GLSU_CUDA_TRY(cudaGetLastError());
