@@ -57,10 +57,11 @@ SUR_TILE, SUR_PATCH, SUR_TOL = 256, 4, 0.05
 # writes 64 B; layer 7 reads 64 B + z and writes the complex output (8 B)
 SUR_BYTES_PER_PX = 72 + 6 * 128 + 80
 SUR_FLOPS_PER_PX = 2 * 18 * 32 + 6 * 2 * 288 * 32 + 2 * 288 * 2
-# kernels per frame: plain = LS, rows, column sweep, final; surrogate = LS,
-# layer 0, six tensor-core layers, layer 7, probe, residual, three masked
-# WFF2 passes, update
-PLAIN_LAUNCHES, SUR_LAUNCHES = 4, 15
+# kernels per frame: plain = LS, rows, column sweep, final (with the update);
+# surrogate = LS, the probe's row and column passes, layer 0, six tensor-core
+# layers, layer 7, the residuals, the tile list, three masked WFF2 passes and
+# the update
+PLAIN_LAUNCHES, SUR_LAUNCHES = 4, 17
 # one 32->32 tensor-core layer per pixel: read 64 B, write 64 B; 2*288*32 flops
 SUR_CONV_BYTES_PER_PX, SUR_CONV_FLOPS_PER_PX = 128, 2 * 288 * 32
 # DRAM bytes (read + write) of one sur_conv_tc_kernel launch at 1024x1024,
