@@ -268,6 +268,16 @@ __global__ void __launch_bounds__(256, 1) sur_conv_tc_kernel(const __grid_consta
             const SurItem it = sur_item(a, item);
             if (it.nout <= 0) continue;
             const int x = it.x0 + q * 32 + lane;
+            // the residual input z of the item's rows, loaded before the first
+            // accumulator wait so that the loads overlap the MMAs
+            float2 zr[kSurRows];
+#pragma unroll
+            for (int k = 0; k < kSurRows; k++) {
+                zr[k] = make_float2(0.f, 0.f);
+                if (k < it.nout && x < a.W)
+                    zr[k] = a.z[((size_t)it.b * a.H + it.r + (size_t)(it.kbeg + k) * a.dil) * a.W + x];
+            }
+#pragma unroll
             for (int k = 0; k < kSurRows; k++) {
                 if (!__all_sync(0xffffffffu, mbar_wait_bounded(&accf[k], li & 1))) {
                     if (lane == 0) atomicExch(a.err, GLSU_ERR_TIMEOUT);
@@ -284,7 +294,7 @@ __global__ void __launch_bounds__(256, 1) sur_conv_tc_kernel(const __grid_consta
                 mbar_arrive(&acce[k]);
                 if (k >= it.nout || x >= a.W) continue;
                 const size_t p = ((size_t)it.b * a.H + it.r + (size_t)(it.kbeg + k) * a.dil) * a.W + x;
-                const float2 zv = a.z[p];
+                const float2 zv = zr[k];
                 const float yr = __fadd_rn(zv.x, h[0]), yi = __fadd_rn(zv.y, h[1]);
                 if (a.yout) {
                     a.yout[p] = make_float2(yr, yi);
