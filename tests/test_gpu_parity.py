@@ -485,6 +485,42 @@ def test_wff_phase_equivariance_full_size(glsu):
     w.close()
 
 
+def test_large_workload_shape_2048(glsu, oracle, synth):
+    """The large streaming workload's shape: 2048x2048 FP32, DPRA 9x9, WFF2
+    sigma 15 with 31x31 frequencies on [-1.5, 1.5], 8 Gaussians, noise 0.05.
+    One frame end to end; its least squares against the oracle (a local
+    stage, so the full frame is checked); the WFF2 stage through the
+    size-independent phase equivariance WFF2(e^{ja} z) = e^{ja} WFF2(z) at this
+    size (its kernels, half size 45, meet the oracle at small sizes in
+    test_wff_f32_matches_oracle)."""
+    torch = _torch()
+    H = W = 2048
+    frames, phi0, _ = synth.sequence(H, W, 2, seed=4, noise=0.05, n_gauss=8)
+    wp = glsu.WffParams(15.0, -1.5, 1.5, 0.1, 15.0, -1.5, 1.5, 0.1, 0.2)
+    d = glsu.DPRA(phi0.astype(np.float32), 1, 4, "f32", wp)
+    print("tuning 2048^2 sigma 15 31x31:", d.tuning())
+    fr = torch.from_numpy(frames[1]).cuda()
+    d.per_frame_device(fr.data_ptr(), glsu.F32)
+    z = d.get_lsq()
+    pc = d.get(glsu.PHI_CURR)
+    d.close()
+    assert np.isfinite(pc).all()
+    zr = oracle.dpra_ls(frames[1].astype(np.float64), phi0.astype(np.float32).astype(np.float64), 4)
+    e = np.abs(np.angle(z * np.conj(zr)))
+    print("2048^2 LS r=4: max %.3g rad, rms %.3g" % (e.max(), np.sqrt(np.mean(e ** 2))))
+    assert e.max() < F32_PHASE_TOL
+    a = torch.from_numpy(z).cuda()
+    b = a * np.exp(1j * 0.77)
+    oa, ob = torch.empty_like(a), torch.empty_like(a)
+    w = glsu.WFF2(W, H, "f32", wp)
+    ms = w.run(a.data_ptr(), oa.data_ptr())
+    w.run(b.data_ptr(), ob.data_ptr())
+    w.close()
+    perr, rel = compare(ob.cpu().numpy(), oa.cpu().numpy() * np.exp(1j * 0.77))
+    print("2048^2 WFF2 (961 frequencies): %.1f ms; equivariance phase %.3g rel %.3g" % (ms, perr, rel))
+    assert perr < 1e-4 and rel < 1e-4
+
+
 def test_glsu_frame_1024_matches_oracle(glsu, oracle, synth):
     """One full-size frame (1024x1024, DPRA 7x7, 441 frequencies) against the oracle."""
     frames, phi0, _ = synth.sequence(1024, 1024, 2, seed=1)
