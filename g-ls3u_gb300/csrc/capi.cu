@@ -447,6 +447,20 @@ extern "C" int glsu_wff_set_fft_plan(glsu_wff *h, int columns_per_cta, int radix
     return h->plan.set_fft_plan(columns_per_cta, radix_order);
 }
 
+extern "C" int glsu_wff_set_fft_length(glsu_wff *h, int length)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    if (h->plan.fft_L == 0) return fail(GLSU_ERR_UNSUPPORTED, "no shared-memory FFT plan for this handle");
+    GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return h->plan.build_colfft(length);
+}
+
+extern "C" int glsu_wff_fft_lengths(const glsu_wff *h, int *lengths, int n)
+{
+    if (!h || (!lengths && n > 0) || n < 0) return fail(GLSU_ERR_INVALID, "bad argument");
+    return fft_length_candidates(h->plan, lengths, n);
+}
+
 // Executable frame graphs capture the handle's configuration and buffers:
 // every change of either drops them.
 static void dpra_drop_graphs(glsu_dpra *h)

@@ -166,6 +166,7 @@ struct WffPlan {
     void *d_khat = nullptr;         // nfy x fft_L spectra of the modulated windows
     void *d_tw = nullptr;           // fft_L twiddles e^{-2 pi i t / L}
     int init_colfft();
+    int build_colfft(int L);  // tables for transform length L, default plan variant
     void release_colfft();
     // FFT plan variant: nc columns per CTA, radix order; GLSU_ERR_UNSUPPORTED
     // where it does not fit (the plan is then unchanged).
@@ -182,6 +183,8 @@ struct WffPlan {
     bool use_colfft() const { return fft_L > 0 && d_khat != nullptr && column_method() == GLSU_METHOD_FFT; }
 };
 
+// The transform lengths the autotuner times for this plan (cheapest first).
+int fft_length_candidates(const WffPlan &P, int *out, int n);
 // The column sweep of a full-frame run (FFT or direct, as the plan selects).
 int launch_column_sweep(WffPlan &P, cudaStream_t s);
 

@@ -309,23 +309,20 @@ static int factor(int n, int *rad, int order = 0)
     return n == 1 ? ns : -1;
 }
 
-// Smallest-cost transform length >= need: cost = L x number of stages.
-static int choose_length(int need, ColFftPlan *out)
+// Transform lengths L >= need (up to 2 need + 16) whose stages factor, in
+// increasing cost L x number of stages (ties: the shorter); at most n of them.
+static int length_candidates(int need, int *out, int n)
 {
-    long best_cost = -1;
+    std::vector<std::pair<long, int>> c;
     for (int L = need; L <= 2 * need + 16; L++) {
-        ColFftPlan p;
-        const int ns = factor(L, p.radix);
-        if (ns < 1 || ns > 12) continue;
-        const long cost = (long)L * ns;
-        if (best_cost < 0 || cost < best_cost) {
-            best_cost = cost;
-            p.L = L;
-            p.nst = ns;
-            *out = p;
-        }
+        int rad[12];
+        const int ns = factor(L, rad);
+        if (ns >= 1 && ns <= 12) c.push_back({(long)L * ns, L});
     }
-    return best_cost < 0 ? -1 : 0;
+    std::sort(c.begin(), c.end());
+    int k = 0;
+    for (; k < n && k < (int)c.size(); k++) out[k] = c[k].second;
+    return k;
 }
 
 static int colfft_nc(int L) { return L <= 1600 ? 4 : 2; }
@@ -339,40 +336,56 @@ static bool colfft_fits(int L, int nc, int pitch)
 int WffPlan::init_colfft()
 {
     if (prec != GLSU_F32) return GLSU_OK;
-    ColFftPlan p;
-    if (choose_length(H + 2 * sy, &p)) return GLSU_OK;  // no suitable length: direct kernel
-    const int nc = colfft_nc(p.L);
-    if (!colfft_fits(p.L, nc, pitch)) return GLSU_OK;  // registers per thread, shared memory
-    fft_L = p.L;
-    fft_nst = p.nst;
-    fft_nc = nc;
-    fft_order = 0;
-    for (int s = 0; s < p.nst; s++) fft_radix[s] = p.radix[s];
-    // H_k = DFT of h_k(m) = gy(m) e^{j wy_k m}, m in [-sy, sy] placed circularly
-    std::vector<float> kh(2 * (size_t)nfy * p.L), tw(2 * (size_t)p.L);
+    int L;
+    if (length_candidates(H + 2 * sy, &L, 1) < 1) return GLSU_OK;  // no suitable length: direct kernel
+    if (!colfft_fits(L, colfft_nc(L), pitch)) return GLSU_OK;      // registers per thread, shared memory
+    return build_colfft(L);
+}
+
+// Tables of the FFT sweep for transform length L (replacing any others), with
+// the default plan variant: H_k = DFT of h_k(m) = gy(m) e^{j wy_k m},
+// m in [-sy, sy] placed circularly, and the twiddles e^{-2 pi i t / L}.
+int WffPlan::build_colfft(int L)
+{
+    if (prec != GLSU_F32 || L < H + 2 * sy || !colfft_fits(L, colfft_nc(L), pitch))
+        return fail(GLSU_ERR_UNSUPPORTED, "no shared-memory FFT plan of that length for this handle");
+    int rad[12];
+    const int ns = factor(L, rad);
+    if (ns < 1 || ns > 12) return fail(GLSU_ERR_UNSUPPORTED, "transform length has a prime factor above 5");
+    release_colfft();
+    std::vector<float> kh(2 * (size_t)nfy * L), tw(2 * (size_t)L);
     for (int k = 0; k < nfy; k++) {
         const double wy = this->p.wyl + (double)k * this->p.wyi;
-        for (int w = 0; w < p.L; w++) {
+        for (int w = 0; w < L; w++) {
             double re = 0, im = 0;
             for (int m = -sy; m <= sy; m++) {
-                const double ang = wy * m - 2.0 * M_PI * (double)w * (double)m / (double)p.L;
+                const double ang = wy * m - 2.0 * M_PI * (double)w * (double)m / (double)L;
                 re += gy[m + sy] * std::cos(ang);
                 im += gy[m + sy] * std::sin(ang);
             }
-            kh[2 * ((size_t)k * p.L + w)] = (float)re;
-            kh[2 * ((size_t)k * p.L + w) + 1] = (float)im;
+            kh[2 * ((size_t)k * L + w)] = (float)re;
+            kh[2 * ((size_t)k * L + w) + 1] = (float)im;
         }
     }
-    for (int t = 0; t < p.L; t++) {
-        tw[2 * t] = (float)std::cos(-2.0 * M_PI * t / p.L);
-        tw[2 * t + 1] = (float)std::sin(-2.0 * M_PI * t / p.L);
+    for (int t = 0; t < L; t++) {
+        tw[2 * t] = (float)std::cos(-2.0 * M_PI * t / L);
+        tw[2 * t + 1] = (float)std::sin(-2.0 * M_PI * t / L);
     }
     if (cudaMalloc(&d_khat, kh.size() * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&d_tw, tw.size() * sizeof(float)) != cudaSuccess)
+        cudaMalloc(&d_tw, tw.size() * sizeof(float)) != cudaSuccess) {
+        release_colfft();
         return fail(GLSU_ERR_ALLOC, "cudaMalloc of the column FFT tables failed");
+    }
     GLSU_CUDA_TRY(cudaMemcpy(d_khat, kh.data(), kh.size() * sizeof(float), cudaMemcpyHostToDevice));
     GLSU_CUDA_TRY(cudaMemcpy(d_tw, tw.data(), tw.size() * sizeof(float), cudaMemcpyHostToDevice));
-    return GLSU_OK;
+    fft_L = L;
+    return set_fft_plan(colfft_nc(L), 0);
+}
+
+int fft_length_candidates(const WffPlan &P, int *out, int n)
+{
+    if (P.prec != GLSU_F32 || P.fft_L == 0) return 0;
+    return length_candidates(P.H + 2 * P.sy, out, n);
 }
 
 int WffPlan::set_fft_plan(int nc, int order)
@@ -440,13 +453,14 @@ int launch_colfft(const WffPlan &P, cudaStream_t s)
 // ---------------------------------------------------------------------------
 // autotuner
 // ---------------------------------------------------------------------------
-// Candidates: the direct column kernel, and the FFT sweep with 4 or 2
-// columns per CTA and each radix order.  Each is launched once (warm-up),
-// then twice between CUDA events on the plan's own buffers; the kernels have
-// no data-dependent control flow, so the buffers' contents do not matter.
-// The FFT is taken only when at least 10% faster than the direct kernel, so
-// that near ties keep the direct kernel, and the other FFT variants are
-// tried only when the default one is within 1.5x of it.  Results are kept
+// Candidates: the direct column kernel, and the FFT sweep at the three
+// cheapest transform lengths (L x stages), then, at the fastest length, with
+// 4 or 2 columns per CTA and each radix order.  Each is launched once
+// (warm-up), then twice between CUDA events on the plan's own buffers; the
+// kernels have no data-dependent control flow, so the buffers' contents do
+// not matter.  The FFT is taken only when at least 10% faster than the
+// direct kernel, so that near ties keep the direct kernel, and the plan
+// variants are tried only when the best length is within 1.5x of it.  Results are kept
 // per shape for the process, so every handle of a shape runs the same
 // kernels.  GLSU_AUTOTUNE=0 in the environment skips the timing (the direct
 // kernel).
@@ -456,7 +470,7 @@ struct TuneKey {
     bool operator<(const TuneKey &o) const { return std::lexicographical_compare(v, v + 9, o.v, o.v + 9); }
 };
 struct TuneResult {
-    int method, nc, order;
+    int method, L, nc, order;
     float ms_direct, ms_fft;
 };
 std::mutex g_tune_mu;
@@ -471,7 +485,7 @@ int WffPlan::autotune(cudaStream_t s)
     if (prec != GLSU_F32 || fft_L == 0 || d_khat == nullptr || mask.flags) return GLSU_OK;
     const char *env = std::getenv("GLSU_AUTOTUNE");
     if (env && env[0] == '0') return GLSU_OK;
-    const TuneKey key{{W, H, pitch, sx, sy, nfx, nfy, fft_L, (int)(1000 * p.wyl + 0.5)}};
+    const TuneKey key{{W, H, pitch, sx, sy, nfx, nfy, H + 2 * sy, (int)(1000 * p.wyl + 0.5)}};
     std::lock_guard<std::mutex> lock(g_tune_mu);
     auto it = g_tune.find(key);
     if (it == g_tune.end()) {
@@ -493,32 +507,42 @@ int WffPlan::autotune(cudaStream_t s)
                 rc = fail(GLSU_ERR_CUDA, "timing a column-sweep candidate failed");
             *ms *= 0.5f;
         };
-        TuneResult r{GLSU_METHOD_DIRECT, fft_nc, fft_order, 0.f, 0.f};
+        TuneResult r{GLSU_METHOD_DIRECT, fft_L, fft_nc, fft_order, 0.f, 0.f};
         time_it(GLSU_METHOD_DIRECT, &r.ms_direct);
         float best = -1.f;
+        int lens[3];
+        const int nl = length_candidates(H + 2 * sy, lens, 3);
+        for (int j = 0; j < nl && rc == GLSU_OK; j++) {
+            if (build_colfft(lens[j]) != GLSU_OK) continue;
+            float ms = 0;
+            time_it(GLSU_METHOD_FFT, &ms);
+            if (rc == GLSU_OK && (best < 0 || ms < best)) {
+                best = ms;
+                r.L = lens[j];
+                r.nc = fft_nc;
+                r.order = fft_order;
+            }
+        }
+        if (rc == GLSU_OK && r.L != fft_L) rc = build_colfft(r.L);
         const int nc0 = fft_nc;
         for (int nc : {nc0, 6 - nc0}) {
+            if (rc != GLSU_OK || best < 0 || best > 1.5f * r.ms_direct) break;
             for (int order = 0; order < 3 && rc == GLSU_OK; order++) {
-                if (set_fft_plan(nc, order) != GLSU_OK) continue;
+                if ((nc == nc0 && order == 0) || set_fft_plan(nc, order) != GLSU_OK) continue;
                 float ms = 0;
                 time_it(GLSU_METHOD_FFT, &ms);
-                if (rc == GLSU_OK && (best < 0 || ms < best)) {
+                if (rc == GLSU_OK && ms < best) {
                     best = ms;
                     r.nc = nc;
                     r.order = order;
                 }
-                if (nc == nc0 && order == 0 && ms > 1.5f * r.ms_direct) break;
             }
-            if (best > 1.5f * r.ms_direct) break;
         }
         set_error(std::string());  // variants that did not fit leave no message
         method = saved;
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        if (rc != GLSU_OK) {
-            set_fft_plan(nc0, 0);
-            return rc;
-        }
+        if (rc != GLSU_OK) return rc;
         r.ms_fft = best;
         if (best > 0 && best < 0.9f * r.ms_direct) r.method = GLSU_METHOD_FFT;
         it = g_tune.emplace(key, r).first;
@@ -527,6 +551,7 @@ int WffPlan::autotune(cudaStream_t s)
     auto_method = r.method;
     tune_ms_direct = r.ms_direct;
     tune_ms_fft = r.ms_fft;
+    if (r.L != fft_L) GLSU_TRY(build_colfft(r.L));
     return set_fft_plan(r.nc, r.order);
 }
 

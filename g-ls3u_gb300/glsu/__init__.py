@@ -138,6 +138,8 @@ def lib() -> ctypes.CDLL:
             "glsu_dpra_batch_wait": ([ctypes.POINTER(c_void_p), c_int], c_int),
             "glsu_dpra_get_tuning": ([c_void_p, ctypes.POINTER(WffTuningC)], c_int),
             "glsu_wff_set_fft_plan": ([c_void_p, c_int, c_int], c_int),
+            "glsu_wff_set_fft_length": ([c_void_p, c_int], c_int),
+            "glsu_wff_fft_lengths": ([c_void_p, intp, c_int], c_int),
             "glsu_dpra_set_unwrap": ([c_void_p, c_int, c_int, c_int], c_int),
             "glsu_unwrap2_device": ([c_int, c_void_p, c_int, c_int, c_int, c_int, c_void_p], c_int),
             "glsu_wff_padded_size": ([c_void_p, intp, intp], c_int),
@@ -339,6 +341,16 @@ class WFF2:
     def set_fft_plan(self, columns_per_cta: int, radix_order: int):
         """Force an FFT plan variant (4 or 2 columns per CTA; radix order 0, 1 or 2)."""
         check(lib().glsu_wff_set_fft_plan(self._h, columns_per_cta, radix_order))
+
+    def set_fft_length(self, length: int):
+        """Rebuild the FFT sweep for another transform length (default plan variant)."""
+        check(lib().glsu_wff_set_fft_length(self._h, length))
+
+    def fft_lengths(self, n: int = 3) -> list:
+        """The transform lengths the autotuner times, cheapest first."""
+        out = (ctypes.c_int * max(n, 1))()
+        k = check(lib().glsu_wff_fft_lengths(self._h, out, n))
+        return list(out[:k])
 
     @property
     def threshold(self) -> float:

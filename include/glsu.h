@@ -122,8 +122,9 @@ int glsu_wff_threshold(glsu_wff *h, double *thr);
 int glsu_wff_set_method(glsu_wff *h, int method);
 /* Column-sweep autotuner.  With GLSU_METHOD_AUTO (the default) the handle
  * runs the column sweep measured fastest for its shape: the direct kernel,
- * or the shared-memory FFT sweep with 4 or 2 columns per CTA and one of
- * three radix orders (0: 8,4,2,5,3; 1: 4,2,5,3; 2: 5,3,8,4,2).  The first
+ * or the shared-memory FFT sweep at one of the three cheapest transform
+ * lengths with 4 or 2 columns per CTA and one of three radix orders
+ * (0: 8,4,2,5,3; 1: 4,2,5,3; 2: 5,3,8,4,2).  The first
  * handle of a shape in the process times the candidates at creation (a few
  * launches each); later handles of that shape reuse the choice.  The FFT is
  * taken only when at least 10% faster.  Setting GLSU_AUTOTUNE=0 in the
@@ -142,6 +143,12 @@ int glsu_wff_get_tuning(const glsu_wff *h, glsu_wff_tuning *t);
 /* Force an FFT plan variant (the autotuner's knobs); GLSU_ERR_UNSUPPORTED
  * where it does not fit.  Takes effect when the FFT sweep runs. */
 int glsu_wff_set_fft_plan(glsu_wff *h, int columns_per_cta, int radix_order);
+/* Rebuild the FFT sweep's tables for another transform length (>= H + 2 sy,
+ * factors 2, 3, 5 only) with the default plan variant. */
+int glsu_wff_set_fft_length(glsu_wff *h, int length);
+/* The transform lengths the autotuner times, cheapest first (length x
+ * stages); returns how many were written (at most n; 0 without an FFT plan). */
+int glsu_wff_fft_lengths(const glsu_wff *h, int *lengths, int n);
 
 /* FFT-padded plane of the reference's formulation (kept for API parity). */
 int glsu_wff_padded_size(const glsu_wff *h, int *padded_width, int *padded_height);

@@ -104,8 +104,9 @@ def test_column_method_switch(glsu):
 
 @pytest.mark.parametrize("case", [0, 2, 4])
 def test_wff_fft_plan_variants_match_oracle(glsu, oracle, case):
-    """Every FFT plan variant the autotuner may pick (4 or 2 columns per CTA,
-    radix orders 0, 1, 2) within the FP32 tolerance of the oracle."""
+    """Every FFT plan the autotuner may pick (its three transform lengths, 4 or
+    2 columns per CTA, radix orders 0, 1, 2) within the FP32 tolerance of the
+    oracle."""
     shape, p = WFF_CASES[case]
     f = field(shape, case)
     ref, _ = oracle.wff2(f.astype(np.complex64).astype(np.complex128), *p)
@@ -115,20 +116,25 @@ def test_wff_fft_plan_variants_match_oracle(glsu, oracle, case):
     w = glsu.WFF2(shape[1], shape[0], "f32", glsu.WffParams(*p))
     w.set_method(glsu.METHOD_FFT)
     ran = 0
-    for nc in (4, 2):
-        for order in (0, 1, 2):
-            try:
-                w.set_fft_plan(nc, order)
-            except glsu.GlsuError as e:
-                assert e.code == glsu.ERR_UNSUPPORTED
-                continue
-            w.run(t.data_ptr(), out.data_ptr())
-            perr, rel = compare(out.cpu().numpy(), ref)
-            print("fft plan case %d nc %d order %d: phase err %.3g, rel %.3g" % (case, nc, order, perr, rel))
-            assert perr < F32_PHASE_TOL and rel < 1e-4
-            ran += 1
+    lengths = w.fft_lengths(3)
+    assert len(lengths) >= 2
+    for L in lengths:
+        w.set_fft_length(L)
+        for nc in (4, 2):
+            for order in (0, 1, 2):
+                try:
+                    w.set_fft_plan(nc, order)
+                except glsu.GlsuError as e:
+                    assert e.code == glsu.ERR_UNSUPPORTED
+                    continue
+                w.run(t.data_ptr(), out.data_ptr())
+                perr, rel = compare(out.cpu().numpy(), ref)
+                print("fft plan case %d L %d nc %d order %d: phase err %.3g, rel %.3g" % (case, L, nc, order, perr,
+                                                                                          rel))
+                assert perr < F32_PHASE_TOL and rel < 1e-4
+                ran += 1
     w.close()
-    assert ran >= 3
+    assert ran >= 6
 
 
 def test_autotuner_choices(glsu, oracle):
