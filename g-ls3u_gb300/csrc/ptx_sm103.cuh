@@ -240,7 +240,7 @@ __device__ __forceinline__ uint64_t umma_desc_sw64(uint32_t saddr, uint32_t base
            ((uint64_t)1 << 46) | ((uint64_t)(base_off & 7) << 49) | ((uint64_t)4 << 61);
 }
 
-// Host: the driver's cuTensorMapEncodeTiled (null when unavailable).
+// Host: cuTensorMapEncodeTiled of the CUDA driver API (null when unavailable).
 PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn();
 
 }  // namespace glsu

@@ -1,4 +1,4 @@
-// wff_probe.cu -- exact WFF2 on sparse patches: the judge of the surrogate.
+// wff_probe.cu -- exact WFF2 on sparse patches: the check on the surrogate.
 //
 // For each tile of the frame, one P x P patch (position hashed from a seed
 // and the tile index) gets the exact FP32 WFF2 output, computed by the same
