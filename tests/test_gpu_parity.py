@@ -395,6 +395,30 @@ def test_pipelined_sequence_equals_frame_loop(glsu, synth, prec, rr, img):
     assert np.array_equal(seq_np, np.stack(ref))
 
 
+def test_graph_mode_on_the_legacy_stream_runs_eagerly(glsu, synth):
+    """The legacy default stream cannot be captured: a handle moved onto it
+    keeps graph mode on but runs its frames eagerly, with the same results;
+    the batched form refuses such a handle."""
+    frames, phi0, _ = synth.sequence(64, 80, 4, seed=12)
+    wp = glsu.WffParams(4.0, -0.5, 0.5, 0.25, 4.0, -0.5, 0.5, 0.25, 0.2)
+    out = []
+    for legacy in (False, True):
+        d = glsu.DPRA(phi0.astype(np.float32), 1, 2, "f32", wp)
+        d.set_graph(True)
+        if legacy:
+            d.set_stream(0)
+        res, _ = d.sequence(frames)
+        out.append(res)
+        if legacy:
+            torch = _torch()
+            t = torch.from_numpy(frames).cuda()
+            with pytest.raises(glsu.GlsuError) as e:
+                glsu.dpra_batch_step([d], [t[0].data_ptr()], glsu.F32)
+            assert e.value.code == glsu.ERR_INVALID
+        d.close()
+    assert np.array_equal(out[0], out[1])
+
+
 @pytest.mark.parametrize("graph", [False, True])
 def test_batched_uneven_sequences_equal_sequential(glsu, synth, graph):
     """The batched form: sequences of uneven sizes, window radii 2..4,
