@@ -404,6 +404,68 @@ def surrogate_accuracy(glsu, torch, dfr, phi0, wp, params, dil, nframes):
             "tiles_probed": probed, "tiles_recomputed": flagged}
 
 
+BATCH_SIZES = ((256, 256), (384, 512), (1024, 1024), (1536, 2048))  # (H, W) of the batched form's mix
+
+
+def batched_measure(glsu, torch, seed, sizes=BATCH_SIZES, per_size=2, nframes=4):
+    """The batched form on a small mix of uneven sequences (per_size sequences
+    of each of four sizes, DPRA 7x7, the plain WFF2 with 21x21 frequencies,
+    every handle in graph mode): nframes frames of each through
+    glsu_dpra_batch_step (each sequence's frame on its own stream), against
+    the same sequences run one after another on one stream.  Device time
+    from CUDA events around the frames, after one warm-up frame each."""
+    from glsu import synth
+    wp = glsu.WffParams(*WFF)
+    seqs, handles, px = [], [], 0
+    for k, (H, W) in enumerate(tuple(sizes) * per_size):
+        frames, phi0, _ = synth.sequence(H, W, nframes + 1, seed=seed + 7 * k)
+        seqs.append((torch.from_numpy(frames).cuda(), phi0.astype(np.float32)))
+        px += H * W * nframes
+
+    def make():
+        hs = []
+        for fr, phi0 in seqs:
+            d = glsu.DPRA(phi0, 1, RADIUS, "f32", wp)
+            d.set_graph(True)
+            hs.append(d)
+        return hs
+
+    def run(hs, batched):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for step in range(nframes + 1):
+            if step == 1:
+                torch.cuda.synchronize()
+                e0.record()
+            if batched:
+                glsu.dpra_batch_step(hs, [fr[step].data_ptr() for fr, _ in seqs], glsu.F32)
+            else:
+                for d, (fr, _) in zip(hs, seqs):
+                    d.per_frame_device(fr[step].data_ptr(), glsu.F32)
+                    d.update_ref_phi()
+                    torch.cuda.synchronize()  # one sequence's frame at a time
+        glsu.dpra_batch_wait(hs)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    hs = make()
+    ms_b = run(hs, True)
+    for d in hs:
+        d.close()
+    hs = make()
+    ms_s = run(hs, False)
+    for d in hs:
+        d.close()
+    nf = len(seqs) * nframes
+    return {"workload": "%d sequences (%s, %d each), %d frames each after one warm-up frame, DPRA %dx%d, "
+                        "WFF2 21x21 frequencies, FP32, graph mode" % (
+                            len(seqs), ", ".join("%dx%d" % (w, h) for h, w in sizes), per_size, nframes,
+                            2 * RADIUS + 1, 2 * RADIUS + 1),
+            "batched_ms": ms_b, "sequential_ms": ms_s, "frames": nf, "megapixels": px / 1e6,
+            "batched_frames_per_s": nf / (ms_b * 1e-3), "batched_mpixels_per_s": px / 1e6 / (ms_b * 1e-3),
+            "speedup_vs_sequential": ms_s / ms_b}
+
+
 def wfr_measure(glsu, torch, phi0, size, seed):
     """WFR2 (windowed Fourier ridges) with the reference's WFR defaults
     (sigma 10, 161 x 161 frequencies on [-2, 2] step 0.025, counted in float as
@@ -449,7 +511,7 @@ def run_ours(args, rank, world, local):
     frames, phi0, _ = synth.sequence(size, size, nfr, seed=seed)
 
     # ---- AIA initial phase (5 frames, shifts U(0, 2pi), <= 30 iterations or 1e-4)
-    aia_ms, aia_iters, aia_err, wfr = None, None, None, None
+    aia_ms, aia_iters, aia_err, wfr, batched = None, None, None, None, None
     if not args.frames_only:
         aframes, _, _ = synth.aia_frames(size, size, 5, seed=seed)
         aia = glsu.AIA(5, size, size)
@@ -457,6 +519,8 @@ def run_ours(args, rank, world, local):
         _, _, aia_ms, aia_iters, aia_err = aia.run(list(aframes), None, max_iter=30, max_err=1e-4, seed=seed)
         aia.close()
         wfr = wfr_measure(glsu, torch, phi0, size, seed)
+        batched = {"uneven_sizes": batched_measure(glsu, torch, seed),
+                   "small_frames": batched_measure(glsu, torch, seed, sizes=((256, 256),), per_size=16, nframes=8)}
 
     stream = torch.cuda.Stream()
     dfr = torch.from_numpy(frames).cuda()
@@ -601,6 +665,7 @@ def run_ours(args, rank, world, local):
                   "column_sweep_autotune": p_tuning},
         "surrogate": sur,
         "wfr": wfr,
+        "batched_form": batched,
         "aia": {"frames": 5, "ms": aia_ms, "iterations": aia_iters, "err": aia_err,
                 "ms_per_frame_over_200": None if aia_ms is None else aia_ms / 200},
     }
