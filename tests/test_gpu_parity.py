@@ -203,7 +203,10 @@ def test_wff_threshold_is_kept_after_first_call(glsu, oracle):
 
 @pytest.mark.parametrize("prec,r,img,ls", [("f32", 1, "u8", 0), ("f32", 3, "f32", 0), ("f32", 4, "f32", 0),
                                            ("f32", 3, "u8", 0), ("f32", 1, "u8", 1), ("f32", 3, "f32", 1),
-                                           ("f64", 2, "f32", 0), ("f64", 3, "f64", 0), ("f64", 1, "u8", 0)])
+                                           ("f64", 2, "f32", 0), ("f64", 3, "f64", 0), ("f64", 1, "u8", 0),
+                                           # the largest windows (radius up to 8, 17x17)
+                                           ("f32", 5, "f32", 0), ("f32", 8, "u8", 0), ("f32", 8, "f32", 1),
+                                           ("f64", 6, "u8", 0), ("f64", 8, "f32", 0)])
 def test_dpra_least_squares_matches_oracle(glsu, oracle, synth, prec, r, img, ls):
     """FP32 form in both arithmetics (ls 0: float-float, 1: FP64 sums); FP64 form."""
     H, W = 61, 75
@@ -486,14 +489,16 @@ def test_aia_reference_bmp_frames(glsu, oracle):
     a.close()
 
 
-def test_aia_synthetic_matches_oracle(glsu, oracle, synth):
-    frames, _, _ = synth.aia_frames(200, 180, 5, seed=4)
-    d0 = glsu.random_deltas(5, 11)
-    a = glsu.AIA(5, 180, 200)
+@pytest.mark.parametrize("M", [3, 5, 32])
+def test_aia_synthetic_matches_oracle(glsu, oracle, synth, M):
+    """AIA from the fewest frames it accepts (3) to the most (32)."""
+    frames, _, _ = synth.aia_frames(200, 180, M, seed=4)
+    d0 = glsu.random_deltas(M, 11)
+    a = glsu.AIA(M, 180, 200)
     phi, d, ms, it, err = a.run(list(frames), None, max_iter=30, max_err=1e-4, seed=11)
     ophi, od, oit, oerr = oracle.aia(frames.astype(np.float64), d0.astype(np.float64), 30, 1e-4)
     e_phi = np.abs(np.angle(np.exp(1j * (phi - ophi)))).max()
-    print("aia synthetic: iters %d/%d, delta err %.3g, phi err %.3g" % (it, oit, np.abs(d - od).max(), e_phi))
+    print("aia synthetic M=%d: iters %d/%d, delta err %.3g, phi err %.3g" % (M, it, oit, np.abs(d - od).max(), e_phi))
     assert it == oit and np.abs(d - od).max() < 1e-4 and e_phi < 1e-3
     a.close()
 
