@@ -398,6 +398,29 @@ def test_pipelined_sequence_equals_frame_loop(glsu, synth, prec, rr, img):
     assert np.array_equal(seq_np, np.stack(ref))
 
 
+@pytest.mark.parametrize("rr", [1, 3])
+def test_graph_mode_equals_eager_fp64(glsu, synth, rr):
+    """The FP64 handle (DPRA_CUDA) replayed from graphs: the eager phases bit
+    for bit, f64 and u8 frames, across reference updates."""
+    frames, phi0, _ = synth.sequence(72, 96, 6, seed=13)
+    wp = glsu.WffParams(4.0, -0.5, 0.5, 0.25, 4.0, -0.5, 0.5, 0.25, 0.2)
+    out = []
+    for graph in (False, True):
+        d = glsu.DPRA(phi0.astype(np.float64), rr, 2, "f64", wp)
+        d.set_graph(graph)
+        res = []
+        for k, f in enumerate(frames):
+            img = f.astype(np.float64) if k % 2 else np.clip(f * 255, 0, 255).astype(np.uint8)
+            dphi, _ = d.per_frame(img)
+            res.append((dphi.copy(), d.get(glsu.PHI_CURR).copy()))
+            if k % rr == 0:
+                d.update_ref_phi()
+        d.close()
+        out.append(res)
+    for (a1, b1), (a2, b2) in zip(*out):
+        assert np.array_equal(a1, a2) and np.array_equal(b1, b2)
+
+
 def test_graph_mode_on_the_legacy_stream_runs_eagerly(glsu, synth):
     """The legacy default stream cannot be captured: a handle moved onto it
     keeps graph mode on but runs its frames eagerly, with the same results;
