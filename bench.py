@@ -466,6 +466,29 @@ def batched_measure(glsu, torch, seed, sizes=BATCH_SIZES, per_size=2, nframes=4)
             "speedup_vs_sequential": ms_s / ms_b}
 
 
+def plain_accuracy(glsu, torch, dfr, phi0, wp, nframes):
+    """Teacher-forced phase error of the plain FP32 form against the FP64
+    G-LS3U frame from the same reference phase (per frame, all pixels and
+    pixels with |WFF2| >= 0.1)."""
+    d = glsu.DPRA(phi0.astype(np.float32), 1, RADIUS, "f32", wp)
+    rm, mx, mxm = [], [], []
+    for k in range(1, nframes + 1):
+        pref = d.get(glsu.PHI_REF).astype(np.float64)
+        d64 = glsu.DPRA(pref, 1, RADIUS, "f64", wp)
+        d64.per_frame_device(dfr[k].data_ptr(), glsu.F32)
+        pc64 = d64.get(glsu.PHI_CURR)
+        d64.close()
+        d.per_frame_device(dfr[k].data_ptr(), glsu.F32)
+        pc = d.get(glsu.PHI_CURR).astype(np.float64)
+        e = np.abs(np.angle(np.exp(1j * (pc - pc64))))
+        rm.append(float(np.sqrt(np.mean(e ** 2))))
+        mx.append(float(e.max()))
+        d.update_ref_phi()
+    d.close()
+    return {"rmse_vs_fp64": float(np.sqrt(np.mean(np.square(rm)))), "max_abs_vs_fp64": max(mx),
+            "frames": nframes, "bar_rad": 1e-3}
+
+
 def wfr_measure(glsu, torch, phi0, size, seed):
     """WFR2 (windowed Fourier ridges) with the reference's WFR defaults
     (sigma 10, 161 x 161 frequencies on [-2, 2] step 0.025, counted in float as
@@ -541,6 +564,7 @@ def run_ours(args, rank, world, local):
         return h
 
     p_e2e = None if args.frames_only else e2e_sequence(glsu, torch, plain_handle, frames, args, stream, flush, world)
+    p_acc = None if args.frames_only else plain_accuracy(glsu, torch, dfr, phi0, wp, 3)
 
     # ---- surrogate form: DPRA LS -> network -> probes -> per-tile fallback -> update
     sur = None
@@ -662,7 +686,7 @@ def run_ours(args, rank, world, local):
                   "stages_ms": {"dpra_ls": p_st[0], "wff_rows": p_st[1], "wff_column_sweep": p_st[2],
                                 "wff_final_update": p_st[3]},
                   "roofline": plain_roof, "clocks": p_clk, "gpu_launches_per_step": PLAIN_LAUNCHES,
-                  "column_sweep_autotune": p_tuning},
+                  "column_sweep_autotune": p_tuning, "accuracy": p_acc},
         "surrogate": sur,
         "wfr": wfr,
         "batched_form": batched,
