@@ -194,8 +194,11 @@ __device__ float2 *fft_run(float2 *a, float2 *b, const ColFftPlan &P, const floa
 }
 
 // MAXE: elements (of the L x NC block) owned per thread, upper bound.
+// Registers are capped for two CTAs per SM: the stages are bound by shared
+// memory and block barriers, and a second CTA hides them (16-19% faster at
+// 1024^2 and 2048^2 despite 144-236 bytes of spills a thread).
 template <int NC, int MAXE>
-__global__ void __launch_bounds__(kFftThreads, 1) wff_colfft_kernel(const float2 *__restrict__ R, float2 *__restrict__ Cout,
+__global__ void __launch_bounds__(kFftThreads, 2) wff_colfft_kernel(const float2 *__restrict__ R, float2 *__restrict__ Cout,
                                                                  int H, int pitch, int nfy,
                                                                  const float2 *__restrict__ khat,
                                                                  const float2 *__restrict__ tw, ColFftPlan P,
