@@ -235,7 +235,8 @@ int glsu_dpra_update_ref_phi(glsu_dpra *h);
  * graphs) and the call returns without waiting.  Each handle follows the
  * sequence rule: after its i-th batched frame the reference is updated when
  * i % rr == 0.  glsu_dpra_batch_wait waits for all of them and reports device
- * errors.  A handle may appear once per step. */
+ * errors.  A handle may appear once per step.  On an error at handle i the
+ * handles before i have already taken their frame of this step. */
 int glsu_dpra_batch_step(glsu_dpra *const *handles, int n, const void *const *d_frames, int img_type);
 int glsu_dpra_batch_wait(glsu_dpra *const *handles, int n);
 /* DPRA_CPU::operator() semantics for a block of frames: for frame i, run
