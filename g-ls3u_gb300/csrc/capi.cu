@@ -3,10 +3,13 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
 
+#include "func_attr.hpp"
 #include "glsu_internal.cuh"
 #include "sur_net.cuh"
 
@@ -28,6 +31,41 @@ int cuda_fail(cudaError_t e, const char *what)
     if (e == cudaErrorMemoryAllocation) return GLSU_ERR_ALLOC;
     if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return GLSU_ERR_NO_DEVICE;
     return GLSU_ERR_CUDA;
+}
+
+static FuncAttrCache g_attr;
+
+int raise_smem_limit(const void *func, int bytes, int carveout)
+{
+    int dev = 0;
+    GLSU_CUDA_TRY(cudaGetDevice(&dev));
+    if (!g_attr.needs(func, dev, bytes)) return GLSU_OK;
+    GLSU_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    if (carveout >= 0)
+        GLSU_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributePreferredSharedMemoryCarveout, carveout));
+    g_attr.done(func, dev, bytes);
+    return GLSU_OK;
+}
+
+int device_sm_count()
+{
+    static std::mutex mu;
+    static std::map<int, int> counts;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = counts.find(dev);
+    if (it != counts.end()) return it->second;
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        n = 1;
+    }
+    counts[dev] = n;
+    return n;
 }
 
 int wff_count_public(double lo, double hi, double step, int prec);
@@ -406,13 +444,14 @@ extern "C" int glsu_wff_threshold(glsu_wff *h, double *thr)
 
 static int set_method(WffPlan &P, int method, cudaStream_t s)
 {
-    if (method != GLSU_METHOD_AUTO && method != GLSU_METHOD_DIRECT && method != GLSU_METHOD_FFT)
+    if (method != GLSU_METHOD_AUTO && method != GLSU_METHOD_DIRECT && method != GLSU_METHOD_FFT &&
+        method != GLSU_METHOD_TIMED)
         return fail(GLSU_ERR_INVALID, "unknown column-sweep method");
     if (method == GLSU_METHOD_FFT && P.fft_L == 0)
         return fail(GLSU_ERR_UNSUPPORTED, "no shared-memory FFT plan for this handle (FP64, or no transform length)");
     GLSU_CUDA_TRY(cudaStreamSynchronize(s));
     P.method = method;
-    if (method == GLSU_METHOD_AUTO && !P.tuned) return P.autotune(s);
+    if (method == GLSU_METHOD_AUTO || method == GLSU_METHOD_TIMED) return P.autotune(s);
     return GLSU_OK;
 }
 
@@ -422,7 +461,7 @@ static void get_tuning(const WffPlan &P, glsu_wff_tuning *t)
     t->fft_length = P.fft_L;
     t->fft_columns = P.fft_nc;
     t->fft_radix_order = P.fft_order;
-    t->tuned = P.tuned ? 1 : 0;
+    t->tuned = P.tuned ? (P.timed ? 1 : 2) : 0;
     t->ms_direct = P.tune_ms_direct;
     t->ms_fft = P.tune_ms_fft;
 }

@@ -457,12 +457,7 @@ template <typename IMG, int R>
 static int launch_sep(const void *d_img, const void *d_phiref, void *d_z, int W, int H, cudaStream_t s)
 {
     using G = SepGeom<IMG, R>;
-    static bool attr = false;
-    if (!attr) {
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(dpra_ls_sep_kernel<IMG, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)G::SMEM));
-        attr = true;
-    }
+    GLSU_TRY(raise_smem_limit((const void *)dpra_ls_sep_kernel<IMG, R>, (int)G::SMEM));
     dim3 blk(kDpraTX, kDpraTY), grd((W + kDpraTX - 1) / kDpraTX, (H + kDpraTY - 1) / kDpraTY);
     dpra_ls_sep_kernel<IMG, R><<<grd, blk, G::SMEM, s>>>((const IMG *)d_img, (const float *)d_phiref, (float2 *)d_z,
                                                          W, H);
@@ -474,12 +469,7 @@ template <typename IMG, int R>
 static int launch_ff(const void *d_img, const void *d_phiref, void *d_z, int W, int H, cudaStream_t s)
 {
     using G = FfGeom<R>;
-    static bool attr = false;
-    if (!attr) {
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(dpra_ls_ff_kernel<IMG, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)G::SMEM));
-        attr = true;
-    }
+    GLSU_TRY(raise_smem_limit((const void *)dpra_ls_ff_kernel<IMG, R>, (int)G::SMEM));
     dim3 blk(kDpraTX, kDpraTY), grd((W + kDpraTX - 1) / kDpraTX, (H + kDpraTY - 1) / kDpraTY);
     dpra_ls_ff_kernel<IMG, R><<<grd, blk, G::SMEM, s>>>((const IMG *)d_img, (const float *)d_phiref, (float2 *)d_z,
                                                         W, H);

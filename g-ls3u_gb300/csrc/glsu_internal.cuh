@@ -30,6 +30,13 @@ int cuda_fail(cudaError_t e, const char *what);
         if (rc_ != GLSU_OK) return rc_; \
     } while (0)
 
+// Raise the dynamic shared-memory limit of kernel `func` to `bytes` on the
+// current device, once per (kernel, device), thread-safe.  carveout >= 0 also
+// sets the kernel's preferred shared-memory carveout (percent).
+int raise_smem_limit(const void *func, int bytes, int carveout = -1);
+// Multiprocessor count of the current device (looked up once per device).
+int device_sm_count();
+
 // ---------------------------------------------------------------------------
 // complex element types
 // ---------------------------------------------------------------------------
@@ -173,13 +180,21 @@ struct WffPlan {
     int set_fft_plan(int nc, int order);
 
     // Autotuner (wff_colfft.cu): with GLSU_METHOD_AUTO the column sweep is
-    // the candidate (direct kernel or FFT plan variant) measured fastest for
-    // this shape, timed once per shape and process.
+    // chosen from the shape by a cost model (deterministic); with
+    // GLSU_METHOD_TIMED it is the candidate (direct kernel or FFT plan
+    // variant) measured fastest for this shape, timed once per shape and
+    // process.
     bool tuned = false;
+    bool timed = false;  // the last resolution was by timing
     int auto_method = GLSU_METHOD_DIRECT;
     float tune_ms_direct = 0, tune_ms_fft = 0;
     int autotune(cudaStream_t s);
-    int column_method() const { return method == GLSU_METHOD_AUTO ? auto_method : method; }
+    int choose_by_model();
+    double model_ms(int method) const;
+    int column_method() const
+    {
+        return (method == GLSU_METHOD_AUTO || method == GLSU_METHOD_TIMED) ? auto_method : method;
+    }
     bool use_colfft() const { return fft_L > 0 && d_khat != nullptr && column_method() == GLSU_METHOD_FFT; }
 };
 
@@ -189,6 +204,10 @@ int fft_length_candidates(const WffPlan &P, int *out, int n);
 int launch_column_sweep(WffPlan &P, cudaStream_t s);
 
 int launch_colfft(const WffPlan &P, cudaStream_t s);
+// Compact the ncx x ncy tiles (ty_rows x tx_cols outputs each) of a column
+// sweep that a masked run needs into list / *count (device, index order).
+int launch_mask_list(const TileMask &m, int ncx, int ncy, int ty_rows, int tx_cols, int2 *list, int *count,
+                     cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // kernel launchers

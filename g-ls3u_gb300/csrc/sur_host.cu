@@ -193,12 +193,7 @@ int SurNet::backward(const void *d_z, const void *d_target)
                                                                        d_grad + sur_layer_offset(7));
     sur_l7_bwd_kernel<<<g, 256, 0, stream>>>(d_dh, d_act[6], B, H, W, dil[7], d_w7r, d_g[0]);
     GLSU_CUDA_TRY(cudaGetLastError());
-    static int attr = 0;
-    const int need = sur_dw32_smem(64);
-    if (attr < need) {
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(sur_dw32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, need));
-        attr = need;
-    }
+    GLSU_TRY(raise_smem_limit((const void *)sur_dw32_kernel, sur_dw32_smem(64)));
     for (int l = 6; l >= 1; l--) {
         uint16_t *gl = d_g[(6 - l) & 1], *gprev = d_g[(7 - l) & 1];
         sur_dw32_kernel<<<nb32, 256, sur_dw32_smem(dil[l]), stream>>>(gl, d_act[l - 1], B, H, W, dil[l], d_part);

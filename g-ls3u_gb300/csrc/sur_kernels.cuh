@@ -47,6 +47,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 
 #include "glsu_internal.cuh"
@@ -430,22 +431,18 @@ int sur_make_out_map(CUtensorMap *tm, const void *act, int B, int H, int W)
 template <int NOUT>
 static int launch_sur_conv_t(const CUtensorMap &tm, const CUtensorMap &tmo, const SurConvArgs &a, cudaStream_t s)
 {
-    static int attr_bytes = 0, sms = 0, regs = 0;
+    // registers per thread are a property of the binary (the same on every device)
+    static std::atomic<int> regs_cached{0};
     const int smem = sur_conv_smem_bytes<NOUT>(a.dil);
-    if (smem > attr_bytes) {
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(sur_conv_tc_kernel<NOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           sur_conv_smem_bytes<NOUT>(64)));
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(sur_conv_tc_kernel<NOUT>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                           (int)cudaSharedmemCarveoutMaxShared));
-        attr_bytes = sur_conv_smem_bytes<NOUT>(64);
-    }
-    if (!sms) {
-        int dev = 0;
-        GLSU_CUDA_TRY(cudaGetDevice(&dev));
-        GLSU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GLSU_TRY(raise_smem_limit((const void *)sur_conv_tc_kernel<NOUT>, sur_conv_smem_bytes<NOUT>(64),
+                              (int)cudaSharedmemCarveoutMaxShared));
+    const int sms = device_sm_count();
+    int regs = regs_cached.load();
+    if (!regs) {
         cudaFuncAttributes fa;
         GLSU_CUDA_TRY(cudaFuncGetAttributes(&fa, sur_conv_tc_kernel<NOUT>));
         regs = std::max(1, fa.numRegs);
+        regs_cached.store(regs);
     }
     // persistent: as many CTAs as are resident at once, each walking a
     // strided list of items.  Residency is bounded by registers (per-warp

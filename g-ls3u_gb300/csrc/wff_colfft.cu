@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -30,6 +31,14 @@
 namespace glsu {
 
 constexpr int kFftThreads = 512;
+
+// Throughputs of the column-sweep cost model (WffPlan::model_ms), measured
+// on GB300: direct kernel in tap-units per second per instantiated
+// half-size, FFT sweep in (length x stages) units per second.
+constexpr double kModelDirectRate30 = 1.1e13;
+constexpr double kModelDirectRate45 = 5.5e12;
+constexpr double kModelDirectRate60 = 3.95e12;
+constexpr double kModelFftRate = 6.0e11;
 
 struct ColFftPlan {
     int L;
@@ -197,13 +206,19 @@ __device__ float2 *fft_run(float2 *a, float2 *b, const ColFftPlan &P, const floa
 // Registers are capped for two CTAs per SM: the stages are bound by shared
 // memory and block barriers, and a second CTA hides them (16-19% faster at
 // 1024^2 and 2048^2 despite 144-236 bytes of spills a thread).
+// A tile-masked run (the surrogate's per-tile fallback) passes the device
+// list of needed column groups (list, *list_count); each CTA then walks the
+// list with stride gridDim.x.  Without a list, CTA x is column group x.
+// Every column is computed the same way in both cases, so a masked run's
+// columns equal the full frame's bit for bit.
 template <int NC, int MAXE>
 __global__ void __launch_bounds__(kFftThreads, 2) wff_colfft_kernel(const float2 *__restrict__ R, float2 *__restrict__ Cout,
                                                                  int H, int pitch, int nfy,
                                                                  const float2 *__restrict__ khat,
                                                                  const float2 *__restrict__ tw, ColFftPlan P,
                                                                  const float *__restrict__ thr_ptr, float LN,
-                                                                 float out_scale)
+                                                                 float out_scale, const int2 *__restrict__ list,
+                                                                 const int *__restrict__ list_count)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = P.L;
@@ -211,9 +226,13 @@ __global__ void __launch_bounds__(kFftThreads, 2) wff_colfft_kernel(const float2
     float2 *bufA = reinterpret_cast<float2 *>(smem_raw);
     float2 *bufB = bufA + pidx(nel) + 1;
     const int tid = threadIdx.x;
-    const int x0 = blockIdx.x * NC, i = blockIdx.y;
+    const int i = blockIdx.y;
     const size_t plane = (size_t)H * pitch;
     const float2 *Ri = R + i * plane;
+    const int nitems = list ? *list_count : (int)gridDim.x;
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const int x0 = (list ? list[item].x : item) * NC;
+    __syncthreads();  // the previous item is done with the shared buffers
 
     // load the NC columns (rows >= H are zero)
     for (int e = tid; e < nel; e += kFftThreads) {
@@ -282,6 +301,7 @@ __global__ void __launch_bounds__(kFftThreads, 2) wff_colfft_kernel(const float2
             Ci[(size_t)rho * pitch + x0 + c] = make_float2(v.x * out_scale, v.y * out_scale);
         }
     }
+    }  // items
 }
 
 // ---------------------------------------------------------------------------
@@ -422,19 +442,29 @@ template <int NC, int MAXE> static int launch_colfft_t(const WffPlan &P, cudaStr
     for (int k = 0; k < 12; k++) cp.radix[k] = k < P.fft_nst ? P.fft_radix[k] : 0;
     const int nel = cp.L * NC;
     const size_t smem = sizeof(float2) * 2 * (size_t)(nel + (nel >> 4) + 1);
-    static bool attr = false;
-    if (!attr) {
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(wff_colfft_kernel<NC, MAXE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           112 * 1024));
-        attr = true;
-    }
+    GLSU_TRY(raise_smem_limit((const void *)wff_colfft_kernel<NC, MAXE>, 112 * 1024));
     if (smem > 112 * 1024) return fail(GLSU_ERR_UNSUPPORTED, "column FFT length too large");
     const double N = 1.0 / P.inv_norm;
-    dim3 grid(P.pitch / NC, P.nfx);
+    const int ngroups = P.pitch / NC;
+    dim3 grid(ngroups, P.nfx);
+    const int2 *list = nullptr;
+    const int *count = nullptr;
+    if (P.mask.flags) {
+        // tile-masked run: the column groups whose columns, grown by sx,
+        // meet a flagged tile (all rows: a column's transform spans them)
+        if (!P.d_list) return fail(GLSU_ERR_INVALID, "tile-masked run without a tile list buffer");
+        TileMask m = P.mask;
+        m.my = 0;
+        m.mx = P.sx;
+        GLSU_TRY(launch_mask_list(m, ngroups, 1, P.H, NC, P.d_list, P.d_list_count, s));
+        list = P.d_list;
+        count = P.d_list_count;
+        grid.x = std::max(1, std::min(ngroups, (2 * device_sm_count() + P.nfx - 1) / P.nfx));
+    }
     wff_colfft_kernel<NC, MAXE><<<grid, kFftThreads, smem, s>>>(
         (const float2 *)P.d_R, (float2 *)P.d_C, P.H, P.pitch, P.nfy, (const float2 *)P.d_khat,
         (const float2 *)P.d_tw, cp, (const float *)P.d_thr, (float)(cp.L * N),
-        (float)(1.0 / ((double)cp.L * cp.L * N)));
+        (float)(1.0 / ((double)cp.L * cp.L * N)), list, count);
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
 }
@@ -456,7 +486,13 @@ int launch_colfft(const WffPlan &P, cudaStream_t s)
 // ---------------------------------------------------------------------------
 // autotuner
 // ---------------------------------------------------------------------------
-// Candidates: the direct column kernel, and the FFT sweep at the three
+// GLSU_METHOD_AUTO (the default) decides from the shape alone, with a cost
+// model of the two column sweeps (model_ms below), so that the same inputs
+// give the same bits in every process and on every box.  The timed search
+// below runs only on request (GLSU_METHOD_TIMED, or GLSU_AUTOTUNE=time in
+// the environment).
+//
+// Timed search.  Candidates: the direct column kernel, and the FFT sweep at the three
 // cheapest transform lengths (L x stages), then, at the fastest length, with
 // 4 or 2 columns per CTA and each radix order.  Each is launched once
 // (warm-up), then twice between CUDA events on the plan's own buffers; the
@@ -480,14 +516,56 @@ std::mutex g_tune_mu;
 std::map<TuneKey, TuneResult> g_tune;
 }  // namespace
 
+// Modelled device time (ms) of one full-frame column sweep of this plan.
+// Direct kernel: per output pixel, x-frequency and y-frequency, two column
+// filters of 2S+1 taps (S the instantiated half-size), the first one also
+// over the 2S-row halo of each 128-row tile, at a rate per instantiation.
+// FFT sweep: per column and x-frequency, 2 nfy + 2 transforms of length L
+// with nst stages, at a rate scaled down when a CTA's L x columns elements
+// leave its 512 threads short of work.  The rates are GB300 measurements
+// (2070 MHz) of both kernels at 256^2 .. 2048^2.
+double WffPlan::model_ms(int m) const
+{
+    if (m == GLSU_METHOD_FFT) {
+        if (fft_L == 0) return 1e30;
+        const double units = (double)pitch * nfx * (2.0 * nfy + 2.0) * fft_L * fft_nst;
+        const double fill = std::min(1.0, (double)fft_L * fft_nc / (kFftThreads * 8.0));
+        return units / (kModelFftRate * fill) * 1e3;
+    }
+    const int S = syi;
+    const double taps = (2.0 * S + 1.0) * (2.0 + 2.0 * S / 128.0);
+    const double rate = S <= 30 ? kModelDirectRate30 : (S <= 45 ? kModelDirectRate45 : kModelDirectRate60);
+    return (double)pitch * H * nfx * nfy * taps / rate * 1e3;
+}
+
+// AUTO without timing: the transform length cheapest by L x stages (built
+// by init_colfft), the default plan variant, and the FFT sweep when its
+// modelled time is below 0.9 x the direct kernel's.
+int WffPlan::choose_by_model()
+{
+    auto_method = GLSU_METHOD_DIRECT;
+    if (prec != GLSU_F32 || fft_L == 0 || d_khat == nullptr) return GLSU_OK;
+    int L;
+    if (length_candidates(H + 2 * sy, &L, 1) == 1 && L != fft_L) GLSU_TRY(build_colfft(L));
+    GLSU_TRY(set_fft_plan(colfft_nc(fft_L), 0));
+    tune_ms_direct = (float)model_ms(GLSU_METHOD_DIRECT);
+    tune_ms_fft = (float)model_ms(GLSU_METHOD_FFT);
+    if (tune_ms_fft < 0.9f * tune_ms_direct) auto_method = GLSU_METHOD_FFT;
+    return GLSU_OK;
+}
+
 int WffPlan::autotune(cudaStream_t s)
 {
     tuned = true;
+    timed = false;
     auto_method = GLSU_METHOD_DIRECT;
     tune_ms_direct = tune_ms_fft = 0;
-    if (prec != GLSU_F32 || fft_L == 0 || d_khat == nullptr || mask.flags) return GLSU_OK;
+    if (prec != GLSU_F32 || fft_L == 0 || d_khat == nullptr) return GLSU_OK;
     const char *env = std::getenv("GLSU_AUTOTUNE");
     if (env && env[0] == '0') return GLSU_OK;
+    const bool want_timing = method == GLSU_METHOD_TIMED || (env && std::strcmp(env, "time") == 0);
+    if (!want_timing) return choose_by_model();
+    timed = true;
     const TuneKey key{{W, H, pitch, sx, sy, nfx, nfy, H + 2 * sy, (int)(1000 * p.wyl + 0.5)}};
     std::lock_guard<std::mutex> lock(g_tune_mu);
     auto it = g_tune.find(key);

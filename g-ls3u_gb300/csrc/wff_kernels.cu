@@ -304,9 +304,10 @@ __global__ void __launch_bounds__(ColGeom<T, S>::THREADS, 1)
     }
 }
 
-// Tiles (bx, by) of the column sweep whose outputs, grown by (0, mx), meet a
-// flagged tile, compacted in index order (one block; deterministic).
-__global__ void __launch_bounds__(1024) wff_mask_list_kernel(TileMask m, int ncx, int ncy, int ty_rows,
+// Tiles (bx, by) of ty_rows x tx_cols outputs of a column sweep whose
+// outputs, grown by the mask's margins, meet a flagged tile, compacted in
+// index order (one block; deterministic).
+__global__ void __launch_bounds__(1024) wff_mask_list_kernel(TileMask m, int ncx, int ncy, int ty_rows, int tx_cols,
                                                              int2 *__restrict__ list, int *__restrict__ count)
 {
     __shared__ int warp_sums[32];
@@ -321,7 +322,7 @@ __global__ void __launch_bounds__(1024) wff_mask_list_kernel(TileMask m, int ncx
         if (e < n) {
             by = e / ncx;
             bx = e - by * ncx;
-            need = m.any(by * ty_rows, by * ty_rows + ty_rows, bx * 32, bx * 32 + 32) ? 1 : 0;
+            need = m.any(by * ty_rows, by * ty_rows + ty_rows, bx * tx_cols, bx * tx_cols + tx_cols) ? 1 : 0;
         }
         const unsigned bal = __ballot_sync(0xffffffffu, need);
         if (lane == 0) warp_sums[w] = __popc(bal);
@@ -648,8 +649,9 @@ int WffPlan::make_tensor_map()
 int WffPlan::alloc_tile_list()
 {
     if (d_list) return GLSU_OK;
-    // column tiles are 32 columns x at least 32 rows
-    const size_t cap = (size_t)(pitch / 32) * ((H + 31) / 32);
+    // column tiles of the direct sweep are 32 columns x at least 32 rows;
+    // column groups of the FFT sweep are 2 or 4 whole columns
+    const size_t cap = std::max((size_t)(pitch / 32) * ((H + 31) / 32), (size_t)(pitch / 2));
     if (cudaMalloc((void **)&d_list, cap * sizeof(int2)) != cudaSuccess ||
         cudaMalloc((void **)&d_list_count, sizeof(int)) != cudaSuccess)
         return fail(GLSU_ERR_ALLOC, "cudaMalloc of the tile list failed");
@@ -691,6 +693,14 @@ int WffPlan::check_device_error(cudaStream_t s)
 }
 
 // ---- launch dispatch ------------------------------------------------------
+int launch_mask_list(const TileMask &m, int ncx, int ncy, int ty_rows, int tx_cols, int2 *list, int *count,
+                     cudaStream_t s)
+{
+    wff_mask_list_kernel<<<1, 1024, 0, s>>>(m, ncx, ncy, ty_rows, tx_cols, list, count);
+    GLSU_CUDA_TRY(cudaGetLastError());
+    return GLSU_OK;
+}
+
 static TileMask with_margins(TileMask m, int my, int mx)
 {
     m.my = my;
@@ -702,12 +712,7 @@ template <typename T, int S>
 static int launch_rows_demod(const WffPlan &P, const void *d_f, cudaStream_t s)
 {
     using G = RowGeom<T, S>;
-    static bool attr = false;
-    if (!attr) {
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(wff_rows_demod_kernel<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)G::SMEM));
-        attr = true;
-    }
+    GLSU_TRY(raise_smem_limit((const void *)wff_rows_demod_kernel<T, S>, (int)G::SMEM));
     dim3 grid(P.pitch / kRowTileCols, (P.H + kRowTileRows - 1) / kRowTileRows);
     wff_rows_demod_kernel<T, S><<<grid, 256, G::SMEM, s>>>(
         (const C2<T> *)d_f, P.W, P.H, P.pitch, (const C2<T> *)P.d_ex, P.nfx, (C2<T> *)P.d_R,
@@ -734,12 +739,7 @@ int WffPlan::enqueue_rows(cudaStream_t s, const void *d_f)
 template <typename T, int S> static int launch_cols(const WffPlan &P, cudaStream_t s)
 {
     using G = ColGeom<T, S>;
-    static bool attr = false;
-    if (!attr) {
-        GLSU_CUDA_TRY(
-            cudaFuncSetAttribute(wff_cols_kernel<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM));
-        attr = true;
-    }
+    GLSU_TRY(raise_smem_limit((const void *)wff_cols_kernel<T, S>, (int)G::SMEM));
     const int ncx = P.pitch / 32, ncy = (P.H + G::TY - 1) / G::TY;
     const Taps<T, S> gA = make_taps<T, S>(P.gy, P.sy, P.inv_norm), gB = make_taps<T, S>(P.gy, P.sy, 1.0);
     if (!P.mask.flags) {
@@ -749,15 +749,9 @@ template <typename T, int S> static int launch_cols(const WffPlan &P, cudaStream
         // tile-masked run: compact the needed column tiles on the device and
         // let a few CTAs per wx walk that list (an empty list costs one short
         // launch instead of a full grid of CTAs that exit at once)
-        static bool attr_l = false;
-        if (!attr_l) {
-            GLSU_CUDA_TRY(cudaFuncSetAttribute(wff_cols_list_kernel<T, S>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM));
-            attr_l = true;
-        }
+        GLSU_TRY(raise_smem_limit((const void *)wff_cols_list_kernel<T, S>, (int)G::SMEM));
         if (!P.d_list) return fail(GLSU_ERR_INVALID, "tile-masked run without a tile list buffer");
-        wff_mask_list_kernel<<<1, 1024, 0, s>>>(with_margins(P.mask, 0, P.sx), ncx, ncy, G::TY, P.d_list,
-                                                P.d_list_count);
+        GLSU_TRY(launch_mask_list(with_margins(P.mask, 0, P.sx), ncx, ncy, G::TY, 32, P.d_list, P.d_list_count, s));
         const int per_wx = std::max(1, std::min(ncx * ncy, (2 * 152 + P.nfx - 1) / P.nfx));
         wff_cols_list_kernel<T, S><<<dim3(per_wx, 1, P.nfx), G::THREADS, G::SMEM, s>>>(
             P.tmR, (C2<T> *)P.d_C, (const C2<T> *)P.d_ey, P.nfy, P.H, P.pitch, (const T *)P.d_thr, gA, gB, P.d_err,
@@ -772,12 +766,7 @@ static int launch_final(const WffPlan &P, void *d_out, const void *phiref, const
                         void *dphi, cudaStream_t s)
 {
     using G = RowGeom<T, S>;
-    static bool attr = false;
-    if (!attr) {
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(wff_rows_final_kernel<T, S, MODE>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM));
-        attr = true;
-    }
+    GLSU_TRY(raise_smem_limit((const void *)wff_rows_final_kernel<T, S, MODE>, (int)G::SMEM));
     dim3 grid(P.pitch / kRowTileCols, (P.H + kRowTileRows - 1) / kRowTileRows);
     wff_rows_final_kernel<T, S, MODE><<<grid, 256, G::SMEM, s>>>(
         (const C2<T> *)P.d_C, P.W, P.H, P.pitch, (const C2<T> *)P.d_ex, P.nfx,
@@ -789,7 +778,7 @@ static int launch_final(const WffPlan &P, void *d_out, const void *phiref, const
 
 template <typename T> static int launch_cols_any(WffPlan &P, cudaStream_t s)
 {
-    if (sizeof(T) == 4 && P.use_colfft() && !P.mask.flags) return launch_colfft(P, s);
+    if (sizeof(T) == 4 && P.use_colfft()) return launch_colfft(P, s);
     switch (P.syi) {
     case 12: return launch_cols<T, 12>(P, s);
     case 20: return launch_cols<T, 20>(P, s);

@@ -345,28 +345,13 @@ template <int S> static PTaps<float, S> probe_taps(const double *g, int strue, d
     return t;
 }
 
-static int sm_count()
-{
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
-    }
-    return n;
-}
+static int sm_count() { return device_sm_count(); }
 
 template <int S> static int launch_probe_sweep(WffPlan &Pl, ProbeArgs a, cudaStream_t s)
 {
     using G = ProbeGeom<S>;
-    static bool attr = false;
-    if (!attr) {
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(wff_probe_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)G::SMEM));
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(wff_probe_rows_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)G::RSMEM));
-        attr = true;
-    }
+    GLSU_TRY(raise_smem_limit((const void *)wff_probe_kernel<S>, (int)G::SMEM));
+    GLSU_TRY(raise_smem_limit((const void *)wff_probe_rows_kernel<S>, (int)G::RSMEM));
     const int ntiles = a.ntx * a.nty;
     // split the wy range (at most 4 parts) so that the last wave of CTAs is well filled
     const int per_sm = (int)((228 * 1024) / (G::SMEM + 1024));

@@ -265,12 +265,7 @@ template <typename T, int S>
 static int launch_wfr_cols(const WffPlan &P, const WfrBuffers &wb, cudaStream_t s)
 {
     using G = WfrGeom<T, S>;
-    static bool attr = false;
-    if (!attr) {
-        GLSU_CUDA_TRY(
-            cudaFuncSetAttribute(wfr_cols_kernel<T, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM));
-        attr = true;
-    }
+    GLSU_TRY(raise_smem_limit((const void *)wfr_cols_kernel<T, S>, (int)G::SMEM));
     const Taps<T, S> gA = make_taps<T, S>(P.gy, P.sy, P.inv_norm);
     dim3 grid(P.pitch / 32, (P.H + G::TY - 1) / G::TY, P.nfx);
     wfr_cols_kernel<T, S><<<grid, G::THREADS, G::SMEM, s>>>(P.tmR, (const C2<T> *)P.d_ex, (const C2<T> *)P.d_ey,

@@ -36,7 +36,7 @@ ERR_UNSUPPORTED, ERR_NOT_POSDEF, ERR_TIMEOUT, ERR_NO_DEVICE = -5, -6, -7, -8
 F32, F64, U8 = 0, 1, 2
 PHI_REF, PHI_CURR, DPHI_REF, DPHI = 0, 1, 2, 3
 WFT_WFF, WFT_WFR = 0, 1
-METHOD_AUTO, METHOD_DIRECT, METHOD_FFT = 0, 1, 2
+METHOD_AUTO, METHOD_DIRECT, METHOD_FFT, METHOD_TIMED = 0, 1, 2, 3
 LS_FLOAT_FLOAT, LS_FP64_SUMS = 0, 1
 
 _lock = threading.Lock()
@@ -329,7 +329,7 @@ class WFF2:
         check(lib().glsu_wff_run_async(self._h, ctypes.c_void_p(d_f), ctypes.c_void_p(d_out)))
 
     def set_method(self, method: int):
-        """Column-sweep method: METHOD_AUTO, METHOD_DIRECT or METHOD_FFT."""
+        """Column-sweep method: METHOD_AUTO, METHOD_DIRECT, METHOD_FFT or METHOD_TIMED."""
         check(lib().glsu_wff_set_method(self._h, method))
 
     def tuning(self) -> dict:
@@ -448,7 +448,7 @@ class DPRA:
         return p.value
 
     def set_method(self, method: int):
-        """Column-sweep method of the WFF2: METHOD_AUTO, METHOD_DIRECT or METHOD_FFT."""
+        """Column-sweep method of the WFF2: METHOD_AUTO, METHOD_DIRECT, METHOD_FFT or METHOD_TIMED."""
         check(lib().glsu_dpra_set_method(self._h, method))
 
     def tuning(self) -> dict:

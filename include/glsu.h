@@ -54,11 +54,15 @@ extern "C" {
 /* Column-sweep method of the WFF2 (glsu_wff_set_method / glsu_dpra_set_method):
  * DIRECT convolves the columns with the truncated window; FFT (FP32 form
  * only) does the same in the frequency domain of each column with
- * shared-memory transforms; AUTO (the default) runs whichever the
- * autotuner measured faster for the handle's shape (glsu_wff_tuning). */
+ * shared-memory transforms.  AUTO (the default) picks one of the two from
+ * the handle's shape with a cost model of both kernels, so the choice, and
+ * therefore every output bit, is the same in every process.  TIMED picks
+ * the one measured fastest on this GPU (glsu_wff_tuning); its choice can
+ * differ from run to run where the two are close. */
 #define GLSU_METHOD_AUTO 0
 #define GLSU_METHOD_DIRECT 1
 #define GLSU_METHOD_FFT 2
+#define GLSU_METHOD_TIMED 3
 
 /* Arithmetic of the FP32 DPRA least squares (glsu_dpra_set_ls_method): the
  * window sums and the solve need more than FP32's 24 bits where phi_ref is
@@ -120,24 +124,28 @@ int glsu_wff_threshold(glsu_wff *h, double *thr);
  * rounding.  GLSU_METHOD_FFT fails with GLSU_ERR_UNSUPPORTED where no
  * transform plan exists (FP64 handles). */
 int glsu_wff_set_method(glsu_wff *h, int method);
-/* Column-sweep autotuner.  With GLSU_METHOD_AUTO (the default) the handle
- * runs the column sweep measured fastest for its shape: the direct kernel,
- * or the shared-memory FFT sweep at one of the three cheapest transform
- * lengths with 4 or 2 columns per CTA and one of three radix orders
- * (0: 8,4,2,5,3; 1: 4,2,5,3; 2: 5,3,8,4,2).  The first
- * handle of a shape in the process times the candidates at creation (a few
+/* Column-sweep autotuner.
+ * GLSU_METHOD_AUTO (the default): the FFT sweep at the transform length
+ * cheapest by length x stages, with its default plan variant, when the cost
+ * model puts it below 0.9 x the direct kernel's time; else the direct
+ * kernel.  Decided from the shape only: deterministic.
+ * GLSU_METHOD_TIMED: the handle runs the column sweep measured fastest for
+ * its shape: the direct kernel, or the shared-memory FFT sweep at one of
+ * the three cheapest transform lengths with 4 or 2 columns per CTA and one
+ * of three radix orders (0: 8,4,2,5,3; 1: 4,2,5,3; 2: 5,3,8,4,2).  The
+ * first handle of a shape in the process times the candidates (a few
  * launches each); later handles of that shape reuse the choice.  The FFT is
- * taken only when at least 10% faster.  Setting GLSU_AUTOTUNE=0 in the
- * environment skips the timing: AUTO is then the direct kernel.  The methods
- * agree to FP32 rounding, not bit for bit. */
+ * taken only when at least 10% faster.  GLSU_AUTOTUNE=time in the
+ * environment makes AUTO behave as TIMED; GLSU_AUTOTUNE=0 makes both the
+ * direct kernel.  The methods agree to FP32 rounding, not bit for bit. */
 typedef struct {
     int method;          /* GLSU_METHOD_DIRECT or GLSU_METHOD_FFT: the sweep that runs */
     int fft_length;      /* transform length of the FFT plan (0: no FFT plan) */
     int fft_columns;     /* columns per CTA of the FFT sweep */
     int fft_radix_order; /* radix order of the FFT stages (see above) */
-    int tuned;           /* 1: the autotuner resolved AUTO for this shape */
-    float ms_direct;     /* measured column-sweep time of the direct kernel (0: not timed) */
-    float ms_fft;        /* best measured time of the FFT sweep (0: not timed) */
+    int tuned;           /* 0: not resolved; 1: resolved by timing; 2: by the cost model */
+    float ms_direct;     /* column-sweep time of the direct kernel: measured (tuned 1) or modelled (tuned 2) */
+    float ms_fft;        /* time of the FFT sweep: best measured (tuned 1) or modelled (tuned 2) */
 } glsu_wff_tuning;
 int glsu_wff_get_tuning(const glsu_wff *h, glsu_wff_tuning *t);
 /* Force an FFT plan variant (the autotuner's knobs); GLSU_ERR_UNSUPPORTED
@@ -170,11 +178,17 @@ int glsu_wff_padded_size(const glsu_wff *h, int *padded_width, int *padded_heigh
  * message giving the size needed (256x256 with 21x21 frequencies uses 22 MiB).
  *
  * The first call on a device looks up that array's device address (once
- * per device, with the device current); make that first call before any
- * stream capture.  All calls share the array and each call overwrites it,
- * so calls whose work overlaps on the GPU race: serialise them.  The call
- * returns when the result is complete.  An automatic threshold (thr < 0) is
- * recomputed on every call, since nothing is kept between calls. */
+ * per device, with the device current).  Every call blocks until its result
+ * is complete: it synchronises the stream to read back the kernels' error
+ * word, so it must not be called while that stream (or the legacy default
+ * stream it may be) is being captured into a CUDA graph.  All calls share
+ * the array and each call overwrites it, so calls whose work overlaps on
+ * the GPU race: serialise them.  An automatic threshold (thr < 0) is
+ * recomputed on every call, since nothing is kept between calls.
+ *
+ * The column sweep is always the direct kernel (GLSU_METHOD_DIRECT): its
+ * output equals glsu_wff_run's bit for bit when that handle also runs the
+ * direct kernel, and agrees with the FFT column sweep to FP32 rounding. */
 int glsu_wff_run_noalloc(int width, int height, const glsu_wff_params *p, const void *d_f, void *d_filtered,
                          void *cuda_stream);
 

@@ -99,3 +99,23 @@ def test_frequency_count_float_and_double_can_differ(glsu):
     and WFT2_cpu / WFT2_CUDA (double): int(1.8 * (1/0.3)) + 1."""
     assert glsu.wff_count(-0.9, 0.9, 0.3, glsu.F64) == 7
     assert glsu.wff_count(-0.9, 0.9, 0.3, glsu.F32) == 6
+
+
+def test_kernel_attribute_record_is_per_device(tmp_path):
+    """The record of raised shared-memory limits (csrc/func_attr.hpp) is kept
+    per kernel and device and is consistent across threads (g++, no GPU)."""
+    import os
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "test_func_attr")
+    r = subprocess.run([gxx, "-O1", "-std=c++17", "-pthread", "-I", os.path.join(root, "g-ls3u_gb300", "csrc"),
+                        os.path.join(root, "tests", "cpp", "test_func_attr.cpp"), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr

@@ -2,8 +2,9 @@
 -> per-tile plain-WFF2 fallback -> phase update), on the GPU.
 
 Bit-exact checks: a tile recomputed by the plain WFF2 runs the same kernels
-on the same data as the plain path with the direct column kernel, so its
-phases equal that path's bit for bit; a tile left to the network equals the
+on the same data as the plain path, with the same column sweep (direct
+kernel or shared-memory FFT sweep, whichever the handle uses), so its phases
+equal that path's bit for bit; a tile left to the network equals the
 network-only run.
 """
 import numpy as np
@@ -14,6 +15,10 @@ pytestmark = pytest.mark.gpu
 DIL = [1, 2, 4, 8, 16, 8, 4, 1]
 H, W, TILE, PATCH = 200, 300, 64, 8
 WP = (6.0, -1.0, 1.0, 0.25, 6.0, -1.0, 1.0, 0.25, 0.2)
+# a wide window with few frequencies, where the cost model picks the FFT
+# column sweep (half-size 45: 4 x 4 probe patches)
+WIDE = dict(H=512, W=512, TILE=128, PATCH=4, WP=(15.0, -0.75, 0.75, 0.25, 15.0, -0.75, 0.75, 0.25, 0.2))
+NARROW = dict(H=H, W=W, TILE=TILE, PATCH=PATCH, WP=WP)
 
 
 def _torch():
@@ -27,15 +32,18 @@ def _params(glsu, seed=3):
     return T.init_params(seed, scale_last=1.0)
 
 
-def _run(glsu, synth, params, tol, nframes=3, seed=11):
-    frames, phi0, _ = synth.sequence(H, W, nframes, seed=seed)
-    d = glsu.DPRA(phi0.astype(np.float32), 1, 3, "f32", glsu.WffParams(*WP))
-    # the per-tile fallback runs the direct column kernel; so does the plain
-    # reference here (the autotuner could pick the FFT sweep for this shape)
-    d.set_method(glsu.METHOD_DIRECT)
+def _run(glsu, synth, params, tol, nframes=3, seed=11, method=None, case=None, tuning=None):
+    c = case or NARROW
+    h, w, tile, patch = c["H"], c["W"], c["TILE"], c["PATCH"]
+    frames, phi0, _ = synth.sequence(h, w, nframes, seed=seed)
+    d = glsu.DPRA(phi0.astype(np.float32), 1, 3, "f32", glsu.WffParams(*c["WP"]))
+    if method is not None:
+        d.set_method(method)
+    if tuning is not None:
+        tuning.append(d.tuning())
     if params is not None:
-        d.set_surrogate(params, DIL, TILE, PATCH, tol)
-    ntiles = ((H + TILE - 1) // TILE) * ((W + TILE - 1) // TILE)
+        d.set_surrogate(params, DIL, tile, patch, tol)
+    ntiles = ((h + tile - 1) // tile) * ((w + tile - 1) // tile)
     out, stats, lsq = [], [], []
     for f in frames[1:]:
         dphi, _ = d.per_frame(f)
@@ -48,25 +56,36 @@ def _run(glsu, synth, params, tol, nframes=3, seed=11):
     return out, stats, lsq
 
 
-def _tiles():
-    for ty in range(0, H, TILE):
-        for tx in range(0, W, TILE):
-            yield (slice(ty, min(H, ty + TILE)), slice(tx, min(W, tx + TILE)))
+def _tiles(case=None):
+    c = case or NARROW
+    for ty in range(0, c["H"], c["TILE"]):
+        for tx in range(0, c["W"], c["TILE"]):
+            yield (slice(ty, min(c["H"], ty + c["TILE"])), slice(tx, min(c["W"], tx + c["TILE"])))
 
 
-def test_all_flagged_tiles_equal_the_plain_path(glsu, synth):
-    plain, _, _ = _run(glsu, synth, None, 0)
-    sur, stats, _ = _run(glsu, synth, _params(glsu), 1e-12)
+@pytest.mark.parametrize("which", ["direct", "fft", "auto_wide"])
+def test_all_flagged_tiles_equal_the_plain_path(glsu, synth, which):
+    """With a zero-width tolerance every probed tile is recomputed by the
+    plain WFF2 and must equal the plain frame bit for bit, whichever column
+    sweep the handle runs: the direct kernel, the FFT sweep, or the default
+    (AUTO) on a shape where it is the FFT sweep."""
+    method = {"direct": glsu.METHOD_DIRECT, "fft": glsu.METHOD_FFT, "auto_wide": None}[which]
+    case = WIDE if which == "auto_wide" else NARROW
+    tu = []
+    plain, _, _ = _run(glsu, synth, None, 0, method=method, case=case, tuning=tu)
+    if which == "auto_wide":
+        assert tu[0]["method"] == glsu.METHOD_FFT and tu[0]["tuned"] == 2, tu[0]
+    sur, stats, _ = _run(glsu, synth, _params(glsu), 1e-12, method=method, case=case)
     for k, ((pd, pc), (sd, sc), st) in enumerate(zip(plain, sur, stats)):
         resid = st[2]
         n_checked = 0
-        for t, (ys, xs) in enumerate(_tiles()):
+        for t, (ys, xs) in enumerate(_tiles(case)):
             if resid[t] > 1e-12:
                 assert np.array_equal(sd[ys, xs], pd[ys, xs]), (k, t)
                 assert np.array_equal(sc[ys, xs], pc[ys, xs]), (k, t)
                 n_checked += 1
         assert n_checked >= len(resid) - 1
-    print("probed/flagged:", stats[-1][:2])
+    print("%s: probed/flagged %s" % (which, stats[-1][:2]))
 
 
 def test_probe_residual_matches_host_recomputation(glsu, synth):
@@ -98,21 +117,23 @@ def test_probe_residual_matches_host_recomputation(glsu, synth):
     print("probe residuals (rad):", np.round(resid, 3))
 
 
-def test_mixed_tiles_come_from_the_right_path(glsu, synth):
+@pytest.mark.parametrize("which", ["direct", "fft"])
+def test_mixed_tiles_come_from_the_right_path(glsu, synth, which):
+    method = glsu.METHOD_DIRECT if which == "direct" else glsu.METHOD_FFT
     p = _params(glsu)
-    _, stats, _ = _run(glsu, synth, p, 1e9, nframes=2)
+    _, stats, _ = _run(glsu, synth, p, 1e9, nframes=2, method=method)
     resid = stats[0][2]
     tol = float(np.median(resid))
-    plain, _, _ = _run(glsu, synth, None, 0, nframes=2)
-    net_only, _, _ = _run(glsu, synth, p, 1e9, nframes=2)
-    mixed, mstats, _ = _run(glsu, synth, p, tol, nframes=2)
+    plain, _, _ = _run(glsu, synth, None, 0, nframes=2, method=method)
+    net_only, _, _ = _run(glsu, synth, p, 1e9, nframes=2, method=method)
+    mixed, mstats, _ = _run(glsu, synth, p, tol, nframes=2, method=method)
     flagged = resid > tol
     assert 0 < flagged.sum() < len(resid)
     assert mstats[0][1] == flagged.sum()
     for t, (ys, xs) in enumerate(_tiles()):
         ref = plain[0][0] if flagged[t] else net_only[0][0]
         assert np.array_equal(mixed[0][0][ys, xs], ref[ys, xs]), t
-    print("tol %.3f: %d of %d tiles recomputed" % (tol, flagged.sum(), len(resid)))
+    print("%s, tol %.3f: %d of %d tiles recomputed" % (which, tol, flagged.sum(), len(resid)))
 
 
 def test_probe_overlap_gives_the_serial_result(glsu, synth):

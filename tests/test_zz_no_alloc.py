@@ -24,20 +24,36 @@ def _field(shape, seed):
     return (np.exp(1j * phi) * (1 + 0.1 * rng.standard_normal(shape))).astype(np.complex64)
 
 
-def _noalloc(glsu, torch, f, params):
-    a = torch.from_numpy(f).cuda()
-    out = torch.full_like(a, complex(np.nan, np.nan))
-    torch.cuda.synchronize()
+def _noalloc(glsu, torch, f, params, stream=None):
+    """One call of the entry point.  With a torch stream, the input is written
+    and the output read on that stream and the call is given its handle."""
+    if stream is None:
+        a = torch.from_numpy(f).cuda()
+        out = torch.full_like(a, complex(np.nan, np.nan))
+        torch.cuda.synchronize()
+        sp = None
+    else:
+        host = torch.from_numpy(f).pin_memory()
+        with torch.cuda.stream(stream):
+            a = host.to("cuda", non_blocking=True)
+            out = torch.full_like(a, complex(np.nan, np.nan))
+        sp = ctypes.c_void_p(stream.cuda_stream)
     rc = glsu.lib().glsu_wff_run_noalloc(f.shape[1], f.shape[0], ctypes.byref(params.c()),
-                                         ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(out.data_ptr()), None)
+                                         ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(out.data_ptr()), sp)
     glsu.check(rc)
-    return out.cpu().numpy()
+    if stream is None:
+        return out.cpu().numpy()
+    with torch.cuda.stream(stream):
+        res = out.cpu().numpy()
+    return res
 
 
-def _allocating(glsu, torch, f, params):
+def _allocating(glsu, torch, f, params, method=None):
     a = torch.from_numpy(f).cuda()
     out = torch.empty_like(a)
     w = glsu.WFF2(f.shape[1], f.shape[0], "f32", params)
+    if method is not None:
+        w.set_method(method)
     w.run(a.data_ptr(), out.data_ptr())
     w.close()
     return out.cpu().numpy()
@@ -49,15 +65,16 @@ CASES = [
 ]
 
 
-@pytest.mark.parametrize("case", range(len(CASES)))
-def test_no_alloc_matches_allocating_entry_point(glsu, case):
+@pytest.mark.parametrize("case,on_stream", [(0, False), (1, False), (0, True)])
+def test_no_alloc_matches_allocating_entry_point(glsu, case, on_stream):
     torch = pytest.importorskip("torch")
     assert torch.cuda.is_available(), "needs a CUDA device"
     shape, p = CASES[case]
     params = glsu.WffParams(*p)
+    stream = torch.cuda.Stream() if on_stream else None
     for seed in (case * 10 + 1, case * 10 + 2):  # two calls in a row on different inputs
         f = _field(shape, seed)
-        got = _noalloc(glsu, torch, f, params)
+        got = _noalloc(glsu, torch, f, params, stream)
         ref = _allocating(glsu, torch, f, params)
         mag = np.abs(ref)
         m = mag > 0.05 * mag.max()
@@ -77,3 +94,16 @@ def test_no_alloc_rejects_problems_beyond_its_scratch(glsu):
     assert rc == glsu.ERR_INVALID
     msg = glsu.lib().glsu_last_error().decode()
     assert "64 MiB" in msg and "needs" in msg
+
+
+def test_no_alloc_equals_direct_sweep_bit_for_bit(glsu):
+    """The entry point runs the direct column sweep, so against an allocating
+    handle forced onto that sweep the two outputs are identical."""
+    torch = pytest.importorskip("torch")
+    shape, p = CASES[0]
+    params = glsu.WffParams(*p)
+    for seed in (5, 6):
+        f = _field(shape, seed)
+        got = _noalloc(glsu, torch, f, params)
+        ref = _allocating(glsu, torch, f, params, method=glsu.METHOD_DIRECT)
+        assert np.array_equal(got, ref)
