@@ -1,8 +1,8 @@
 """Regenerate the golden fixtures in this folder from the reference project.
 
-Run in a checkout that has the reference at REF (default /root/reference):
+Run with the path of a reference checkout (read only):
 
-    python tests/golden/make_golden.py [REF]
+    python tests/golden/make_golden.py REF
 
 Nothing at test time reads the reference; the tests read only the files this
 script writes:
@@ -106,4 +106,6 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout>")
+    main(sys.argv[1])
