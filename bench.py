@@ -68,6 +68,9 @@ SUR_CONV_BYTES_PER_PX, SUR_CONV_FLOPS_PER_PX = 128, 2 * 288 * 32
 # from the ncu capture summarised in profiles/sur_conv_tc_kernel_1024.md
 SUR_CONV_TRAFFIC_1024 = 67.170304e6 + 21.358592e6
 SIZE = 1024
+# the surrogate form's deployment check: held-out seeds (training used
+# 10000.., 20000.., 90000.., 95000..), free-running frames, sampling period
+DEPLOY_SEED0, DEPLOY_SEEDS, DEPLOY_FRAMES, DEPLOY_EVERY = 50000, 10, 200, 20
 RADIUS = 3
 WFF = (10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)
 NFX = NFY = 21
@@ -81,8 +84,6 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=SIZE)
-    ap.add_argument("--cpu-rows", type=int, default=None,
-                    help="frequency rows (of 21) in the CPU-baseline sample (default: one per host thread)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--frames-only", action="store_true",
                     help="only the timed plain and surrogate frames (no AIA, WFR, e2e or accuracy runs): "
@@ -222,20 +223,20 @@ def barrier(world: int):
 
 # ---------------------------------------------------------------------------
 def cpu_sample(size, rows=None, seed=1000, prec="f32"):
-    """Bounded CPU sample of the same frame with the oracle restatements of
-    the reference's CPU path: full DPRA LS + update, WFF2 over `rows` of the
-    21 frequency rows.  The WFF2 sweep runs one frequency row per OpenMP
-    thread at a time (as the reference's does), so the sample is one round of
-    rows (rows = threads by default) and the frame is extrapolated by rounds:
-    ceil(21 / threads) rounds of that duration.  prec "f64": DPRA_CPU /
+    """One frame of the CPU path with the oracle restatements of the
+    reference's CPU classes: DPRA LS, WFF2 over `rows` of the 21 frequency
+    rows (all of them by default: the whole frame), phase update.  The WFF2
+    sweep runs one frequency row per OpenMP thread at a time, as the
+    reference's does (WFT/WFT2_CPU.cpp:227-237).  prec "f64": DPRA_CPU /
     WFT2_cpu (glsu_oracle.c); "f32": the float classes DPRA_CPUF / WFT2_cpuF
-    (glsu_oracle_f32.c).  Returns (frames_per_s, seconds, threads, rows)."""
+    (glsu_oracle_f32.c).  Returns (frames_per_s, seconds, threads, rows);
+    with rows < 21 the rate is that of the partial frame (warm-up only)."""
     from oracle import oracle as O
     from glsu import synth
     O.build()
     frames, phi0, _ = synth.sequence(size, size, 2, seed=seed)
     threads = os.cpu_count() or 1
-    rows = min(NFY, threads) if rows is None else max(1, min(NFY, rows))
+    rows = NFY if rows is None else max(1, min(NFY, rows))
     wp = O.WffParams(*WFF)
     if prec == "f64":
         ls, wff, upd, img, pref = O.dpra_ls, O.wff2, O.dpra_update, frames[1].astype(np.float64), phi0
@@ -243,46 +244,49 @@ def cpu_sample(size, rows=None, seed=1000, prec="f32"):
         ls, wff, upd, img, pref = O.dpra_ls_f32, O.wff2_f32, O.dpra_update_f32, frames[1], phi0.astype(np.float32)
     t0 = time.perf_counter()
     z = ls(img, pref, RADIUS, threads)
-    t1 = time.perf_counter()
     filt = wff(z, *wp.tuple(), nthreads=threads, ky=(0, rows))
     if isinstance(filt, tuple):
         filt = filt[0]
-    t2 = time.perf_counter()
     upd(filt, pref, np.zeros_like(pref))
-    t3 = time.perf_counter()
-    rounds = -(-NFY // threads) / -(-rows // threads)
-    per_frame = (t1 - t0) + (t2 - t1) * rounds + (t3 - t2)
-    return 1.0 / per_frame, t3 - t0, threads, rows
+    el = time.perf_counter() - t0
+    return 1.0 / el, el, threads, rows
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU algorithm (the oracle restatements of its CPU
+    classes) on the host cores, rank 0 only: every timed step is one whole
+    1024^2 frame (all 441 frequencies).  The first warm-up step times one
+    round of frequency rows in each precision to pick the faster variant;
+    the other warm-up steps run one frequency row."""
     if rank != 0:
         return None
     steps, warm = args.steps, args.warmup
-    # warm-up: both variants; the timed steps run the faster one
-    vw = {"f32": [], "f64": []}
-    for _ in range(max(1, warm)):
-        for prec in vw:
-            vw[prec].append(cpu_sample(args.size, prec=prec)[0])
-    best = max(vw, key=lambda k: max(vw[k]))
-    tot = 0.0
+    threads = os.cpu_count() or 1
+    vw = {}
+    for prec in ("f32", "f64"):
+        vw[prec] = cpu_sample(args.size, rows=min(NFY, threads), prec=prec)[1]
+    best = min(vw, key=vw.get)
+    for _ in range(max(0, warm - 1)):
+        cpu_sample(args.size, rows=1, prec=best)
+    times = []
     for _ in range(steps):
-        v, _, threads, rows = cpu_sample(args.size, prec=best)
-        tot += 1.0 / v
+        _, el, threads, rows = cpu_sample(args.size, prec=best)
+        times.append(el)
+    tot = float(sum(times))
     value = steps / tot
-    value32, value64 = (value, max(vw["f64"])) if best == "f32" else (max(vw["f32"]), value)
-    sample = ("per step: one %dx%d frame, DPRA LS + update in full, WFF2 over %d of 21 frequency rows "
-              "(one row per OpenMP thread, %d threads), extrapolated by rounds of rows to the 441 frequencies; "
-              "the restatement of the reference's %s CPU classes, the faster of the FP32 (DPRA_CPUF/WFT2_cpuF) "
-              "and FP64 (DPRA_CPU/WFT2_cpu) variants in the warm-up"
-              % (args.size, args.size, rows, threads, "float" if best == "f32" else "double"))
+    sample = ("per step: one whole %dx%d frame on the host cores (%d threads): DPRA LS (7x7), WFF2 over all "
+              "21 x 21 frequencies (one frequency row per OpenMP thread at a time, as the reference schedules "
+              "it), phase update; the restatement of the reference's %s CPU classes (%s), the faster variant "
+              "in the warm-up (one round of rows: FP32 %.1f s, FP64 %.1f s)"
+              % (args.size, args.size, threads, "float" if best == "f32" else "double",
+                 "DPRA_CPUF/WFT2_cpuF" if best == "f32" else "DPRA_CPU/WFT2_cpu", vw["f32"], vw["f64"]))
     return {
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": args.gpus, "steps": steps,
-        "warmup": warm, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
+        "warmup": warm, "ms_per_step": 1e3 * tot / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": best, "data": "synthetic",
         "config": workload_config(args.size), "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port", "sample": sample,
-                         "fp32_value": value32, "fp64_value": value64},
+                         "step_seconds": times},
         "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -338,26 +342,69 @@ def timed_frames(glsu, torch, d, dfr, nfr, args, stream, flush, world, local):
     return world * args.steps / (max_ms / 1e3), max_ms, stage / STAGE_FRAMES, clk
 
 
-def e2e_sequence(glsu, torch, make_handle, frames, args, stream, flush, world):
-    """Frames/s through glsu_dpra_sequence with pinned host frames and
-    outputs: a fresh handle (reference phase phi0) runs warm-up frames
-    0..W-1, then the timed call runs frames W..W+K-1 of the same sequence."""
-    size = frames.shape[-1]
-    d = make_handle()
-    W, K = args.warmup, args.steps
-    hwarm = torch.from_numpy(np.ascontiguousarray(frames[:W])).pin_memory()
-    hseq = torch.from_numpy(np.ascontiguousarray(frames[W:W + K])).pin_memory()
-    hout = torch.empty((max(W, K), size, size), dtype=torch.float32).pin_memory()
-    d.sequence_ptr(W, hwarm.data_ptr(), glsu.F32, hout.data_ptr())  # warms the copy streams
-    with torch.cuda.stream(stream):
-        flush.zero_()
-    torch.cuda.synchronize()
-    barrier(world)
-    t0 = time.perf_counter()
-    d.sequence_ptr(K, hseq.data_ptr(), glsu.F32, hout.data_ptr())
-    el = reduce_max(time.perf_counter() - t0, world)
-    d.close()
-    return world * K / el
+E2E_FRAMES, E2E_RUNS = 200, 3
+
+
+def host_sequence(torch, size, nframes, seed):
+    """nframes consecutive frames of the seeded generator in pinned host
+    memory (made on the GPU: synth.DeviceSequence), and its phi0."""
+    from glsu import synth
+    seq = synth.DeviceSequence(size, size, seed=seed)
+    h = torch.empty((nframes, size, size), dtype=torch.float32).pin_memory()
+    for k in range(nframes):
+        h[k].copy_(seq.frame(k + 1), non_blocking=False)
+    return h, seq.phi0
+
+
+def copy_times(torch, size, reps=20):
+    """Device time (ms) of one frame's H2D copy (4 B/px from pinned memory)
+    and one dphi D2H copy, each alone on a stream."""
+    st = torch.cuda.Stream()
+    hin = torch.empty((size, size), dtype=torch.float32).pin_memory()
+    hout = torch.empty_like(hin).pin_memory()
+    dev = torch.empty((size, size), dtype=torch.float32, device="cuda")
+    res = []
+    for direction in ("h2d", "d2h"):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(st):
+            for k in range(reps + 2):
+                if k == 2:
+                    e0.record(st)
+                if direction == "h2d":
+                    dev.copy_(hin, non_blocking=True)
+                else:
+                    hout.copy_(dev, non_blocking=True)
+            e1.record(st)
+        st.synchronize()
+        res.append(e0.elapsed_time(e1) / reps)
+    return res
+
+
+def e2e_sequence(glsu, torch, make_handle, hframes, args, stream, flush, world):
+    """Frames/s end to end through glsu_dpra_sequence, the public sequence
+    call: after W warm-up frames on a fresh handle (reference phase phi0), one
+    call runs E2E_FRAMES pinned host frames, uploads, compute and dphi
+    downloads overlapped on the handle's copy streams, and returns when every
+    output is on the host; wall clock around that call, max over ranks, the
+    median of E2E_RUNS runs."""
+    W = args.warmup
+    K = hframes.shape[0] - W
+    hout = torch.empty(hframes.shape[1:], dtype=torch.float32).unsqueeze(0).expand(K, -1, -1).contiguous()
+    hout = hout.pin_memory()
+    vals = []
+    for _ in range(E2E_RUNS):
+        d = make_handle()
+        d.sequence_ptr(W, hframes.data_ptr(), glsu.F32, hout.data_ptr())  # warms the copy streams
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        d.sequence_ptr(K, hframes[W].data_ptr(), glsu.F32, hout.data_ptr())
+        el = reduce_max(time.perf_counter() - t0, world)
+        d.close()
+        vals.append(world * K / el)
+    return float(np.median(vals)), vals
 
 
 def surrogate_accuracy(glsu, torch, dfr, phi0, wp, params, dil, nframes):
@@ -402,6 +449,162 @@ def surrogate_accuracy(glsu, torch, dfr, phi0, wp, params, dil, nframes):
             "rmse_per_frame": rm, "rmse": float(np.sqrt(np.mean(np.square(rm)))), "max_abs": max(mx),
             "rmse_without_network": float(np.sqrt(np.mean(np.square(rid)))), "frames": nframes,
             "tiles_probed": probed, "tiles_recomputed": flagged}
+
+
+def aligned_phase_error(est, truth):
+    """Phase error of est against truth up to the global constant (and sign)
+    that AIA cannot determine: (rmse, max, sign, offset)."""
+    best = None
+    for sgn in (1.0, -1.0):
+        d = np.angle(np.exp(1j * (sgn * np.asarray(est, np.float64) - truth)))
+        c = float(np.angle(np.mean(np.exp(1j * d))))
+        e = np.angle(np.exp(1j * (d - c)))
+        r = (float(np.sqrt(np.mean(e * e))), float(np.abs(e).max()), sgn, c)
+        if best is None or r[0] < best[0]:
+            best = r
+    return best
+
+
+def fp64_frame_error(glsu, pref, dev_frame, radius, wp, pc):
+    """Phase error (wrapped, all pixels) of a frame's phi_curr against the
+    FP64 G-LS3U frame from the same reference phase: (rmse, max)."""
+    d64 = glsu.DPRA(np.asarray(pref, np.float64), 1, radius, "f64", wp)
+    d64.per_frame_device(dev_frame.data_ptr(), glsu.F32)
+    pc64 = d64.get(glsu.PHI_CURR)
+    d64.close()
+    e = np.angle(np.exp(1j * (np.asarray(pc, np.float64) - pc64)))
+    return float(np.sqrt(np.mean(e * e))), float(np.abs(e).max())
+
+
+def precision_form(glsu, torch, seed, size=SIZE, nframes=200, every=20):
+    """The precision form (AIA initial phase, then the FP32 G-LS3U sequence):
+    AIA on 5 frames with shifts U(0, 2 pi) (at most 30 iterations or a shift
+    change below 1e-4) against the generator's phase and shifts, with the
+    reference's convergence measure and with the relative one of its second
+    AIA variant; then `nframes` frames of the generator from AIA's phase,
+    DPRA 7x7 + WFF2 in FP32, graph mode, with every `every`-th frame compared
+    with the FP64 frame from the same reference phase."""
+    from glsu import synth
+    out = {"shifts": None}
+    fr, phi_true, shifts = synth.aia_frames(size, size, 5, seed=seed)
+    out["shifts"] = [float(v) for v in shifts]
+    for rel in (False, True):
+        a = glsu.AIA(5, size, size)
+        a.set_convergence(rel)
+        a.run(list(fr), None, max_iter=30, max_err=1e-4, seed=seed)  # warm
+        phi, deltas, ms, iters, err = a.run(list(fr), None, max_iter=30, max_err=1e-4, seed=seed)
+        a.close()
+        rm, mx, sgn, c = aligned_phase_error(phi, phi_true)
+        ds = np.angle(np.exp(1j * (sgn * np.asarray(deltas, np.float64) - (shifts - shifts[0]))))
+        ds = np.angle(np.exp(1j * (ds - ds[0])))
+        out["aia_relative_measure" if rel else "aia"] = {
+            "ms": ms, "iterations": int(iters), "last_change": float(err), "phase_rmse_vs_truth": rm,
+            "phase_max_vs_truth": mx, "shift_max_err_vs_truth": float(np.abs(ds).max()),
+            "measure": ("change of the shifts relative to the first (AIA_CUDAF_YC2, AIA/aia_cudaf_v2.cu:665-677)"
+                        if rel else "max |delta - delta_old| (AIA_CUDAF, AIA/aia_cpu.cpp:249-263)")}
+        if not rel:
+            phi_aia = np.asarray(phi, np.float64)
+    out["note"] = ("the phase and frame steps leave a common rotation of the shifts free; the iterates drift along "
+                   "it by a constant step per iteration, so the first measure stays at that step and the run "
+                   "stops at the cap while the normalised shifts have settled; the phase error against the "
+                   "generator's phase (up to the global constant AIA cannot fix) is set by the 5 shifts' spread "
+                   "and the noise")
+    wp = glsu.WffParams(*WFF)
+    seq = synth.DeviceSequence(size, size, seed=seed)
+    d = glsu.DPRA(phi_aia.astype(np.float32), 1, RADIUS, "f32", wp)
+    st = torch.cuda.Stream()
+    d.set_stream(st.cuda_stream)
+    d.set_graph(True)
+    buf = torch.empty((size, size), dtype=torch.float32, device="cuda")
+    dev_ms, errs = 0.0, []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for k in range(1, nframes + 1):
+        buf.copy_(seq.frame(k))
+        sample = k % every == 0
+        pref = d.get(glsu.PHI_REF) if sample else None
+        torch.cuda.synchronize()
+        e0.record(st)
+        d.per_frame_device(buf.data_ptr(), glsu.F32)
+        d.update_ref_phi()
+        e1.record(st)
+        torch.cuda.synchronize()
+        dev_ms += e0.elapsed_time(e1)
+        if sample:
+            errs.append((k,) + fp64_frame_error(glsu, pref, buf, RADIUS, wp, d.get(glsu.PHI_REF)))
+    d.close()
+    out["sequence"] = {
+        "frames": nframes, "device_ms_per_frame": dev_ms / nframes, "frames_per_s": nframes / (dev_ms * 1e-3),
+        "initial_phase": "AIA output", "fp64_samples": [{"frame": k, "rmse": r, "max": m} for k, r, m in errs],
+        "rmse_vs_fp64": float(np.sqrt(np.mean([r * r for _, r, _ in errs]))),
+        "max_abs_vs_fp64": max(m for _, _, m in errs), "bar_rad": 1e-3,
+        "note": "each sampled frame is compared with the FP64 frame (FP64 DPRA LS + FP64 WFF2) run from the same "
+                "reference phase; frames are made on the GPU from the seeded generator"}
+    return out
+
+
+CONFIG4 = dict(size=2048, radius=4, wff=(15.0, -1.5, 1.5, 0.1, 15.0, -1.5, 1.5, 0.1, 0.2), noise=0.05, n_gauss=8)
+
+
+def large_workload(glsu, torch, seed, nframes=12, warm=2, fp64_frames=(6, 12)):
+    """The large streaming workload (2048^2, 8 Gaussians, noise 0.05, DPRA
+    9x9, WFF2 sigma 15 with 31 x 31 frequencies on [-1.5, 1.5]), plain FP32
+    form in graph mode: device frames/s over `nframes` frames after `warm`,
+    the column sweep's share, HBM throughput figures, and the FP64 check on
+    sampled frames."""
+    from glsu import synth
+    c = CONFIG4
+    size, wp = c["size"], glsu.WffParams(*c["wff"])
+    seq = synth.DeviceSequence(size, size, seed=seed, noise=c["noise"], n_gauss=c["n_gauss"])
+    d = glsu.DPRA(seq.phi0.astype(np.float32), 1, c["radius"], "f32", wp)
+    tu = d.tuning()
+    st = torch.cuda.Stream()
+    d.set_stream(st.cuda_stream)
+    d.set_graph(True)
+    buf = torch.empty((size, size), dtype=torch.float32, device="cuda")
+    ms, errs = [], []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for k in range(1, warm + nframes + 1):
+        buf.copy_(seq.frame(k))
+        sample = k - warm in fp64_frames
+        pref = d.get(glsu.PHI_REF) if sample else None
+        torch.cuda.synchronize()
+        e0.record(st)
+        d.per_frame_device(buf.data_ptr(), glsu.F32)
+        d.update_ref_phi()
+        e1.record(st)
+        torch.cuda.synchronize()
+        if k > warm:
+            ms.append(e0.elapsed_time(e1))
+        if sample:
+            errs.append((k,) + fp64_frame_error(glsu, pref, buf, c["radius"], wp, d.get(glsu.PHI_REF)))
+    d.set_graph(False)
+    d.stage_timing(True)
+    buf.copy_(seq.frame(warm + nframes + 1))
+    d.per_frame_device(buf.data_ptr(), glsu.F32)
+    st = d.stage_times()
+    d.close()
+    s = int(np.floor(3 * c["wff"][0] + 0.5))
+    nfx = glsu.wff_count(c["wff"][1], c["wff"][2], c["wff"][3], glsu.F32)
+    P = fft_padded(size + 2 * s) ** 2
+    fft_bytes = (64 * nfx * nfx + 32) * P
+    pitch = (size + 127) // 128 * 128
+    col_bytes = 2 * nfx * size * pitch * 8
+    mean_ms = float(np.mean(ms))
+    return {
+        "workload": "2048x2048 FP32, 8 Gaussians, noise 0.05, DPRA 9x9, WFF2 sigma 15, xi in [-1.5, 1.5] step "
+                    "0.1 (%dx%d frequencies), thr 0.2, plain form, graph mode" % (nfx, nfx),
+        "frames_per_s": 1e3 / mean_ms, "ms_per_frame": mean_ms, "frames_timed": nframes,
+        "stages_ms": {"dpra_ls": st[0], "wff_rows": st[1], "wff_column_sweep": st[2], "wff_final_update": st[3]},
+        "column_sweep": tu,
+        "hbm": {"compulsory_gb_per_s": col_bytes / (st[2] * 1e-3) / 1e9,
+                "fft_model_bytes_per_frame": fft_bytes, "fft_model_gb_per_s": fft_bytes / (mean_ms * 1e-3) / 1e9,
+                "what": "compulsory: the column sweep's R-plane read and C-plane write over its time; fft_model: "
+                        "frame throughput x the FFT formulation's algorithmic bytes per frame ((64 n_freq + 32) P, "
+                        "P = %d^2)" % int(P ** 0.5)},
+        "fp64_samples": [{"frame": k, "rmse": r, "max": m} for k, r, m in errs],
+        "rmse_vs_fp64": float(np.sqrt(np.mean([r * r for _, r, _ in errs]))) if errs else None,
+        "max_abs_vs_fp64": max(m for _, _, m in errs) if errs else None,
+    }
 
 
 BATCH_SIZES = ((256, 256), (384, 512), (1024, 1024), (1536, 2048))  # (H, W) of the batched form's mix
@@ -516,11 +719,20 @@ def wfr_measure(glsu, torch, phi0, size, seed):
             "fp32_frac_of_peak_at_2070mhz": 2 * fma / (ms * 1e-3) / (152 * 128 * 2 * 2070e6)}
 
 
+def fft_sweep_flops(size, nfx, nfy, L, pitch):
+    """Algorithmic FP32 flops of one FFT column sweep: per column and
+    x-frequency, 2 nfy + 2 transforms of length L at 5 L log2 L each, plus
+    per wy the two window products (6 flops a point each), the threshold and
+    the accumulation (4)."""
+    return float(pitch) * nfx * ((2 * nfy + 2) * 5.0 * L * np.log2(L) + nfy * 16.0 * L)
+
+
 def run_ours(args, rank, world, local):
     import torch
     import glsu
     from glsu import synth
     from glsu import train_surrogate as TS
+    from glsu import surrogate_eval as SE
     if not torch.cuda.is_available():
         raise RuntimeError("no CUDA device: the GB300 path has no CPU fallback")
     torch.cuda.set_device(local)
@@ -532,18 +744,15 @@ def run_ours(args, rank, world, local):
     # wrapped index would feed frame 0 after frame k, a k-frame phase jump)
     nfr = args.warmup + args.steps + STAGE_FRAMES + 1
     frames, phi0, _ = synth.sequence(size, size, nfr, seed=seed)
+    extras = not args.frames_only and rank == 0  # the legs beside the headline run on rank 0
 
-    # ---- AIA initial phase (5 frames, shifts U(0, 2pi), <= 30 iterations or 1e-4)
-    aia_ms, aia_iters, aia_err, wfr, batched = None, None, None, None, None
-    if not args.frames_only:
-        aframes, _, _ = synth.aia_frames(size, size, 5, seed=seed)
-        aia = glsu.AIA(5, size, size)
-        aia.run(list(aframes), None, max_iter=30, max_err=1e-4, seed=seed)  # warm
-        _, _, aia_ms, aia_iters, aia_err = aia.run(list(aframes), None, max_iter=30, max_err=1e-4, seed=seed)
-        aia.close()
+    wfr = batched = prec1 = large = None
+    if extras:
         wfr = wfr_measure(glsu, torch, phi0, size, seed)
         batched = {"uneven_sizes": batched_measure(glsu, torch, seed),
                    "small_frames": batched_measure(glsu, torch, seed, sizes=((256, 256),), per_size=16, nframes=8)}
+        prec1 = precision_form(glsu, torch, seed, size)
+        large = large_workload(glsu, torch, seed)
 
     stream = torch.cuda.Stream()
     dfr = torch.from_numpy(frames).cuda()
@@ -557,14 +766,21 @@ def run_ours(args, rank, world, local):
     p_tuning = dp.tuning()
     dp.close()
 
+    hseq = hphi0 = None
+    if not args.frames_only:
+        hseq, hphi0 = host_sequence(torch, size, args.warmup + E2E_FRAMES, seed)
+
     def plain_handle():
-        h = glsu.DPRA(phi0.astype(np.float32), 1, RADIUS, "f32", wp)
+        h = glsu.DPRA(hphi0.astype(np.float32), 1, RADIUS, "f32", wp)
         h.set_stream(stream.cuda_stream)
         h.set_graph(True)
         return h
 
-    p_e2e = None if args.frames_only else e2e_sequence(glsu, torch, plain_handle, frames, args, stream, flush, world)
-    p_acc = None if args.frames_only else plain_accuracy(glsu, torch, dfr, phi0, wp, 3)
+    p_e2e = p_e2e_runs = p_acc = copies = None
+    if not args.frames_only:
+        p_e2e, p_e2e_runs = e2e_sequence(glsu, torch, plain_handle, hseq, args, stream, flush, world)
+        p_acc = plain_accuracy(glsu, torch, dfr, phi0, wp, 3)
+        copies = copy_times(torch, size)
 
     # ---- surrogate form: DPRA LS -> network -> probes -> per-tile fallback -> update
     sur = None
@@ -587,12 +803,23 @@ def run_ours(args, rank, world, local):
             h.set_surrogate(params, dil, SUR_TILE, SUR_PATCH, SUR_TOL)
             return h
 
-        s_e2e, acc = None, {"rmse": None, "rmse_vs_fp64": None}
+        s_e2e = s_e2e_runs = deploy = None
+        acc = {"rmse": None, "rmse_vs_fp64": None}
         if not args.frames_only:
-            s_e2e = e2e_sequence(glsu, torch, sur_handle, frames, args, stream, flush, world)
+            s_e2e, s_e2e_runs = e2e_sequence(glsu, torch, sur_handle, hseq, args, stream, flush, world)
             acc = surrogate_accuracy(glsu, torch, dfr, phi0, wp, params, dil, min(6, nfr - 1))
+        if extras:
+            dep = SE.deployment(glsu, params, dil, range(DEPLOY_SEED0, DEPLOY_SEED0 + DEPLOY_SEEDS),
+                                DEPLOY_FRAMES, DEPLOY_EVERY, size, wff=WFF, radius=RADIUS, tile=SUR_TILE,
+                                patch=SUR_PATCH, tol=SUR_TOL)
+            deploy = {k: v for k, v in dep.items() if k != "per_frame"}
+            deploy["rmse_per_sampled_frame"] = [round(x["rmse"], 5) for x in dep["per_frame"]]
+            deploy["workload"] = ("%d held-out seeds (%d..) of the 1024^2 generator, %d free-running frames each in "
+                                  "the surrogate form (graph mode); every %d-th frame against the FP64 frame from "
+                                  "the same reference phase" % (DEPLOY_SEEDS, DEPLOY_SEED0, DEPLOY_FRAMES,
+                                                                 DEPLOY_EVERY))
         sur = {"frames_per_s": s_val, "ms_per_step": s_ms / args.steps, "speedup_vs_plain": s_val / p_val,
-               "e2e_frames_per_s": s_e2e,
+               "e2e_frames_per_s": s_e2e, "e2e_runs": s_e2e_runs,
                "stages_ms": {"dpra_ls": s_st[0], "network": s_st[1], "wff2_probe_and_residuals": s_st[2],
                              "fallback_and_update": s_st[3]},
                "network_ms": {"layer0": s_st[4], "tensor_core_layers_1_6": s_st[5], "layer7": s_st[6]},
@@ -603,8 +830,10 @@ def run_ours(args, rank, world, local):
                "probe": {"tile": SUR_TILE, "patch": SUR_PATCH, "tol_rad": SUR_TOL},
                "dilations": dil, "params": int(params.size),
                "accuracy": acc,
+               "deployment": deploy,
                "rmse_target_rad": 0.02,
-               "meets_rmse_target": None if acc["rmse_vs_fp64"] is None else acc["rmse_vs_fp64"] <= 0.02}
+               "meets_rmse_target": (None if deploy is None else
+                                     bool(deploy["rmse_median"] <= 0.02 and deploy["rmse_p90"] <= 0.02))}
 
     # ---- rooflines
     peaks = {}
@@ -614,52 +843,57 @@ def run_ours(args, rank, world, local):
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
-    peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
+    peak_kind = "measured (MEASURED_PEAKS.json)" if "hbm_gbs" in peaks else "fallback"
     pitch = (size + 127) // 128 * 128
     col_bytes = 2 * NFX * size * pitch * 8  # read R_i planes + write C_i planes (complex64)
-    sx = int(np.floor(3 * WFF[0] + 0.5))
-    col_fma = NFX * NFY * N * 2 * (2 * sx + 1) * 2
     sm_mhz = p_clk.get("sm_mhz") or 1900.0
     fp32_peak_tflops = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    plain_roof = {"kernel": "wff_cols_kernel (WFF2 column sweep)", "bound": "hbm",
-                  "achieved": col_bytes / (p_st[2] * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                  "frac": col_bytes / (p_st[2] * 1e-3) / 1e9 / hbm_peak, "traffic": None,
-                  "peak_source": peak_kind, "algorithmic_bytes_per_launch": col_bytes,
-                  "fp32_pipe": {"achieved_tflops": 2 * col_fma / (p_st[2] * 1e-3) / 1e12,
-                                "peak_tflops_at_clock": fp32_peak_tflops,
-                                "frac": 2 * col_fma / (p_st[2] * 1e-3) / 1e12 / fp32_peak_tflops}}
+    if p_tuning["method"] == glsu.METHOD_FFT:
+        col_flops = fft_sweep_flops(size, NFX, NFY, p_tuning["fft_length"], pitch)
+        col_kernel, flop_rule = "wff_colfft_kernel (WFF2 FFT column sweep, L = %d)" % p_tuning["fft_length"], \
+            "5 L log2 L per transform, 2 nfy + 2 transforms per column and wx, + 16 L per wy"
+    else:
+        sx = int(np.floor(3 * WFF[0] + 0.5))
+        col_flops = float(NFX * NFY * N * 2 * (2 * sx + 1) * 2)
+        col_kernel, flop_rule = "wff_cols_kernel (WFF2 direct column sweep)", "2 column filters x (2s+1) taps x 2"
+    col_s = p_st[2] * 1e-3
     fb, P = fft_model_bytes(size)
-    plain_roof["fft_model"] = {
-        "what": "frame throughput x the FFT formulation's algorithmic bytes per frame ((64 n_freq + 32) P, "
-                "P = padded plane %d^2); the direct formulation here moves only the compulsory bytes" % int(P ** 0.5),
-        "bytes_per_frame": fb, "achieved": fb * p_val / world / 1e9, "peak": hbm_peak, "unit": "GB/s",
-        "frac": fb * p_val / world / 1e9 / hbm_peak}
+    plain_roof = {"kernel": col_kernel, "bound": "fp32",
+                  "achieved": col_flops / col_s / 1e12, "peak": fp32_peak_tflops, "unit": "TFLOP/s",
+                  "frac": col_flops / col_s / 1e12 / fp32_peak_tflops,
+                  "peak_source": "152 SMs x 128 FP32 lanes x 2 x sampled SM clock (%.0f MHz)" % sm_mhz,
+                  "algorithmic_flops_per_launch": col_flops, "flop_rule": flop_rule, "launch_ms": p_st[2],
+                  "hbm_compulsory": {"bytes_per_launch": col_bytes, "achieved": col_bytes / col_s / 1e9,
+                                     "peak": hbm_peak, "unit": "GB/s", "frac": col_bytes / col_s / 1e9 / hbm_peak},
+                  "fft_model": {
+                      "what": "side figure: frame throughput x the reference FFT formulation's algorithmic bytes "
+                              "per frame ((64 n_freq + 32) P, P = padded plane %d^2)" % int(P ** 0.5),
+                      "bytes_per_frame": fb, "achieved": fb * p_val / world / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                      "frac": fb * p_val / world / 1e9 / hbm_peak}}
     roof = plain_roof
     if sur and "stages_ms" in sur:
-        net_bytes = SUR_BYTES_PER_PX * N
         net_ms = sur["stages_ms"]["network"]
-        net_roof = {"kernel": "surrogate network (sur_l0 + 6 x sur_conv_tc tcgen05 + sur_l7)", "bound": "hbm",
-                    "achieved": net_bytes / (net_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                    "frac": net_bytes / (net_ms * 1e-3) / 1e9 / hbm_peak, "traffic": None,
-                    "peak_source": peak_kind, "algorithmic_bytes_per_launch": net_bytes,
-                    "tensor": {"achieved_tflops": SUR_FLOPS_PER_PX * N / (net_ms * 1e-3) / 1e12,
-                               "peak_tflops": bf16_peak,
-                               "frac": SUR_FLOPS_PER_PX * N / (net_ms * 1e-3) / 1e12 / bf16_peak}}
         # the tensor-core layer: six launches per frame, timed together
         conv_ms = sur["network_ms"]["tensor_core_layers_1_6"] / 6
         conv_bytes, conv_flops = SUR_CONV_BYTES_PER_PX * N, SUR_CONV_FLOPS_PER_PX * N
-        conv_roof = {"kernel": "sur_conv_tc_kernel (tcgen05 32->32 dilated 3x3 layer, per launch)", "bound": "hbm",
-                     "achieved": conv_bytes / (conv_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": conv_bytes / (conv_ms * 1e-3) / 1e9 / hbm_peak,
-                     "traffic": SUR_CONV_TRAFFIC_1024 if size == 1024 else None,
+        traffic = SUR_CONV_TRAFFIC_1024 if size == 1024 else None
+        conv_roof = {"kernel": "sur_conv_tc_kernel (tcgen05 32->32 dilated 3x3 layer, per launch)", "bound": "tensor",
+                     "achieved": conv_flops / (conv_ms * 1e-3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
+                     "frac": conv_flops / (conv_ms * 1e-3) / 1e12 / bf16_peak,
+                     "traffic": traffic,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at "
                                        "1024x1024 (profiles/sur_conv_tc_kernel_1024.md)",
-                     "peak_source": peak_kind, "algorithmic_bytes_per_launch": conv_bytes,
-                     "launch_ms": conv_ms,
-                     "tensor": {"achieved_tflops": conv_flops / (conv_ms * 1e-3) / 1e12,
-                                "peak_tflops": bf16_peak,
-                                "frac": conv_flops / (conv_ms * 1e-3) / 1e12 / bf16_peak}}
-        sur["roofline_network"] = net_roof
+                     "peak_source": peak_kind + ", dense bf16 burst",
+                     "algorithmic_flops_per_launch": conv_flops, "launch_ms": conv_ms,
+                     "hbm": {"algorithmic_bytes_per_launch": conv_bytes,
+                             "achieved": conv_bytes / (conv_ms * 1e-3) / 1e9,
+                             "dram_achieved": None if traffic is None else traffic / (conv_ms * 1e-3) / 1e9,
+                             "peak": hbm_peak, "unit": "GB/s",
+                             "dram_frac": None if traffic is None else traffic / (conv_ms * 1e-3) / 1e9 / hbm_peak}}
+        net_flops = SUR_FLOPS_PER_PX * N
+        sur["roofline_network"] = {"kernels": "sur_l0 + 6 x sur_conv_tc (tcgen05) + sur_l7", "bound": "tensor",
+                                   "achieved": net_flops / (net_ms * 1e-3) / 1e12, "peak": bf16_peak,
+                                   "unit": "TFLOP/s", "frac": net_flops / (net_ms * 1e-3) / 1e12 / bf16_peak}
         sur["roofline_tensor_core_layer"] = conv_roof
         sur["roofline_plain_column_sweep"] = plain_roof
         kern = {"sur_conv_tc_kernel x6": sur["network_ms"]["tensor_core_layers_1_6"],
@@ -670,6 +904,7 @@ def run_ours(args, rank, world, local):
         roof = conv_roof
 
     headline = sur if (sur and "frames_per_s" in sur) else None
+    e2e_val = headline["e2e_frames_per_s"] if headline else p_e2e
     out = {
         "metric": METRIC, "value": headline["frames_per_s"] if headline else p_val, "unit": "frames/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -678,31 +913,36 @@ def run_ours(args, rank, world, local):
         "form": "surrogate" if headline else "plain",
         "config": workload_config(size),
         "clocks": s_clk if headline else p_clk,
-        "e2e": {"value": headline["e2e_frames_per_s"] if headline else p_e2e, "unit": "frames/s",
-                "h2d_bytes_per_step": 4 * N, "d2h_bytes_per_step": 4 * N},
+        "e2e": {"value": e2e_val, "unit": "frames/s", "h2d_bytes_per_step": 4 * N, "d2h_bytes_per_step": 4 * N,
+                "frames_per_run": E2E_FRAMES, "runs": headline["e2e_runs"] if headline else p_e2e_runs,
+                "statistic": "median of the runs",
+                "h2d_ms_per_frame": copies[0] if copies else None, "d2h_ms_per_frame": copies[1] if copies else None,
+                "overhead_ms_per_frame": None if not e2e_val else 1e3 / e2e_val -
+                (headline["ms_per_step"] if headline else p_ms / args.steps)},
         "gpu_launches": (SUR_LAUNCHES if headline else PLAIN_LAUNCHES) * args.steps,
         "roofline": roof,
         "plain": {"frames_per_s": p_val, "ms_per_step": p_ms / args.steps, "e2e_frames_per_s": p_e2e,
+                  "e2e_runs": p_e2e_runs,
                   "stages_ms": {"dpra_ls": p_st[0], "wff_rows": p_st[1], "wff_column_sweep": p_st[2],
                                 "wff_final_update": p_st[3]},
                   "roofline": plain_roof, "clocks": p_clk, "gpu_launches_per_step": PLAIN_LAUNCHES,
                   "column_sweep_autotune": p_tuning, "accuracy": p_acc},
         "surrogate": sur,
+        "precision_form": prec1,
+        "large_workload": large,
         "wfr": wfr,
         "batched_form": batched,
-        "aia": {"frames": 5, "ms": aia_ms, "iterations": aia_iters, "err": aia_err,
-                "ms_per_frame_over_200": None if aia_ms is None else aia_ms / 200},
     }
     if rank == 0 and not args.no_cpu_baseline:
-        v32, secs, threads, rows = cpu_sample(size, args.cpu_rows, prec="f32")
-        v64, secs64, _, _ = cpu_sample(size, args.cpu_rows, prec="f64")
+        v32, secs, threads, rows = cpu_sample(size, prec="f32")
+        v64, secs64, _, _ = cpu_sample(size, prec="f64")
         out["cpu_baseline"] = {
             "value": max(v32, v64), "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": "one %dx%d frame: DPRA LS + update in full, WFF2 over %d of 21 frequency rows (one row per "
-                      "OpenMP thread, %d threads) extrapolated by rounds of rows to the 441 frequencies (%.1f s + "
-                      "%.1f s of CPU work), with the restatements of the reference's CPU classes in FP32 "
-                      "(DPRA_CPUF/WFT2_cpuF) and FP64 (DPRA_CPU/WFT2_cpu); value is the faster of the two"
-                      % (size, size, rows, threads, secs, secs64),
+            "sample": "one whole %dx%d frame in each precision (%d threads; FP32 %.1f s, FP64 %.1f s): DPRA LS, "
+                      "WFF2 over all 441 frequencies (one frequency row per OpenMP thread at a time), update, "
+                      "with the restatements of the reference's CPU classes in FP32 (DPRA_CPUF/WFT2_cpuF) and "
+                      "FP64 (DPRA_CPU/WFT2_cpu); value is the faster of the two"
+                      % (size, size, threads, secs, secs64),
             "fp32_value": v32, "fp64_value": v64}
     return out if rank == 0 else None
 

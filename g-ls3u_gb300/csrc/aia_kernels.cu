@@ -124,8 +124,14 @@ __global__ void __launch_bounds__(kAiaThreads)
 
 // One block: reduce the partials in a fixed order, solve A2 y = b for every
 // frame (Cholesky, as LAPACKE_dposv at AIA/aia_cpu.cpp:235), update deltas.
+// The convergence measure is max_i |delta_i - old_i| (AIA_CUDAF,
+// AIA/aia_cpu.cpp:249-263), or with rel != 0 the change of the shifts
+// relative to the first, max_i |(delta_i - delta_0) - (old_i - old_0)|
+// (AIA_CUDAF_YC2, AIA/aia_cudaf_v2.cu:665-677), which does not see the
+// common rotation the two steps leave free.
 __global__ void aia_solve_kernel(const double *__restrict__ part, int nblocks, int M, int N,
-                                 double *__restrict__ state, int *__restrict__ done, int max_iter, double max_err)
+                                 double *__restrict__ state, int *__restrict__ done, int max_iter, double max_err,
+                                 int rel)
 {
     if (*done) return;
     __shared__ double tot[5 + 3 * kAiaMaxM];
@@ -154,7 +160,8 @@ __global__ void aia_solve_kernel(const double *__restrict__ part, int nblocks, i
             U[j][i] = t / U[j][j];
         }
     }
-    double err = 0;
+    double err = 0, new0 = 0;
+    const double old0 = state[0];
     for (int m = 0; m < M; m++) {
         double b[3] = {tot[5 + 3 * m], tot[6 + 3 * m], tot[7 + 3 * m]};
         double y[3];
@@ -169,7 +176,8 @@ __global__ void aia_solve_kernel(const double *__restrict__ part, int nblocks, i
             b[i] = t / U[i][i];
         }
         const double dn = atan2(-b[2], b[1]);
-        const double e = fabs(dn - state[m]);
+        if (m == 0) new0 = dn;
+        const double e = rel ? fabs((dn - new0) - (state[m] - old0)) : fabs(dn - state[m]);
         err = e > err ? e : err;
         state[M + m] = state[m];
         state[m] = dn;
@@ -218,7 +226,8 @@ int aia_launch_pass(const AiaDev &a, int img_type, const void *d_frames, int fin
 
 int aia_launch_solve(const AiaDev &a, int max_iter, double max_err, cudaStream_t s)
 {
-    aia_solve_kernel<<<1, 128, 0, s>>>(a.d_part, a.nblocks, a.M, a.N, a.d_state, a.d_done, max_iter, max_err);
+    aia_solve_kernel<<<1, 128, 0, s>>>(a.d_part, a.nblocks, a.M, a.N, a.d_state, a.d_done, max_iter, max_err,
+                                       a.err_mode == GLSU_AIA_ERR_RELATIVE ? 1 : 0);
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
 }

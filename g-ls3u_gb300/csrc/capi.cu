@@ -1258,6 +1258,15 @@ static int aia_core(glsu_aia *h, const void *d_frames, int img_type, float *d_ph
     return GLSU_OK;
 }
 
+extern "C" int glsu_aia_set_convergence(glsu_aia *h, int mode)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    if (mode != GLSU_AIA_ERR_ABS && mode != GLSU_AIA_ERR_RELATIVE)
+        return fail(GLSU_ERR_INVALID, "unknown AIA convergence measure");
+    h->dev.err_mode = mode;
+    return GLSU_OK;
+}
+
 extern "C" int glsu_aia_run(glsu_aia *h, const void *const *h_frames, int img_type, float *h_phi, float *h_deltas,
                             int n_deltas_in, double *time_ms, int *iters, float *err, int max_iter, float max_err,
                             uint64_t seed)

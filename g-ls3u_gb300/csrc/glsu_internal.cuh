@@ -277,6 +277,7 @@ struct AiaDev {
     double *d_part = nullptr;   // nblocks x (5 + 3M) partial sums
     double *d_state = nullptr;  // deltas, old deltas, err, iteration, flags
     int *d_done = nullptr;
+    int err_mode = GLSU_AIA_ERR_ABS;  // convergence measure (glsu_aia_set_convergence)
 };
 int aia_launch_pass(const AiaDev &a, int img_type, const void *d_frames, int final_pass, float *d_phi,
                     cudaStream_t s);

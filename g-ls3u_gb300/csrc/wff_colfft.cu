@@ -1,23 +1,7 @@
-// wff_colfft.cu -- WFF2 column sweep with shared-memory FFTs (FP32 form).
-//
-// Same mathematics as wff_cols_kernel, evaluated in the frequency domain of
-// each column.  For one x-frequency plane R_i and one column, with
-// h_k(m) = gy(m) e^{j wy_k m} (m in [-s, s]) the truncated, modulated
-// window and L >= H + 2s (so the circular convolutions below are the
-// linear, zero-boundary ones of the reference):
-//     U_k  = IFFT( FFT(R) . H_k )            (|U_k| / (L N) is |sf|)
-//     T_k  = U_k . [ |U_k| >= L N thr ],  rows >= H set to 0
-//     Ch  += FFT(T_k) . H_k                  (sum over wy_k in the spectrum)
-//     C    = IFFT(Ch) / (L^2 N)              (the C_i plane of the direct kernel)
-// H_k = FFT(h_k) is tabulated exactly (host, FP64), so the window is the
-// reference CPU path's truncated one.  Per column and plane: 1 + 2 nfy + 1
-// transforms of length L, all in shared memory / registers; FFT(R) and the
-// spectrum accumulator stay in registers for all nfy frequencies.
-//
-// Transforms: Stockham auto-sort, radix 8/4/2/5/3 stages, ping-pong between
-// two shared buffers laid out [L][NC] (NC columns per CTA, column index
-// fastest) with one float2 of padding per 16 elements against bank
-// conflicts on the strided writes of the early stages.
+// wff_colfft.cu -- host side of the WFF2 FFT column sweep (FP32 form): the
+// transform length and CTA width of a plan, its tables, the launch, and the
+// column-sweep autotuner.  The kernels are in wff_colfft.cuh, compiled per
+// transform length in wff_colfft_k{1,2,3}.cu.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -26,355 +10,73 @@
 #include <mutex>
 #include <vector>
 
-#include "glsu_internal.cuh"
+#include "wff_colfft_plans.cuh"
 
 namespace glsu {
 
-constexpr int kFftThreads = 512;
+namespace colfft {
 
-// Throughputs of the column-sweep cost model (WffPlan::model_ms), measured
-// on GB300: direct kernel in tap-units per second per instantiated
-// half-size, FFT sweep in (length x stages) units per second.
-constexpr double kModelDirectRate30 = 1.1e13;
-constexpr double kModelDirectRate45 = 5.5e12;
-constexpr double kModelDirectRate60 = 3.95e12;
-constexpr double kModelFftRate = 6.0e11;
-
-struct ColFftPlan {
-    int L;
-    int nst;
-    int radix[12];
-};
-
-__device__ __forceinline__ int pidx(int e) { return e + (e >> 4); }
-
-__device__ __forceinline__ float2 cmulf(float2 a, float2 b)
+bool len_info(int L, LenInfo *out)
 {
-    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-
-// In-register DFTs; INV selects the sign of the exponent (+ for the inverse).
-template <bool INV> __device__ __forceinline__ float2 mul_mi(float2 a)
-{
-    // forward: multiply by -i ; inverse: by +i
-    return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
-}
-
-template <bool INV> __device__ __forceinline__ void dft2(float2 *v)
-{
-    const float2 a = v[0], b = v[1];
-    v[0] = make_float2(a.x + b.x, a.y + b.y);
-    v[1] = make_float2(a.x - b.x, a.y - b.y);
-}
-
-template <bool INV> __device__ __forceinline__ void dft4(float2 *v)
-{
-    const float2 a0 = make_float2(v[0].x + v[2].x, v[0].y + v[2].y);
-    const float2 a1 = make_float2(v[0].x - v[2].x, v[0].y - v[2].y);
-    const float2 a2 = make_float2(v[1].x + v[3].x, v[1].y + v[3].y);
-    const float2 a3 = mul_mi<INV>(make_float2(v[1].x - v[3].x, v[1].y - v[3].y));
-    v[0] = make_float2(a0.x + a2.x, a0.y + a2.y);
-    v[2] = make_float2(a0.x - a2.x, a0.y - a2.y);
-    v[1] = make_float2(a1.x + a3.x, a1.y + a3.y);
-    v[3] = make_float2(a1.x - a3.x, a1.y - a3.y);
-}
-
-template <bool INV> __device__ __forceinline__ void dft8(float2 *v)
-{
-    // X[2q] = DFT4(v_r + v_{r+4}), X[2q+1] = DFT4((v_r - v_{r+4}) w8^r)
-    const float h = 0.70710678118654752f;
-    float2 b[4], c[4];
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        b[r] = make_float2(v[r].x + v[r + 4].x, v[r].y + v[r + 4].y);
-        c[r] = make_float2(v[r].x - v[r + 4].x, v[r].y - v[r + 4].y);
+#define GLSU_LEN(LEN, PLAN, NC0)                                                    \
+    case LEN:                                                                       \
+        *out = LenInfo{LEN, PLAN::T, PLAN::NP, NC0, smem_per_column<PLAN>()};       \
+        return true;
+    switch (L) {
+        GLSU_LEN(256, P256, 4)
+        GLSU_LEN(384, P384, 8)
+        GLSU_LEN(512, P512, 4)
+        GLSU_LEN(640, P640, 8)
+        GLSU_LEN(768, P768, 4)
+        GLSU_LEN(1024, P1024, 4)
+        GLSU_LEN(1280, P1280, 4)
+        GLSU_LEN(1536, P1536, 2)
+        GLSU_LEN(2048, P2048, 2)
+        GLSU_LEN(2560, P2560, 2)
+        GLSU_LEN(3072, P3072, 1)
+        GLSU_LEN(4096, P4096, 1)
+    default: return false;
     }
-    // w8 = e^{-+ i pi/4}
-    c[1] = INV ? make_float2(h * (c[1].x - c[1].y), h * (c[1].x + c[1].y))
-               : make_float2(h * (c[1].x + c[1].y), h * (c[1].y - c[1].x));
-    c[2] = mul_mi<INV>(c[2]);
-    c[3] = INV ? make_float2(-h * (c[3].x + c[3].y), h * (c[3].x - c[3].y))
-               : make_float2(h * (c[3].y - c[3].x), -h * (c[3].x + c[3].y));
-    dft4<INV>(b);
-    dft4<INV>(c);
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-        v[2 * q] = b[q];
-        v[2 * q + 1] = c[q];
-    }
+#undef GLSU_LEN
 }
 
-template <bool INV> __device__ __forceinline__ void dft3(float2 *v)
-{
-    const float s3 = 0.86602540378443865f;  // sin(2 pi / 3)
-    const float2 t1 = make_float2(v[1].x + v[2].x, v[1].y + v[2].y);
-    const float2 t2 = make_float2(v[1].x - v[2].x, v[1].y - v[2].y);
-    const float2 m = make_float2(v[0].x - 0.5f * t1.x, v[0].y - 0.5f * t1.y);
-    // forward: X1 = m - i s3 t2, X2 = m + i s3 t2
-    const float2 j = INV ? make_float2(-s3 * t2.y, s3 * t2.x) : make_float2(s3 * t2.y, -s3 * t2.x);
-    v[0] = make_float2(v[0].x + t1.x, v[0].y + t1.y);
-    v[1] = make_float2(m.x + j.x, m.y + j.y);
-    v[2] = make_float2(m.x - j.x, m.y - j.y);
-}
+}  // namespace colfft
 
-template <bool INV> __device__ __forceinline__ void dft5(float2 *v)
-{
-    // X_q = sum_r v_r e^{-+ 2 pi i q r / 5}, via the two symmetric pairs
-    const float c1 = 0.30901699437494742f, c2 = -0.80901699437494742f;  // cos(2pi/5), cos(4pi/5)
-    const float s1 = 0.95105651629515357f, s2 = 0.58778525229247313f;   // sin(2pi/5), sin(4pi/5)
-    const float2 a1 = make_float2(v[1].x + v[4].x, v[1].y + v[4].y);
-    const float2 b1 = make_float2(v[1].x - v[4].x, v[1].y - v[4].y);
-    const float2 a2 = make_float2(v[2].x + v[3].x, v[2].y + v[3].y);
-    const float2 b2 = make_float2(v[2].x - v[3].x, v[2].y - v[3].y);
-    const float2 m1 = make_float2(v[0].x + c1 * a1.x + c2 * a2.x, v[0].y + c1 * a1.y + c2 * a2.y);
-    const float2 m2 = make_float2(v[0].x + c2 * a1.x + c1 * a2.x, v[0].y + c2 * a1.y + c1 * a2.y);
-    // n1 = s1 b1 + s2 b2, n2 = s2 b1 - s1 b2; X1 = m1 -+ i n1, X4 = m1 +- i n1, X2 = m2 -+ i n2, X3 = m2 +- i n2
-    const float2 n1 = make_float2(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y);
-    const float2 n2 = make_float2(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y);
-    const float2 j1 = INV ? make_float2(-n1.y, n1.x) : make_float2(n1.y, -n1.x);
-    const float2 j2 = INV ? make_float2(-n2.y, n2.x) : make_float2(n2.y, -n2.x);
-    v[0] = make_float2(v[0].x + a1.x + a2.x, v[0].y + a1.y + a2.y);
-    v[1] = make_float2(m1.x + j1.x, m1.y + j1.y);
-    v[4] = make_float2(m1.x - j1.x, m1.y - j1.y);
-    v[2] = make_float2(m2.x + j2.x, m2.y + j2.y);
-    v[3] = make_float2(m2.x - j2.x, m2.y - j2.y);
-}
-
-template <int R, bool INV> __device__ __forceinline__ void dft(float2 *v)
-{
-    if (R == 2) dft2<INV>(v);
-    else if (R == 4) dft4<INV>(v);
-    else if (R == 8) dft8<INV>(v);
-    else if (R == 3) dft3<INV>(v);
-    else dft5<INV>(v);
-}
-
-// One Stockham stage over all NC columns: in -> out.
-template <int R, bool INV, int NC>
-__device__ __forceinline__ void fft_stage(const float2 *__restrict__ in, float2 *__restrict__ out, int L, int Ns,
-                                          const float2 *__restrict__ tw)
-{
-    const int LR = L / R;
-    const int tstep = L / (Ns * R);
-    const int nb = LR * NC;
-    for (int b = threadIdx.x; b < nb; b += kFftThreads) {
-        const int c = b % NC, j = b / NC;
-        const int k = j % Ns;
-        float2 v[R];
-#pragma unroll
-        for (int r = 0; r < R; r++) v[r] = in[pidx((j + r * LR) * NC + c)];
-        if (Ns > 1) {
-#pragma unroll
-            for (int r = 1; r < R; r++) {
-                float2 w = __ldg(tw + r * k * tstep);
-                if (INV) w.y = -w.y;
-                v[r] = cmulf(v[r], w);
-            }
-        }
-        dft<R, INV>(v);
-        const int idxD = (j / Ns) * Ns * R + k;
-#pragma unroll
-        for (int r = 0; r < R; r++) out[pidx((idxD + r * Ns) * NC + c)] = v[r];
-    }
-}
-
-// Full transform; returns the buffer holding the result (a or b).
-template <bool INV, int NC>
-__device__ float2 *fft_run(float2 *a, float2 *b, const ColFftPlan &P, const float2 *__restrict__ tw)
-{
-    int Ns = 1;
-    float2 *in = a, *out = b;
-    for (int s = 0; s < P.nst; s++) {
-        const int R = P.radix[s];
-        switch (R) {
-        case 8: fft_stage<8, INV, NC>(in, out, P.L, Ns, tw); break;
-        case 4: fft_stage<4, INV, NC>(in, out, P.L, Ns, tw); break;
-        case 2: fft_stage<2, INV, NC>(in, out, P.L, Ns, tw); break;
-        case 5: fft_stage<5, INV, NC>(in, out, P.L, Ns, tw); break;
-        default: fft_stage<3, INV, NC>(in, out, P.L, Ns, tw); break;
-        }
-        __syncthreads();
-        Ns *= R;
-        float2 *t = in;
-        in = out;
-        out = t;
-    }
-    return in;
-}
-
-// MAXE: elements (of the L x NC block) owned per thread, upper bound.
-// Registers are capped for two CTAs per SM: the stages are bound by shared
-// memory and block barriers, and a second CTA hides them (16-19% faster at
-// 1024^2 and 2048^2 despite 144-236 bytes of spills a thread).
-// A tile-masked run (the surrogate's per-tile fallback) passes the device
-// list of needed column groups (list, *list_count); each CTA then walks the
-// list with stride gridDim.x.  Without a list, CTA x is column group x.
-// Every column is computed the same way in both cases, so a masked run's
-// columns equal the full frame's bit for bit.
-template <int NC, int MAXE>
-__global__ void __launch_bounds__(kFftThreads, 2) wff_colfft_kernel(const float2 *__restrict__ R, float2 *__restrict__ Cout,
-                                                                 int H, int pitch, int nfy,
-                                                                 const float2 *__restrict__ khat,
-                                                                 const float2 *__restrict__ tw, ColFftPlan P,
-                                                                 const float *__restrict__ thr_ptr, float LN,
-                                                                 float out_scale, const int2 *__restrict__ list,
-                                                                 const int *__restrict__ list_count)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int L = P.L;
-    const int nel = L * NC;
-    float2 *bufA = reinterpret_cast<float2 *>(smem_raw);
-    float2 *bufB = bufA + pidx(nel) + 1;
-    const int tid = threadIdx.x;
-    const int i = blockIdx.y;
-    const size_t plane = (size_t)H * pitch;
-    const float2 *Ri = R + i * plane;
-    const int nitems = list ? *list_count : (int)gridDim.x;
-    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-    const int x0 = (list ? list[item].x : item) * NC;
-    __syncthreads();  // the previous item is done with the shared buffers
-
-    // load the NC columns (rows >= H are zero)
-    for (int e = tid; e < nel; e += kFftThreads) {
-        const int rho = e / NC, c = e - rho * NC;
-        float2 v = make_float2(0.f, 0.f);
-        if (rho < H) v = Ri[(size_t)rho * pitch + x0 + c];
-        bufA[pidx(e)] = v;
-    }
-    __syncthreads();
-    const float2 *res = fft_run<false, NC>(bufA, bufB, P, tw);
-    float2 rh[MAXE], ch[MAXE];
-#pragma unroll
-    for (int j = 0; j < MAXE; j++) {
-        const int e = tid + j * kFftThreads;
-        rh[j] = (e < nel) ? res[pidx(e)] : make_float2(0.f, 0.f);
-        ch[j] = make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    const float T = LN * (*thr_ptr);
-    const float T2 = T * T;
-    for (int k = 0; k < nfy; k++) {
-        const float2 *hk = khat + (size_t)k * L;
-#pragma unroll
-        for (int j = 0; j < MAXE; j++) {
-            const int e = tid + j * kFftThreads;
-            if (e < nel) bufA[pidx(e)] = cmulf(rh[j], __ldg(hk + e / NC));
-        }
-        __syncthreads();
-        float2 *u = fft_run<true, NC>(bufA, bufB, P, tw);
-        // hard threshold in the spatial domain (own elements only)
-#pragma unroll
-        for (int j = 0; j < MAXE; j++) {
-            const int e = tid + j * kFftThreads;
-            if (e < nel) {
-                const float2 v = u[pidx(e)];
-                const bool keep = (e / NC < H) && (v.x * v.x + v.y * v.y >= T2);
-                if (!keep) u[pidx(e)] = make_float2(0.f, 0.f);
-            }
-        }
-        __syncthreads();
-        float2 *other = (u == bufA) ? bufB : bufA;
-        const float2 *sp = fft_run<false, NC>(u, other, P, tw);
-#pragma unroll
-        for (int j = 0; j < MAXE; j++) {
-            const int e = tid + j * kFftThreads;
-            if (e < nel) {
-                const float2 a = sp[pidx(e)], h = __ldg(hk + e / NC);
-                ch[j].x += a.x * h.x - a.y * h.y;
-                ch[j].y += a.x * h.y + a.y * h.x;
-            }
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int j = 0; j < MAXE; j++) {
-        const int e = tid + j * kFftThreads;
-        if (e < nel) bufA[pidx(e)] = ch[j];
-    }
-    __syncthreads();
-    const float2 *cres = fft_run<true, NC>(bufA, bufB, P, tw);
-    float2 *Ci = Cout + i * plane;
-    for (int e = tid; e < nel; e += kFftThreads) {
-        const int rho = e / NC, c = e - rho * NC;
-        if (rho < H) {
-            const float2 v = cres[pidx(e)];
-            Ci[(size_t)rho * pitch + x0 + c] = make_float2(v.x * out_scale, v.y * out_scale);
-        }
-    }
-    }  // items
-}
-
-// ---------------------------------------------------------------------------
-// host side
-// ---------------------------------------------------------------------------
-// Stage radices of a length-n transform in one of three orders (the tuner's
-// radix-plan knob): 0 = 8, 4, 2 then 5, 3; 1 = 4, 2 then 5, 3 (no radix 8);
-// 2 = 5, 3 first, then 8, 4, 2.  Returns the stage count, or -1 when n has a
-// prime factor above 5.
-static int factor(int n, int *rad, int order = 0)
-{
-    int ns = 0;
-    auto take = [&](int r) {
-        while (n % r == 0 && ns < 12) {
-            rad[ns++] = r;
-            n /= r;
-        }
-    };
-    if (order == 2) {
-        take(5);
-        take(3);
-    }
-    if (order != 1) take(8);
-    take(4);
-    take(2);
-    take(5);
-    take(3);
-    return n == 1 ? ns : -1;
-}
-
-// Transform lengths L >= need (up to 2 need + 16) whose stages factor, in
-// increasing cost L x number of stages (ties: the shorter); at most n of them.
+// Compiled transform lengths >= need, ascending; at most n of them.
 static int length_candidates(int need, int *out, int n)
 {
-    std::vector<std::pair<long, int>> c;
-    for (int L = need; L <= 2 * need + 16; L++) {
-        int rad[12];
-        const int ns = factor(L, rad);
-        if (ns >= 1 && ns <= 12) c.push_back({(long)L * ns, L});
-    }
-    std::sort(c.begin(), c.end());
     int k = 0;
-    for (; k < n && k < (int)c.size(); k++) out[k] = c[k].second;
+    for (int i = 0; i < colfft::kNumLengths && k < n; i++)
+        if (colfft::kLengths[i] >= need) out[k++] = colfft::kLengths[i];
     return k;
 }
 
-static int colfft_nc(int L) { return L <= 1600 ? 4 : 2; }
-static bool colfft_fits(int L, int nc, int pitch)
+// CTA widths (columns per CTA) compiled for length L: the default and twice it.
+static bool ncol_ok(int L, int nc, int pitch)
 {
-    const int nel = L * nc;
-    return (nc == 4 || nc == 2) && (size_t)nel <= (size_t)kFftThreads * 13 && pitch % nc == 0 &&
-           sizeof(float2) * 2 * (size_t)(nel + (nel >> 4) + 1) <= 112 * 1024;
+    colfft::LenInfo li;
+    if (!colfft::len_info(L, &li)) return false;
+    if (nc != li.ncol_default && nc != 2 * li.ncol_default) return false;
+    return li.T * nc <= 512 && (size_t)nc * li.smem_col <= 227 * 1024 && pitch % nc == 0;
 }
 
 int WffPlan::init_colfft()
 {
     if (prec != GLSU_F32) return GLSU_OK;
     int L;
-    if (length_candidates(H + 2 * sy, &L, 1) < 1) return GLSU_OK;  // no suitable length: direct kernel
-    if (!colfft_fits(L, colfft_nc(L), pitch)) return GLSU_OK;      // registers per thread, shared memory
+    if (length_candidates(H + 2 * sy, &L, 1) < 1) return GLSU_OK;  // taller than the longest plan: direct kernel
     return build_colfft(L);
 }
 
-// Tables of the FFT sweep for transform length L (replacing any others), with
-// the default plan variant: H_k = DFT of h_k(m) = gy(m) e^{j wy_k m},
-// m in [-sy, sy] placed circularly, and the twiddles e^{-2 pi i t / L}.
+// Tables of the FFT sweep for transform length L (replacing any others),
+// with the default CTA width: H_k = DFT of h_k(m) = gy(m) e^{j wy_k m},
+// m in [-sy, sy] placed circularly, and the twiddles e^{-2 pi i t / L},
+// both computed in FP64.
 int WffPlan::build_colfft(int L)
 {
-    if (prec != GLSU_F32 || L < H + 2 * sy || !colfft_fits(L, colfft_nc(L), pitch))
-        return fail(GLSU_ERR_UNSUPPORTED, "no shared-memory FFT plan of that length for this handle");
-    int rad[12];
-    const int ns = factor(L, rad);
-    if (ns < 1 || ns > 12) return fail(GLSU_ERR_UNSUPPORTED, "transform length has a prime factor above 5");
+    colfft::LenInfo li;
+    if (prec != GLSU_F32 || L < H + 2 * sy || !colfft::len_info(L, &li))
+        return fail(GLSU_ERR_UNSUPPORTED, "no compiled FFT plan of that length for this handle");
     release_colfft();
     std::vector<float> kh(2 * (size_t)nfy * L), tw(2 * (size_t)L);
     for (int k = 0; k < nfy; k++) {
@@ -402,7 +104,8 @@ int WffPlan::build_colfft(int L)
     GLSU_CUDA_TRY(cudaMemcpy(d_khat, kh.data(), kh.size() * sizeof(float), cudaMemcpyHostToDevice));
     GLSU_CUDA_TRY(cudaMemcpy(d_tw, tw.data(), tw.size() * sizeof(float), cudaMemcpyHostToDevice));
     fft_L = L;
-    return set_fft_plan(colfft_nc(L), 0);
+    fft_nst = li.passes;
+    return set_fft_plan(li.ncol_default, 0);
 }
 
 int fft_length_candidates(const WffPlan &P, int *out, int n)
@@ -411,18 +114,15 @@ int fft_length_candidates(const WffPlan &P, int *out, int n)
     return length_candidates(P.H + 2 * P.sy, out, n);
 }
 
+// Plan variant: nc columns per CTA (the length's default or twice it);
+// radix order 0 only (each length has one compiled radix sequence).
 int WffPlan::set_fft_plan(int nc, int order)
 {
     if (fft_L == 0) return fail(GLSU_ERR_UNSUPPORTED, "no shared-memory FFT plan for this handle");
-    if (order < 0 || order > 2 || !colfft_fits(fft_L, nc, pitch))
-        return fail(GLSU_ERR_UNSUPPORTED, "FFT plan variant does not fit this transform length");
-    int rad[12];
-    const int ns = factor(fft_L, rad, order);
-    if (ns < 1 || ns > 12) return fail(GLSU_ERR_UNSUPPORTED, "transform length does not factor in that order");
+    if (order != 0 || !ncol_ok(fft_L, nc, pitch))
+        return fail(GLSU_ERR_UNSUPPORTED, "FFT plan variant not compiled for this transform length");
     fft_nc = nc;
     fft_order = order;
-    fft_nst = ns;
-    for (int k = 0; k < ns; k++) fft_radix[k] = rad[k];
     return GLSU_OK;
 }
 
@@ -434,53 +134,31 @@ void WffPlan::release_colfft()
     fft_L = 0;
 }
 
-template <int NC, int MAXE> static int launch_colfft_t(const WffPlan &P, cudaStream_t s)
+int launch_colfft(const WffPlan &P, cudaStream_t s)
 {
-    ColFftPlan cp;
-    cp.L = P.fft_L;
-    cp.nst = P.fft_nst;
-    for (int k = 0; k < 12; k++) cp.radix[k] = k < P.fft_nst ? P.fft_radix[k] : 0;
-    const int nel = cp.L * NC;
-    const size_t smem = sizeof(float2) * 2 * (size_t)(nel + (nel >> 4) + 1);
-    GLSU_TRY(raise_smem_limit((const void *)wff_colfft_kernel<NC, MAXE>, 112 * 1024));
-    if (smem > 112 * 1024) return fail(GLSU_ERR_UNSUPPORTED, "column FFT length too large");
-    const double N = 1.0 / P.inv_norm;
-    const int ngroups = P.pitch / NC;
-    dim3 grid(ngroups, P.nfx);
+    const int ngroups = P.pitch / P.fft_nc;
+    int grid_x = ngroups;
     const int2 *list = nullptr;
     const int *count = nullptr;
     if (P.mask.flags) {
-        // tile-masked run: the column groups whose columns, grown by sx,
-        // meet a flagged tile (all rows: a column's transform spans them)
+        // tile-masked run (the surrogate's per-tile fallback): the column
+        // groups whose columns, grown by sx, meet a flagged tile; all rows,
+        // since a column's transform spans them.  Each column is computed as
+        // in the full frame, so its outputs are the same bits.
         if (!P.d_list) return fail(GLSU_ERR_INVALID, "tile-masked run without a tile list buffer");
         TileMask m = P.mask;
         m.my = 0;
         m.mx = P.sx;
-        GLSU_TRY(launch_mask_list(m, ngroups, 1, P.H, NC, P.d_list, P.d_list_count, s));
+        GLSU_TRY(launch_mask_list(m, ngroups, 1, P.H, P.fft_nc, P.d_list, P.d_list_count, s));
         list = P.d_list;
         count = P.d_list_count;
-        grid.x = std::max(1, std::min(ngroups, (2 * device_sm_count() + P.nfx - 1) / P.nfx));
+        grid_x = std::max(1, std::min(ngroups, (2 * device_sm_count() + P.nfx - 1) / P.nfx));
     }
-    wff_colfft_kernel<NC, MAXE><<<grid, kFftThreads, smem, s>>>(
-        (const float2 *)P.d_R, (float2 *)P.d_C, P.H, P.pitch, P.nfy, (const float2 *)P.d_khat,
-        (const float2 *)P.d_tw, cp, (const float *)P.d_thr, (float)(cp.L * N),
-        (float)(1.0 / ((double)cp.L * cp.L * N)), list, count);
-    GLSU_CUDA_TRY(cudaGetLastError());
-    return GLSU_OK;
-}
-
-int launch_colfft(const WffPlan &P, cudaStream_t s)
-{
-    const int nc = P.fft_nc;
-    const int per = (P.fft_L * nc + kFftThreads - 1) / kFftThreads;  // elements owned per thread
-    if (nc == 4) {
-        if (per <= 3) return launch_colfft_t<4, 3>(P, s);
-        if (per <= 5) return launch_colfft_t<4, 5>(P, s);
-        if (per <= 10) return launch_colfft_t<4, 10>(P, s);
-        return launch_colfft_t<4, 13>(P, s);
-    }
-    if (per <= 10) return launch_colfft_t<2, 10>(P, s);
-    return launch_colfft_t<2, 13>(P, s);
+    int rc = colfft::launch_len_small(P.fft_L, P.fft_nc, P, s, list, count, grid_x);
+    if (rc == GLSU_ERR_UNSUPPORTED) rc = colfft::launch_len_mid(P.fft_L, P.fft_nc, P, s, list, count, grid_x);
+    if (rc == GLSU_ERR_UNSUPPORTED) rc = colfft::launch_len_large(P.fft_L, P.fft_nc, P, s, list, count, grid_x);
+    if (rc == GLSU_ERR_UNSUPPORTED) return fail(GLSU_ERR_UNSUPPORTED, "no compiled FFT plan for this length");
+    return rc;
 }
 
 // ---------------------------------------------------------------------------
@@ -492,17 +170,14 @@ int launch_colfft(const WffPlan &P, cudaStream_t s)
 // below runs only on request (GLSU_METHOD_TIMED, or GLSU_AUTOTUNE=time in
 // the environment).
 //
-// Timed search.  Candidates: the direct column kernel, and the FFT sweep at the three
-// cheapest transform lengths (L x stages), then, at the fastest length, with
-// 4 or 2 columns per CTA and each radix order.  Each is launched once
-// (warm-up), then twice between CUDA events on the plan's own buffers; the
-// kernels have no data-dependent control flow, so the buffers' contents do
-// not matter.  The FFT is taken only when at least 10% faster than the
-// direct kernel, so that near ties keep the direct kernel, and the plan
-// variants are tried only when the best length is within 1.5x of it.  Results are kept
-// per shape for the process, so every handle of a shape runs the same
-// kernels.  GLSU_AUTOTUNE=0 in the environment skips the timing (the direct
-// kernel).
+// Timed search.  Candidates: the direct column kernel, and the FFT sweep at
+// the two shortest compiled transform lengths, then, at the faster length,
+// with the other compiled CTA width.  Each is launched once (warm-up), then
+// twice between CUDA events on the plan's own buffers; the kernels have no
+// data-dependent control flow, so the buffers' contents do not matter.  The
+// FFT is taken only when at least 10% faster than the direct kernel, so
+// that near ties keep the direct kernel.  Results are kept per shape for the
+// process, so every handle of a shape runs the same kernels.
 namespace {
 struct TuneKey {
     int v[9];
@@ -514,6 +189,18 @@ struct TuneResult {
 };
 std::mutex g_tune_mu;
 std::map<TuneKey, TuneResult> g_tune;
+
+// Throughputs of the column-sweep cost model (WffPlan::model_ms), measured
+// on GB300 at 2070 MHz from 256^2 to 2048^2: direct kernel in tap-units per
+// second per instantiated half-size; FFT sweep in (length x passes) units
+// per second, with the load, window products and store of a column worth
+// kModelFftColumnUnits passes; both plus a launch and tail constant.
+constexpr double kModelDirectRate30 = 1.1e13;
+constexpr double kModelDirectRate45 = 5.5e12;
+constexpr double kModelDirectRate60 = 3.95e12;
+constexpr double kModelFftRate = 1.35e12;
+constexpr double kModelFftColumnUnits = 30.0;
+constexpr double kModelLaunchMs = 0.05;
 }  // namespace
 
 // Modelled device time (ms) of one full-frame column sweep of this plan.
@@ -521,33 +208,32 @@ std::map<TuneKey, TuneResult> g_tune;
 // filters of 2S+1 taps (S the instantiated half-size), the first one also
 // over the 2S-row halo of each 128-row tile, at a rate per instantiation.
 // FFT sweep: per column and x-frequency, 2 nfy + 2 transforms of length L
-// with nst stages, at a rate scaled down when a CTA's L x columns elements
-// leave its 512 threads short of work.  The rates are GB300 measurements
-// (2070 MHz) of both kernels at 256^2 .. 2048^2.
+// in a number of radix passes.
 double WffPlan::model_ms(int m) const
 {
     if (m == GLSU_METHOD_FFT) {
         if (fft_L == 0) return 1e30;
-        const double units = (double)pitch * nfx * (2.0 * nfy + 2.0) * fft_L * fft_nst;
-        const double fill = std::min(1.0, (double)fft_L * fft_nc / (kFftThreads * 8.0));
-        return units / (kModelFftRate * fill) * 1e3;
+        const double units = (double)pitch * nfx * fft_L * (fft_nst * (2.0 * nfy + 2.0) + kModelFftColumnUnits);
+        return units / kModelFftRate * 1e3 + kModelLaunchMs;
     }
     const int S = syi;
     const double taps = (2.0 * S + 1.0) * (2.0 + 2.0 * S / 128.0);
     const double rate = S <= 30 ? kModelDirectRate30 : (S <= 45 ? kModelDirectRate45 : kModelDirectRate60);
-    return (double)pitch * H * nfx * nfy * taps / rate * 1e3;
+    return (double)pitch * H * nfx * nfy * taps / rate * 1e3 + kModelLaunchMs;
 }
 
-// AUTO without timing: the transform length cheapest by L x stages (built
-// by init_colfft), the default plan variant, and the FFT sweep when its
-// modelled time is below 0.9 x the direct kernel's.
+// AUTO without timing: the shortest compiled transform length (built by
+// init_colfft), its default CTA width, and the FFT sweep when its modelled
+// time is below 0.9 x the direct kernel's.
 int WffPlan::choose_by_model()
 {
     auto_method = GLSU_METHOD_DIRECT;
     if (prec != GLSU_F32 || fft_L == 0 || d_khat == nullptr) return GLSU_OK;
     int L;
     if (length_candidates(H + 2 * sy, &L, 1) == 1 && L != fft_L) GLSU_TRY(build_colfft(L));
-    GLSU_TRY(set_fft_plan(colfft_nc(fft_L), 0));
+    colfft::LenInfo li;
+    colfft::len_info(fft_L, &li);
+    GLSU_TRY(set_fft_plan(li.ncol_default, 0));
     tune_ms_direct = (float)model_ms(GLSU_METHOD_DIRECT);
     tune_ms_fft = (float)model_ms(GLSU_METHOD_FFT);
     if (tune_ms_fft < 0.9f * tune_ms_direct) auto_method = GLSU_METHOD_FFT;
@@ -591,8 +277,8 @@ int WffPlan::autotune(cudaStream_t s)
         TuneResult r{GLSU_METHOD_DIRECT, fft_L, fft_nc, fft_order, 0.f, 0.f};
         time_it(GLSU_METHOD_DIRECT, &r.ms_direct);
         float best = -1.f;
-        int lens[3];
-        const int nl = length_candidates(H + 2 * sy, lens, 3);
+        int lens[2];
+        const int nl = length_candidates(H + 2 * sy, lens, 2);
         for (int j = 0; j < nl && rc == GLSU_OK; j++) {
             if (build_colfft(lens[j]) != GLSU_OK) continue;
             float ms = 0;
@@ -605,18 +291,12 @@ int WffPlan::autotune(cudaStream_t s)
             }
         }
         if (rc == GLSU_OK && r.L != fft_L) rc = build_colfft(r.L);
-        const int nc0 = fft_nc;
-        for (int nc : {nc0, 6 - nc0}) {
-            if (rc != GLSU_OK || best < 0 || best > 1.5f * r.ms_direct) break;
-            for (int order = 0; order < 3 && rc == GLSU_OK; order++) {
-                if ((nc == nc0 && order == 0) || set_fft_plan(nc, order) != GLSU_OK) continue;
-                float ms = 0;
-                time_it(GLSU_METHOD_FFT, &ms);
-                if (rc == GLSU_OK && ms < best) {
-                    best = ms;
-                    r.nc = nc;
-                    r.order = order;
-                }
+        if (rc == GLSU_OK && best > 0 && set_fft_plan(2 * fft_nc, 0) == GLSU_OK) {
+            float ms = 0;
+            time_it(GLSU_METHOD_FFT, &ms);
+            if (rc == GLSU_OK && ms < best) {
+                best = ms;
+                r.nc = fft_nc;
             }
         }
         set_error(std::string());  // variants that did not fit leave no message

@@ -650,8 +650,8 @@ int WffPlan::alloc_tile_list()
 {
     if (d_list) return GLSU_OK;
     // column tiles of the direct sweep are 32 columns x at least 32 rows;
-    // column groups of the FFT sweep are 2 or 4 whole columns
-    const size_t cap = std::max((size_t)(pitch / 32) * ((H + 31) / 32), (size_t)(pitch / 2));
+    // column groups of the FFT sweep are 1 to 16 whole columns
+    const size_t cap = std::max((size_t)(pitch / 32) * ((H + 31) / 32), (size_t)pitch);
     if (cudaMalloc((void **)&d_list, cap * sizeof(int2)) != cudaSuccess ||
         cudaMalloc((void **)&d_list_count, sizeof(int)) != cudaSuccess)
         return fail(GLSU_ERR_ALLOC, "cudaMalloc of the tile list failed");

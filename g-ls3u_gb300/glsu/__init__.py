@@ -37,6 +37,7 @@ F32, F64, U8 = 0, 1, 2
 PHI_REF, PHI_CURR, DPHI_REF, DPHI = 0, 1, 2, 3
 WFT_WFF, WFT_WFR = 0, 1
 METHOD_AUTO, METHOD_DIRECT, METHOD_FFT, METHOD_TIMED = 0, 1, 2, 3
+AIA_ERR_ABS, AIA_ERR_RELATIVE = 0, 1
 LS_FLOAT_FLOAT, LS_FP64_SUMS = 0, 1
 
 _lock = threading.Lock()
@@ -158,6 +159,7 @@ def lib() -> ctypes.CDLL:
             "glsu_dpra_stage_times": ([c_void_p, fltp, c_int], c_int),
             "glsu_aia_create": ([pp, c_int, c_int, c_int], c_int),
             "glsu_aia_destroy": ([c_void_p], c_int),
+            "glsu_aia_set_convergence": ([c_void_p, c_int], c_int),
             "glsu_aia_set_stream": ([c_void_p, c_void_p], c_int),
             "glsu_aia_run": ([c_void_p, pp, c_int, fltp, fltp, c_int, dblp, intp, fltp, c_int, c_float,
                               ctypes.c_uint64], c_int),
@@ -548,6 +550,11 @@ class AIA:
             self._h = None
 
     __del__ = close
+
+    def set_convergence(self, relative: bool):
+        """Convergence measure: relative=False is AIA_CUDAF's max |delta - old|,
+        True the change of the shifts relative to the first (AIA_CUDAF_YC2)."""
+        check(lib().glsu_aia_set_convergence(self._h, AIA_ERR_RELATIVE if relative else AIA_ERR_ABS))
 
     def run(self, frames, deltas=None, max_iter: int = 20, max_err: float = 1e-4, seed: int = 0):
         frames = [np.ascontiguousarray(f) for f in frames]

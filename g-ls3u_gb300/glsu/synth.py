@@ -46,6 +46,50 @@ def sequence(H: int, W: int, nframes: int, seed: int = 0, noise: float = 0.02, n
     return frames, phi0, delta
 
 
+def sequence_params(H: int, W: int, seed: int = 0, n_gauss: int = 4):
+    """The deterministic part of ``sequence``'s generator for a seed:
+    (a, b, phi0, delta), drawn in the same order, so that
+    a + b cos(phi0 + k delta) is its noise-free frame k."""
+    rng = np.random.default_rng(seed)
+    scale = max(H, W) / 256.0
+    y, x = np.mgrid[0:H, 0:W].astype(np.float64)
+    cy, cx = rng.uniform(0, H), rng.uniform(0, W)
+    sa = 80.0 * scale
+    a = 0.5 + 0.1 * np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2 * sa * sa))
+    phi0 = _gauss(rng, H, W, n_gauss, 5.0, 15.0, 20.0, 60.0, scale)
+    delta = _gauss(rng, H, W, 2, 0.5, 1.0, 20.0, 60.0, scale)
+    delta *= 0.3 / max(np.abs(delta).max(), 1e-12)
+    return a, 0.4, phi0, delta
+
+
+class DeviceSequence:
+    """Frames of ``sequence``'s generator made on the GPU with torch, for
+    long sequences at large sizes: I_k = a + b cos(phi0 + k delta) + N(0,
+    noise), with the noise drawn by a torch generator seeded from `seed`
+    (the same distribution as ``sequence``, not the same numbers)."""
+
+    def __init__(self, H: int, W: int, seed: int = 0, noise: float = 0.02, n_gauss: int = 4, device="cuda"):
+        import torch
+        a, b, phi0, delta = sequence_params(H, W, seed, n_gauss)
+        self.phi0, self.delta = phi0, delta
+        self._t = torch
+        self._a = torch.from_numpy(a).to(device)
+        self._b = b
+        self._phi0 = torch.from_numpy(phi0).to(device)
+        self._delta = torch.from_numpy(delta).to(device)
+        self._noise = noise
+        self._gen = torch.Generator(device=device)
+        self._gen.manual_seed(int(seed) * 7919 + 17)
+        self._dev = device
+
+    def frame(self, k: int):
+        """Frame k as a float32 device tensor (the noise of successive calls is fresh)."""
+        t = self._t
+        clean = self._a + self._b * t.cos(self._phi0 + k * self._delta)
+        n = t.randn(clean.shape, generator=self._gen, device=self._dev, dtype=t.float64) * self._noise
+        return (clean + n).to(t.float32).contiguous()
+
+
 def aia_frames(H: int, W: int, M: int, seed: int = 0, noise: float = 0.02, n_gauss: int = 4,
                bump: bool = True):
     """M frames with unknown phase shifts U(0, 2 pi): returns (frames, phi, shifts).

@@ -125,37 +125,41 @@ int glsu_wff_threshold(glsu_wff *h, double *thr);
  * transform plan exists (FP64 handles). */
 int glsu_wff_set_method(glsu_wff *h, int method);
 /* Column-sweep autotuner.
- * GLSU_METHOD_AUTO (the default): the FFT sweep at the transform length
- * cheapest by length x stages, with its default plan variant, when the cost
+ * GLSU_METHOD_AUTO (the default): the FFT sweep at the shortest compiled
+ * transform length >= H + 2 sy, with its default CTA width, when the cost
  * model puts it below 0.9 x the direct kernel's time; else the direct
  * kernel.  Decided from the shape only: deterministic.
  * GLSU_METHOD_TIMED: the handle runs the column sweep measured fastest for
- * its shape: the direct kernel, or the shared-memory FFT sweep at one of
- * the three cheapest transform lengths with 4 or 2 columns per CTA and one
- * of three radix orders (0: 8,4,2,5,3; 1: 4,2,5,3; 2: 5,3,8,4,2).  The
- * first handle of a shape in the process times the candidates (a few
- * launches each); later handles of that shape reuse the choice.  The FFT is
- * taken only when at least 10% faster.  GLSU_AUTOTUNE=time in the
- * environment makes AUTO behave as TIMED; GLSU_AUTOTUNE=0 makes both the
- * direct kernel.  The methods agree to FP32 rounding, not bit for bit. */
+ * its shape: the direct kernel, or the FFT sweep at one of the two shortest
+ * compiled transform lengths, at either compiled CTA width.  The first
+ * handle of a shape in the process times the candidates (a few launches
+ * each); later handles of that shape reuse the choice.  The FFT is taken
+ * only when at least 10% faster.  GLSU_AUTOTUNE=time in the environment
+ * makes AUTO behave as TIMED; GLSU_AUTOTUNE=0 makes both the direct kernel.
+ * The methods agree to FP32 rounding, not bit for bit.
+ * Compiled transform lengths: 256, 384, 512, 640, 768, 1024, 1280, 1536,
+ * 2048, 2560, 3072, 4096 (one radix sequence each, radix order 0); taller
+ * windows run the direct kernel. */
 typedef struct {
     int method;          /* GLSU_METHOD_DIRECT or GLSU_METHOD_FFT: the sweep that runs */
     int fft_length;      /* transform length of the FFT plan (0: no FFT plan) */
     int fft_columns;     /* columns per CTA of the FFT sweep */
-    int fft_radix_order; /* radix order of the FFT stages (see above) */
+    int fft_radix_order; /* radix order of the FFT passes (always 0) */
     int tuned;           /* 0: not resolved; 1: resolved by timing; 2: by the cost model */
     float ms_direct;     /* column-sweep time of the direct kernel: measured (tuned 1) or modelled (tuned 2) */
     float ms_fft;        /* time of the FFT sweep: best measured (tuned 1) or modelled (tuned 2) */
 } glsu_wff_tuning;
 int glsu_wff_get_tuning(const glsu_wff *h, glsu_wff_tuning *t);
-/* Force an FFT plan variant (the autotuner's knobs); GLSU_ERR_UNSUPPORTED
- * where it does not fit.  Takes effect when the FFT sweep runs. */
+/* Force an FFT plan variant: columns_per_cta is the length's default
+ * (glsu_wff_get_tuning after glsu_wff_set_fft_length) or twice it, and
+ * radix_order is 0; GLSU_ERR_UNSUPPORTED otherwise.  Takes effect when the
+ * FFT sweep runs. */
 int glsu_wff_set_fft_plan(glsu_wff *h, int columns_per_cta, int radix_order);
-/* Rebuild the FFT sweep's tables for another transform length (>= H + 2 sy,
- * factors 2, 3, 5 only) with the default plan variant. */
+/* Rebuild the FFT sweep's tables for another compiled transform length
+ * (>= H + 2 sy) with its default CTA width. */
 int glsu_wff_set_fft_length(glsu_wff *h, int length);
-/* The transform lengths the autotuner times, cheapest first (length x
- * stages); returns how many were written (at most n; 0 without an FFT plan). */
+/* The compiled transform lengths >= H + 2 sy, shortest first; returns how
+ * many were written (at most n; 0 without an FFT plan). */
 int glsu_wff_fft_lengths(const glsu_wff *h, int *lengths, int n);
 
 /* FFT-padded plane of the reference's formulation (kept for API parity). */
@@ -329,6 +333,18 @@ int glsu_aia_set_stream(glsu_aia *h, void *cuda_stream);
 int glsu_aia_run(glsu_aia *h, const void *const *h_frames, int img_type, float *h_phi, float *h_deltas,
                  int n_deltas_in, double *time_ms, int *iters, float *err, int max_iter, float max_err,
                  uint64_t seed);
+/* Convergence measure of glsu_aia_run: GLSU_AIA_ERR_ABS (the default) is
+ * AIA_CUDAF's max_i |delta_i - delta_i,old| (AIA/aia_cpu.cpp:249-263);
+ * GLSU_AIA_ERR_RELATIVE is the change of the shifts relative to the first,
+ * max_i |(delta_i - delta_0) - (delta_i,old - delta_0,old)|, as
+ * AIA_CUDAF_YC2 measures it (AIA/aia_cudaf_v2.cu:665-677).  The phase and
+ * frame steps leave a common rotation of all shifts free, and the iterates
+ * can drift along it by a constant step per iteration: then the first
+ * measure never falls below max_err although the normalised shifts have
+ * settled, and the run stops at max_iter. */
+#define GLSU_AIA_ERR_ABS 0
+#define GLSU_AIA_ERR_RELATIVE 1
+int glsu_aia_set_convergence(glsu_aia *h, int mode);
 /* Same on M device frames stored back to back (M*cols*rows), enqueued on
  * the stream; results stay on the device (d_phi, d_deltas) and *iters/*err
  * are written after an internal synchronisation. */

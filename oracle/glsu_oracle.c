@@ -701,9 +701,12 @@ int or_aia_phi_solve(int M, int N, const double *f, const double *delta, double 
 /*
  * Full AIA (aia_cpu.cpp:16-100).  delta (M) holds the initial deltas on entry
  * and the normalised deltas on exit; phi (N) receives the wrapped phase.
+ * rel = 0: the convergence measure of aia_cpu.cpp:249-263, max |delta - old|;
+ * rel = 1: that of AIA_CUDAF_YC2 (aia_cudaf_v2.cu:665-677), the change of
+ * delta_i - delta_0.
  */
-int or_aia(int M, int N, const double *f, double *delta, int max_iter, double max_err, double *phi,
-           int *iters, double *err)
+int or_aia_mode(int M, int N, const double *f, double *delta, int max_iter, double max_err, int rel, double *phi,
+                int *iters, double *err)
 {
     double *x = (double *)malloc(sizeof(double) * 3 * (size_t)N);
     double *old = (double *)malloc(sizeof(double) * (size_t)M);
@@ -716,7 +719,7 @@ int or_aia(int M, int N, const double *f, double *delta, int max_iter, double ma
         it++;
         e = 0;
         for (int i = 0; i < M; i++) {
-            double d = fabs(delta[i] - old[i]);
+            double d = rel ? fabs((delta[i] - delta[0]) - (old[i] - old[0])) : fabs(delta[i] - old[i]);
             if (d > e) e = d;
         }
     }
@@ -736,6 +739,12 @@ int or_aia(int M, int N, const double *f, double *delta, int max_iter, double ma
     free(x);
     free(old);
     return info;
+}
+
+int or_aia(int M, int N, const double *f, double *delta, int max_iter, double max_err, double *phi,
+           int *iters, double *err)
+{
+    return or_aia_mode(M, N, f, delta, max_iter, max_err, 0, phi, iters, err);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -65,7 +65,7 @@ static void OR_FN(fft_exec)(const OR_FN(fft_plan) *p, OR_REAL *x, OR_REAL *y, in
             }
             if (Ns > 1) {
                 for (int r = 1; r < R; r++) {
-                    int e = (int)(((long long)r * k * tstep) % n);
+                    const int e = r * k * tstep; /* < R Ns tstep = n */
                     OR_REAL c = p->w[2 * e], sn = sgn * p->w[2 * e + 1];
                     OR_REAL a = vr[r] * c - vi[r] * sn;
                     OR_REAL b = vr[r] * sn + vi[r] * c;
@@ -92,8 +92,9 @@ static void OR_FN(fft_exec)(const OR_FN(fft_plan) *p, OR_REAL *x, OR_REAL *y, in
                 const int step = n / R;
                 for (int q = 0; q < R; q++) {
                     OR_REAL sr = 0, si = 0;
-                    for (int r = 0; r < R; r++) {
-                        int e = (int)(((long long)q * r % R) * step);
+                    int qr = 0; /* (q r) mod R */
+                    for (int r = 0; r < R; r++, qr = (qr + q >= R) ? qr + q - R : qr + q) {
+                        const int e = qr * step;
                         OR_REAL c = p->w[2 * e], sn = sgn * p->w[2 * e + 1];
                         sr += vr[r] * c - vi[r] * sn;
                         si += vr[r] * sn + vi[r] * c;
@@ -114,10 +115,15 @@ static void OR_FN(fft_exec)(const OR_FN(fft_plan) *p, OR_REAL *x, OR_REAL *y, in
     if (in != x) memcpy(x, in, sizeof(OR_REAL) * 2 * (size_t)n);
 }
 
-/* 2D transform of an H x W row-major plane, in place. */
+/* 2D transform of an H x W row-major plane, in place.  Columns are moved
+ * through the scratch in blocks of OR_COLBLK (whole cache lines of the
+ * plane), then transformed one by one. */
+#ifndef OR_COLBLK
+#define OR_COLBLK 8
+#endif
 typedef struct {
     OR_FN(fft_plan) row, col;
-    OR_REAL *buf, *scr; /* 2*max(W,H) each */
+    OR_REAL *buf, *scr; /* buf: 2 * OR_COLBLK * H; scr: 2 * max(W, H) */
 } OR_FN(fft2_plan);
 
 static int OR_FN(fft2_init)(OR_FN(fft2_plan) *p, int W, int H)
@@ -125,7 +131,7 @@ static int OR_FN(fft2_init)(OR_FN(fft2_plan) *p, int W, int H)
     if (OR_FN(fft_plan_init)(&p->row, W)) return -1;
     if (OR_FN(fft_plan_init)(&p->col, H)) return -1;
     int m = W > H ? W : H;
-    p->buf = (OR_REAL *)malloc(sizeof(OR_REAL) * 2 * (size_t)m);
+    p->buf = (OR_REAL *)malloc(sizeof(OR_REAL) * 2 * (size_t)OR_COLBLK * (size_t)H);
     p->scr = (OR_REAL *)malloc(sizeof(OR_REAL) * 2 * (size_t)m);
     return (p->buf && p->scr) ? 0 : -1;
 }
@@ -145,15 +151,22 @@ static void OR_FN(fft2_exec)(OR_FN(fft2_plan) *p, OR_REAL *a, int inverse)
         OR_REAL *r = a + 2 * (size_t)i * W;
         OR_FN(fft_exec)(&p->row, r, p->scr, inverse);
     }
-    for (int j = 0; j < W; j++) {
+    for (int j0 = 0; j0 < W; j0 += OR_COLBLK) {
+        const int nb = W - j0 < OR_COLBLK ? W - j0 : OR_COLBLK;
         for (int i = 0; i < H; i++) {
-            p->buf[2 * i] = a[2 * ((size_t)i * W + j)];
-            p->buf[2 * i + 1] = a[2 * ((size_t)i * W + j) + 1];
+            const OR_REAL *src = a + 2 * ((size_t)i * W + j0);
+            for (int b = 0; b < nb; b++) {
+                p->buf[2 * ((size_t)b * H + i)] = src[2 * b];
+                p->buf[2 * ((size_t)b * H + i) + 1] = src[2 * b + 1];
+            }
         }
-        OR_FN(fft_exec)(&p->col, p->buf, p->scr, inverse);
+        for (int b = 0; b < nb; b++) OR_FN(fft_exec)(&p->col, p->buf + 2 * (size_t)b * H, p->scr, inverse);
         for (int i = 0; i < H; i++) {
-            a[2 * ((size_t)i * W + j)] = p->buf[2 * i];
-            a[2 * ((size_t)i * W + j) + 1] = p->buf[2 * i + 1];
+            OR_REAL *dst = a + 2 * ((size_t)i * W + j0);
+            for (int b = 0; b < nb; b++) {
+                dst[2 * b] = p->buf[2 * ((size_t)b * H + i)];
+                dst[2 * b + 1] = p->buf[2 * ((size_t)b * H + i) + 1];
+            }
         }
     }
 }

@@ -64,6 +64,7 @@ def lib():
             L.or_dpra_update.argtypes = [c_int, dp, dp, dp, dp, dp]
             L.or_aia_phi_solve.argtypes = [c_int, c_int, dp, dp, dp, dp]
             L.or_aia.argtypes = [c_int, c_int, dp, dp, c_int, c_double, dp, ip, dp]
+            L.or_aia_mode.argtypes = [c_int, c_int, dp, dp, c_int, c_double, c_int, dp, ip, dp]
             L.or_unwrap2.argtypes = [c_int, c_int, dp, c_int, c_int]
             L.or_wfr2.argtypes = [c_int, c_int, dp] + [c_double] * 8 + [dp] * 8 + [c_int]
             fp = ctypes.POINTER(ctypes.c_float)
@@ -219,15 +220,17 @@ def aia_phi_solve(frames, deltas):
     return phi.reshape(f.shape[1:]), x.reshape(-1, 3)
 
 
-def aia(frames, deltas, max_iter=20, max_err=1e-4):
+def aia(frames, deltas, max_iter=20, max_err=1e-4, relative=False):
+    """AIA (aia_cpu.cpp:16-100); relative=True measures convergence as
+    AIA_CUDAF_YC2 does (aia_cudaf_v2.cu:665-677)."""
     f = _f64(frames)
     M = f.shape[0]
     N = f[0].size
     d = _f64(deltas).copy()
     phi = np.zeros(N)
     it = ctypes.c_int(0); err = ctypes.c_double(0)
-    info = lib().or_aia(M, N, _dp(f), _dp(d), int(max_iter), float(max_err), _dp(phi),
-                        ctypes.byref(it), ctypes.byref(err))
+    info = lib().or_aia_mode(M, N, _dp(f), _dp(d), int(max_iter), float(max_err), int(relative), _dp(phi),
+                             ctypes.byref(it), ctypes.byref(err))
     if info:
         raise ValueError("matrix not positive definite")
     return phi.reshape(f.shape[1:]), d, it.value, err.value

@@ -23,16 +23,59 @@ def test_fft_model_bytes_at_1024():
     assert abs(b / 1e9 - 35.44) < 0.01          # (64 * 441 + 32) * P bytes
 
 
-def test_cpu_sample_runs_both_variants_and_extrapolates_by_rounds(monkeypatch):
-    """The CPU baseline's sample: one round of frequency rows (one per host
-    thread, at most 21), extrapolated by ceil(21 / threads) rounds; both the
-    FP64 and the FP32 restatements run."""
+def test_cpu_sample_runs_whole_frames_in_both_variants(monkeypatch):
+    """The CPU baseline's sample is a whole frame (all 21 frequency rows, at
+    any host thread count) in the FP32 and the FP64 restatement; a partial
+    sample (warm-up) sweeps fewer rows."""
     import bench
     for threads in (4, 16, 32):
         monkeypatch.setattr(os, "cpu_count", lambda t=threads: t)
         fps, secs, th, rows = bench.cpu_sample(64, prec="f32")
-        assert th == threads and rows == min(bench.NFY, threads)
-        assert fps > 0 and secs > 0
+        assert th == threads and rows == bench.NFY
+        assert fps > 0 and secs > 0 and abs(fps * secs - 1.0) < 1e-9
     monkeypatch.setattr(os, "cpu_count", lambda: 8)
     fps64, _, _, rows = bench.cpu_sample(64, 3, prec="f64")
     assert rows == 3 and fps64 > 0
+
+
+def test_reference_arm_times_every_step_as_a_whole_frame(monkeypatch):
+    """--impl reference: each timed step is one whole frame, and the line's
+    time per step is the mean of the timed steps (no extrapolation)."""
+    import argparse
+    import bench
+    calls = []
+
+    def fake(size, rows=None, seed=1000, prec="f32"):
+        calls.append((rows, prec))
+        el = 0.5 if rows is None else 0.1
+        return 1.0 / el, el, 4, bench.NFY if rows is None else rows
+
+    monkeypatch.setattr(bench, "cpu_sample", fake)
+    args = argparse.Namespace(steps=3, warmup=2, size=64, gpus=1)
+    res = bench.run_reference(args, 0, 1)
+    timed = [c for c in calls if c[0] is None]
+    assert len(timed) == 3
+    assert abs(res["ms_per_step"] - 500.0) < 1e-9 and abs(res["value"] - 2.0) < 1e-9
+    assert res["impl"] == "reference" and res["e2e"]["value"] == res["value"]
+    assert bench.run_reference(args, 1, 2) is None
+
+
+def test_aligned_phase_error_removes_the_global_constant_and_sign():
+    """AIA determines the phase up to a global constant and sign; the
+    precision form's accuracy figure removes both before measuring."""
+    import numpy as np
+    import bench
+    rng = np.random.default_rng(3)
+    truth = rng.uniform(-np.pi, np.pi, (40, 50))
+    noise = 1e-3 * rng.standard_normal(truth.shape)
+    for sgn in (1.0, -1.0):
+        est = np.angle(np.exp(1j * (sgn * (truth + 1.234) + noise)))
+        rm, mx, s, c = bench.aligned_phase_error(est, truth)
+        assert s == sgn and abs(np.angle(np.exp(1j * (c - 1.234)))) < 1e-3
+        assert abs(rm - np.sqrt(np.mean(noise ** 2))) < 2e-4 and mx < 6e-3
+
+
+def test_fft_sweep_flop_count():
+    import bench
+    f = bench.fft_sweep_flops(1024, 21, 21, 1280, 1024)
+    assert abs(f - 1024 * 21 * (44 * 5 * 1280 * 10.321928094887362 + 21 * 16 * 1280)) < 1e3

@@ -103,10 +103,10 @@ def test_column_method_switch(glsu):
 
 
 @pytest.mark.parametrize("case", [0, 2, 4])
-def test_wff_fft_plan_variants_match_oracle(glsu, oracle, case):
-    """Every FFT plan the autotuner may pick (its three transform lengths, 4 or
-    2 columns per CTA, radix orders 0, 1, 2) within the FP32 tolerance of the
-    oracle."""
+def test_wff_fft_plans_match_oracle(glsu, oracle, case):
+    """Every compiled FFT plan that fits the shape -- each transform length
+    >= H + 2s, at both compiled CTA widths -- within the FP32 tolerance of
+    the oracle; radix orders other than 0 are rejected."""
     shape, p = WFF_CASES[case]
     f = field(shape, case)
     ref, _ = oracle.wff2(f.astype(np.complex64).astype(np.complex128), *p)
@@ -116,32 +116,34 @@ def test_wff_fft_plan_variants_match_oracle(glsu, oracle, case):
     w = glsu.WFF2(shape[1], shape[0], "f32", glsu.WffParams(*p))
     w.set_method(glsu.METHOD_FFT)
     ran = 0
-    lengths = w.fft_lengths(3)
-    assert len(lengths) >= 2
+    lengths = w.fft_lengths(16)
+    assert len(lengths) >= 10
     for L in lengths:
         w.set_fft_length(L)
-        for nc in (4, 2):
-            for order in (0, 1, 2):
-                try:
-                    w.set_fft_plan(nc, order)
-                except glsu.GlsuError as e:
-                    assert e.code == glsu.ERR_UNSUPPORTED
-                    continue
-                w.run(t.data_ptr(), out.data_ptr())
-                perr, rel = compare(out.cpu().numpy(), ref)
-                print("fft plan case %d L %d nc %d order %d: phase err %.3g, rel %.3g" % (case, L, nc, order, perr,
-                                                                                          rel))
-                assert perr < F32_PHASE_TOL and rel < 1e-4
-                ran += 1
+        nc0 = w.tuning()["fft_columns"]
+        for nc in (nc0, 2 * nc0):
+            try:
+                w.set_fft_plan(nc, 0)
+            except glsu.GlsuError as e:
+                assert e.code == glsu.ERR_UNSUPPORTED
+                continue
+            w.run(t.data_ptr(), out.data_ptr())
+            perr, rel = compare(out.cpu().numpy(), ref)
+            print("fft plan case %d L %d nc %d: phase err %.3g, rel %.3g" % (case, L, nc, perr, rel))
+            assert perr < F32_PHASE_TOL and rel < 1e-4
+            ran += 1
+        with pytest.raises(glsu.GlsuError):
+            w.set_fft_plan(nc0, 1)
     w.close()
-    assert ran >= 6
+    assert ran >= len(lengths)
 
 
 def test_autotuner_choices(glsu, oracle):
     """METHOD_AUTO (the default) resolves from the shape by the cost model,
     with no timing: with the reference's DPRA WFF parameters (sigma 20, 7x7
-    frequencies) it is the FFT sweep, with sigma 10 and 21x21 frequencies the
-    direct kernel, bit for bit an explicit METHOD_DIRECT handle's output.
+    frequencies) and with sigma 10 and 21x21 frequencies it is the FFT sweep,
+    for a narrow window on a small frame the direct kernel, in each case bit
+    for bit the output of a handle with that method set explicitly.
     METHOD_TIMED times the candidates once per shape and process and picks
     the FFT sweep for the DPRA defaults (about 3x faster there)."""
     import os
@@ -177,11 +179,24 @@ def test_autotuner_choices(glsu, oracle):
     p10 = glsu.WffParams(10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)
     f = field((256, 256), 4)
     a, _, _ = wff_gpu(glsu, f, "f32", p10)
-    b, _, _ = wff_gpu(glsu, f, "f32", p10, glsu.METHOD_DIRECT)
+    b, _, _ = wff_gpu(glsu, f, "f32", p10, glsu.METHOD_FFT)
     w = glsu.WFF2(256, 256, "f32", p10)
     tu = w.tuning()
     w.close()
     print("model choice, sigma 10 21x21 256^2:", tu)
+    assert tu["method"] == glsu.METHOD_FFT and tu["tuned"] == 2
+    assert np.array_equal(a, b)
+
+    # a narrow window (half-size 12) on a small frame: the direct kernel,
+    # bit for bit an explicit METHOD_DIRECT handle's output
+    p4 = glsu.WffParams(4.0, -1.0, 1.0, 0.25, 4.0, -1.0, 1.0, 0.25, 0.5)
+    f = field((64, 80), 5)
+    a, _, _ = wff_gpu(glsu, f, "f32", p4)
+    b, _, _ = wff_gpu(glsu, f, "f32", p4, glsu.METHOD_DIRECT)
+    w = glsu.WFF2(80, 64, "f32", p4)
+    tu = w.tuning()
+    w.close()
+    print("model choice, sigma 4 9x9 64x80:", tu)
     assert tu["method"] == glsu.METHOD_DIRECT and tu["tuned"] == 2
     assert np.array_equal(a, b)
 
@@ -571,6 +586,25 @@ def test_aia_synthetic_matches_oracle(glsu, oracle, synth, M):
     a.close()
 
 
+@pytest.mark.parametrize("M", [5, 8])
+def test_aia_relative_convergence_matches_oracle(glsu, oracle, synth, M):
+    """With the convergence measure of AIA_CUDAF_YC2 (the change of the shifts
+    relative to the first) the GPU stops where the oracle stops, well before
+    the cap, with the oracle's shifts and phase."""
+    frames, _, _ = synth.aia_frames(200, 180, M, seed=1000)
+    d0 = glsu.random_deltas(M, 7)
+    a = glsu.AIA(M, 180, 200)
+    a.set_convergence(True)
+    phi, d, ms, it, err = a.run(list(frames), None, max_iter=30, max_err=1e-4, seed=7)
+    a.close()
+    ophi, od, oit, oerr = oracle.aia(frames.astype(np.float64), d0.astype(np.float64), 30, 1e-4, relative=True)
+    e_phi = np.abs(np.angle(np.exp(1j * (phi - ophi)))).max()
+    print("aia relative M=%d: iters %d/%d, err %.3g, delta err %.3g, phi err %.3g"
+          % (M, it, oit, err, np.abs(d - od).max(), e_phi))
+    assert it == oit and it < 30 and err <= 1e-4
+    assert np.abs(d - od).max() < 1e-4 and e_phi < 1e-3
+
+
 def test_wff_phase_equivariance_full_size(glsu):
     """Size-independent property at 1024x1024: WFF2(e^{ja} f) = e^{ja} WFF2(f)."""
     torch = _torch()
@@ -751,7 +785,15 @@ def test_wff_matches_reference_wft2_cpu(glsu, prec):
     g = _ref_gold()
     for k in range(3):
         f, ref = g["wff%d_in" % k], g["wff%d_out" % k]
-        out, thr, _ = wff_gpu(glsu, f, prec, glsu.WffParams(*g["wff%d_params" % k]))
+        p = g["wff%d_params" % k]
+        counts = [(glsu.wff_count(p[1 + o], p[2 + o], p[3 + o], glsu.F32),
+                   glsu.wff_count(p[1 + o], p[2 + o], p[3 + o], glsu.F64)) for o in (0, 4)]
+        if prec == "f32" and any(a != b for a, b in counts):
+            # the reference counts frequencies in the class's precision: the
+            # float class sweeps another grid than the double class's fixture
+            print("f32 case %d skipped: frequency counts (float, double) %s" % (k, counts))
+            continue
+        out, thr, _ = wff_gpu(glsu, f, prec, glsu.WffParams(*p))
         perr, rel = compare(out, ref, 1e-3)
         print("%s case %d: phase %.3g rad, rel %.3g, thr %.9g / %.9g" % (prec, k, perr, rel, thr, g["wff%d_thr" % k]))
         if prec == "f64":

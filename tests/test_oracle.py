@@ -217,3 +217,28 @@ def test_unwrap_matches_matlab_loops(oracle, shape, start):
     u = oracle.unwrap2(smooth, *start)
     d = u - (0.4 * x - 0.3 * y)
     assert np.allclose(d, d[start], atol=1e-12)
+
+
+def test_aia_iterates_drift_along_the_common_rotation(oracle):
+    """AIA's phase and frame steps leave a common rotation of all shifts
+    free.  On the synthetic 5-frame data the iterates drift along it by a
+    constant step per iteration, so the reference's measure max|delta - old|
+    (aia_cpu.cpp:249-263) stays constant and the run stops at the cap, while
+    the normalised shifts have settled; the measure of AIA_CUDAF_YC2
+    (aia_cudaf_v2.cu:665-677), relative to the first shift, converges, to the
+    same normalised shifts and phase."""
+    import glsu
+    from glsu import synth
+    fr, _, _ = synth.aia_frames(96, 80, 5, seed=1000)
+    f = fr.astype(np.float64)
+    d0 = glsu.random_deltas(5, 1000).astype(np.float64)
+    _, da, it_a, err_a = oracle.aia(f, d0, 40, 1e-4)
+    _, db, it_b, err_b = oracle.aia(f, d0, 41, 1e-4)
+    assert it_a == 40 and it_b == 41 and abs(err_a - err_b) < 1e-6 * err_a
+    assert err_a > 1e-4
+    assert np.abs(da - db).max() < 1e-9                      # settled, although the measure is not small
+    pr, dr, it_r, err_r = oracle.aia(f, d0, 40, 1e-4, relative=True)
+    print("abs measure: %d iterations, err %.3g; relative measure: %d iterations, err %.3g" % (it_a, err_a, it_r,
+                                                                                            err_r))
+    assert it_r < 40 and err_r <= 1e-4
+    assert np.abs(np.angle(np.exp(1j * (dr - da)))).max() < 1e-3  # within a few stopping tolerances
