@@ -123,6 +123,7 @@ struct glsu_dpra {
     bool unwrap = false;  // MATLAB fp_ls3u semantics: dphi = dphi_ref + unwrap(t)
     int unwrap_row = -1, unwrap_col = -1;
     int ls_method = GLSU_LS_FLOAT_FLOAT;
+    int ls_tile = 0;  // output tile of the float-float LS: 0 = 32 x 16, 1 = 32 x 8, 2 = 32 x 32
     cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     int frames_done = 0;
@@ -816,7 +817,7 @@ static int dpra_enqueue_frame(glsu_dpra *h, const void *d_img, int img_type)
     cudaEvent_t *ev = h->timing ? h->ev : nullptr;
     if (ev) GLSU_CUDA_TRY(cudaEventRecord(ev[4], h->stream));
     GLSU_TRY(launch_dpra_ls(h->prec, img_type, d_img, h->d_phi[GLSU_PHI_REF], h->d_z, h->W, h->H, h->r, h->stream,
-                            h->ls_method));
+                            h->ls_method, h->ls_tile));
     if (h->sur)
         GLSU_TRY(dpra_surrogate_frame(h, ev));
     else
@@ -968,6 +969,71 @@ extern "C" int glsu_dpra_set_ls_method(glsu_dpra *h, int method)
     if (method != GLSU_LS_FLOAT_FLOAT && method != GLSU_LS_FP64_SUMS)
         return fail(GLSU_ERR_INVALID, "unknown least-squares method");
     h->ls_method = method;
+    return GLSU_OK;
+}
+
+static const int kLsTiles[3][2] = {{32, 16}, {32, 8}, {32, 32}};
+
+extern "C" int glsu_dpra_set_ls_tile(glsu_dpra *h, int tile_width, int tile_height)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    for (int t = 0; t < 3; t++)
+        if (kLsTiles[t][0] == tile_width && kLsTiles[t][1] == tile_height) {
+            dpra_drop_graphs(h);
+            GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
+            h->ls_tile = t;
+            return GLSU_OK;
+        }
+    return fail(GLSU_ERR_UNSUPPORTED, "least-squares tiles: 32x16, 32x8, 32x32");
+}
+
+extern "C" int glsu_dpra_get_ls_tile(const glsu_dpra *h, int *tile_width, int *tile_height)
+{
+    if (!h || !tile_width || !tile_height) return fail(GLSU_ERR_INVALID, "null argument");
+    *tile_width = kLsTiles[h->ls_tile][0];
+    *tile_height = kLsTiles[h->ls_tile][1];
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_tune_ls_tile(glsu_dpra *h, float *ms)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    if (h->prec != GLSU_F32 || h->ls_method != GLSU_LS_FLOAT_FLOAT)
+        return fail(GLSU_ERR_UNSUPPORTED, "the least-squares tile is a knob of the FP32 float-float form");
+    dpra_drop_graphs(h);
+    cudaStream_t s = h->stream;
+    // a zero frame against the handle's own reference phase: the kernels'
+    // work does not depend on the values
+    GLSU_CUDA_TRY(cudaMemsetAsync(h->d_img, 0, (size_t)h->W * h->H * sizeof(float), s));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return fail(GLSU_ERR_CUDA, "cudaEventCreate failed");
+    }
+    int best = 0, rc = GLSU_OK;
+    float best_ms = 0;
+    for (int t = 0; t < 3 && rc == GLSU_OK; t++) {
+        for (int k = 0; k < 4 && rc == GLSU_OK; k++) {
+            if (k == 1 && cudaEventRecord(e0, s) != cudaSuccess) rc = fail(GLSU_ERR_CUDA, "cudaEventRecord");
+            if (rc == GLSU_OK)
+                rc = launch_dpra_ls(h->prec, GLSU_F32, h->d_img, h->d_phi[GLSU_PHI_REF], h->d_z, h->W, h->H, h->r, s,
+                                    h->ls_method, t);
+        }
+        float t_ms = 0;
+        if (rc == GLSU_OK && (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                              cudaEventElapsedTime(&t_ms, e0, e1) != cudaSuccess))
+            rc = fail(GLSU_ERR_CUDA, "timing a least-squares tile failed");
+        t_ms /= 3;
+        if (ms) ms[t] = t_ms;
+        if (rc == GLSU_OK && (t == 0 || t_ms < best_ms)) {
+            best = t;
+            best_ms = t_ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != GLSU_OK) return rc;
+    h->ls_tile = best;
     return GLSU_OK;
 }
 

@@ -212,8 +212,10 @@ int launch_mask_list(const TileMask &m, int ncx, int ncy, int ty_rows, int tx_co
 // ---------------------------------------------------------------------------
 // kernel launchers
 // ---------------------------------------------------------------------------
+// tile (FP32 float-float form only): 0 = 32 x 16 outputs per CTA (the
+// default), 1 = 32 x 8, 2 = 32 x 32.
 int launch_dpra_ls(int prec, int img_type, const void *d_img, const void *d_phiref, void *d_z, int W, int H,
-                   int r, cudaStream_t s, int method = GLSU_LS_FLOAT_FLOAT);
+                   int r, cudaStream_t s, int method = GLSU_LS_FLOAT_FLOAT, int tile = 0);
 int launch_dpra_update(int prec, const void *d_filtered, const void *phiref, const void *dphiref,
                        void *phicurr, void *dphi, int n, cudaStream_t s);
 // Line-scanning unwrapping in place; d_add (optional) is added to every

@@ -186,6 +186,9 @@ def lib() -> ctypes.CDLL:
                                            ctypes.POINTER(ctypes.c_longlong), fltp, intp], c_int),
             "glsu_dpra_lsq_device": ([c_void_p, c_void_p], c_int),
             "glsu_dpra_set_ls_method": ([c_void_p, c_int], c_int),
+            "glsu_dpra_set_ls_tile": ([c_void_p, c_int, c_int], c_int),
+            "glsu_dpra_get_ls_tile": ([c_void_p, intp, intp], c_int),
+            "glsu_dpra_tune_ls_tile": ([c_void_p, fltp], c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -458,6 +461,21 @@ class DPRA:
         t = WffTuningC()
         check(lib().glsu_dpra_get_tuning(self._h, ctypes.byref(t)))
         return t.asdict()
+
+    def set_ls_tile(self, width: int, height: int):
+        """Output tile of the FP32 float-float least squares: 32x16 (default), 32x8 or 32x32."""
+        check(lib().glsu_dpra_set_ls_tile(self._h, width, height))
+
+    def ls_tile(self):
+        w, h = ctypes.c_int(0), ctypes.c_int(0)
+        check(lib().glsu_dpra_get_ls_tile(self._h, ctypes.byref(w), ctypes.byref(h)))
+        return w.value, h.value
+
+    def tune_ls_tile(self):
+        """Time the three least-squares tiles and select the fastest; returns their times (ms)."""
+        ms = (ctypes.c_float * 3)()
+        check(lib().glsu_dpra_tune_ls_tile(self._h, ms))
+        return list(ms)
 
     def set_ls_method(self, method: int):
         """FP32 least-squares arithmetic: LS_FLOAT_FLOAT (default) or LS_FP64_SUMS."""

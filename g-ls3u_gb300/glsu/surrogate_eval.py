@@ -16,8 +16,12 @@ phi_ref is taken and, from that same phi_ref and frame:
 
 Reported per sampled frame: RMSE and max |error| (wrapped, all pixels) of
 each against phi_curr64, the tiles recomputed, and the probe's recall: of
-the tiles whose network-only RMSE against phi_curr64 exceeds the tolerance,
-the fraction the probe flagged.
+the tiles whose network-only RMSE against phi_curr64 exceeds the tolerance
+(over the tile's pixels where the FP64 WFF2 magnitude is at least 0.1, the
+probe's own mask: elsewhere the phase is not defined), the fraction the
+probe flagged; and the tiles flagged although within the tolerance.  ``noisy_region`` gives a noise map
+with a region far outside the training noise, where the network's output
+degrades, so that the recall is measured on tiles that need the fallback.
 
     python -m glsu.surrogate_eval [--seeds 10] [--frames 200] [--every 20]
 """
@@ -43,14 +47,19 @@ def _stats(e):
 
 
 def deployment(glsu, params, dil, seeds, nframes=200, every=20, size=1024, noise=0.02, wff=WFF_SIGMA10,
-               radius=DPRA_RADIUS, tile=256, patch=4, tol=0.05, graph=True):
-    """Run the deployment evaluation; returns a dict of per-frame records and summaries."""
+               radius=DPRA_RADIUS, tile=256, patch=4, tol=0.05, graph=True, delta_extra=None, n_gauss=4):
+    """Run the deployment evaluation; returns a dict of per-frame records and
+    summaries.  noise: the generator's noise level, or an H x W map of it;
+    delta_extra: an H x W addition to the per-frame phase change."""
     import torch
     wp = glsu.WffParams(*wff)
     ntx, nty = -(-size // tile), -(-size // tile)
     recs = []
+    w64 = glsu.WFF2(size, size, "f64", wp)
+    zd = torch.empty((size, size), dtype=torch.complex128, device="cuda")
+    fd = torch.empty_like(zd)
     for seed in seeds:
-        seq = synth.DeviceSequence(size, size, seed=seed, noise=noise)
+        seq = synth.DeviceSequence(size, size, seed=seed, noise=noise, delta_extra=delta_extra, n_gauss=n_gauss)
         ds = glsu.DPRA(seq.phi0.astype(np.float32), 1, radius, "f32", wp)
         ds.set_surrogate(params, dil, tile, patch, tol)
         if graph:
@@ -68,7 +77,11 @@ def deployment(glsu, params, dil, seeds, nframes=200, every=20, size=1024, noise
             d64 = glsu.DPRA(pref.astype(np.float64), 1, radius, "f64", wp)
             d64.per_frame_device(buf.data_ptr(), glsu.F32)
             pc64 = d64.get(glsu.PHI_CURR)
+            d64.lsq_device(zd.data_ptr())
+            torch.cuda.synchronize()
             d64.close()
+            w64.run(zd.data_ptr(), fd.data_ptr())
+            defined = np.abs(fd.cpu().numpy()) >= 0.1  # where the WFF2 phase is defined (the probe's mask)
             # the network alone: probes on, no tile recomputed
             dn = glsu.DPRA(pref, 1, radius, "f32", wp)
             dn.set_surrogate(params, dil, tile, patch, 1e9)
@@ -86,25 +99,42 @@ def deployment(glsu, params, dil, seeds, nframes=200, every=20, size=1024, noise
             e = _wrap(pc.astype(np.float64) - pc64)
             en = _wrap(pc_net.astype(np.float64) - pc64)
             els = _wrap(pref.astype(np.float64) + np.angle(z) - pc64)
-            bad = flagged_bad = 0
+            bad = flagged_bad = good_flagged = 0
             tiles_bad_rmse = []
             for ty in range(nty):
                 for tx in range(ntx):
-                    t = en[ty * tile:(ty + 1) * tile, tx * tile:(tx + 1) * tile]
-                    r = float(np.sqrt(np.mean(t * t)))
+                    sl = (slice(ty * tile, (ty + 1) * tile), slice(tx * tile, (tx + 1) * tile))
+                    t = en[sl][defined[sl]]
+                    r = float(np.sqrt(np.mean(t * t))) if t.size else 0.0
+                    flagged = int(resid[ty * ntx + tx] > tol)
                     if r > tol:
                         bad += 1
                         tiles_bad_rmse.append(r)
-                        flagged_bad += int(resid[ty * ntx + tx] > tol)
+                        flagged_bad += flagged
+                    else:
+                        good_flagged += flagged
             rm, mx = _stats(e)
             rn, mn = _stats(en)
             rl, ml = _stats(els)
             recs.append({"seed": int(seed), "frame": k, "rmse": rm, "max": mx, "rmse_network_only": rn,
                          "max_network_only": mn, "rmse_without_network": rl, "max_without_network": ml,
                          "tiles_flagged": int(f1 - f0), "tiles": int(p1 - p0), "tiles_bad": bad,
-                         "tiles_bad_flagged": flagged_bad, "bad_tile_rmse": tiles_bad_rmse})
+                         "tiles_bad_flagged": flagged_bad, "tiles_good_flagged": good_flagged,
+                         "bad_tile_rmse": tiles_bad_rmse})
         ds.close()
+    w64.close()
     return summarise(recs, tol)
+
+
+def noisy_region(size, level=0.2, base=0.02, frac=0.25):
+    """A noise map for the probe's recall check: `base` everywhere, `level`
+    in a centred square covering `frac` of the frame, far outside the
+    training range U(0.01, 0.08), where the network's output degrades."""
+    m = np.full((size, size), base)
+    h = int(round(size * np.sqrt(frac) / 2))
+    c = size // 2
+    m[c - h:c + h, c - h:c + h] = level
+    return m
 
 
 def summarise(recs, tol=0.05):
@@ -122,7 +152,8 @@ def summarise(recs, tol=0.05):
         "rmse_without_network_median": float(np.median(rl)),
         "tiles_recomputed_fraction": float(sum(x["tiles_flagged"] for x in recs) /
                                            max(1, sum(x["tiles"] for x in recs))),
-        "tiles_over_tol": bad, "probe_recall": (caught / bad) if bad else None, "tol_rad": tol,
+        "tiles_over_tol": bad, "probe_recall": (caught / bad) if bad else None,
+        "tiles_flagged_within_tol": sum(x["tiles_good_flagged"] for x in recs), "tol_rad": tol,
         "per_frame": recs,
     }
 

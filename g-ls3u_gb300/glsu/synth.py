@@ -66,18 +66,23 @@ class DeviceSequence:
     """Frames of ``sequence``'s generator made on the GPU with torch, for
     long sequences at large sizes: I_k = a + b cos(phi0 + k delta) + N(0,
     noise), with the noise drawn by a torch generator seeded from `seed`
-    (the same distribution as ``sequence``, not the same numbers)."""
+    (the same distribution as ``sequence``, not the same numbers).  noise
+    may also be an H x W array of per-pixel standard deviations;
+    delta_extra (H x W, rad/frame) is added to the per-frame phase change."""
 
-    def __init__(self, H: int, W: int, seed: int = 0, noise: float = 0.02, n_gauss: int = 4, device="cuda"):
+    def __init__(self, H: int, W: int, seed: int = 0, noise=0.02, n_gauss: int = 4, device="cuda",
+                 delta_extra=None):
         import torch
         a, b, phi0, delta = sequence_params(H, W, seed, n_gauss)
+        if delta_extra is not None:
+            delta = delta + np.asarray(delta_extra, np.float64)
         self.phi0, self.delta = phi0, delta
         self._t = torch
         self._a = torch.from_numpy(a).to(device)
         self._b = b
         self._phi0 = torch.from_numpy(phi0).to(device)
         self._delta = torch.from_numpy(delta).to(device)
-        self._noise = noise
+        self._noise = noise if np.isscalar(noise) else torch.from_numpy(np.asarray(noise, np.float64)).to(device)
         self._gen = torch.Generator(device=device)
         self._gen.manual_seed(int(seed) * 7919 + 17)
         self._dev = device

@@ -17,6 +17,12 @@ saved as an ``.npz`` holding ``params`` (FP32), ``dilations`` and the WFF2
 parameters it was trained for.
 
     python -m glsu.train_surrogate --out glsu/surrogate_sigma10.npz
+
+For a large deployment shape, pairs come from sequences of that size only
+(frames made on the GPU), e.g. the 2048^2 workload with sigma 15:
+
+    python -m glsu.train_surrogate --size 2048 --wff 15,-1.5,1.5,0.1,15,-1.5,1.5,0.1,0.2 --radius 4 \
+        --n-gauss 8 --noise 0.02,0.08 --dilations 1,3,9,27,27,9,3,1 --out glsu/surrogate_sigma15.npz
 """
 from __future__ import annotations
 
@@ -68,6 +74,41 @@ def make_pool(size: int, nseq: int, nframes: int, seed: int, noise=(0.01, 0.08),
     w.close()
     torch.cuda.synchronize()
     return x, t
+
+
+def make_pool_device(size: int, nseq: int, nframes: int, seed: int, noise=(0.01, 0.08), wff=WFF, radius=RADIUS,
+                     n_gauss: int = 4, stride: int = 1):
+    """Like make_pool, with the frames made on the GPU (synth.DeviceSequence),
+    for large deployment sizes: every `stride`-th frame of each sequence
+    gives a pair (the sequence itself runs through every frame)."""
+    torch = _torch()
+    import glsu
+    from glsu import synth
+    wp = glsu.WffParams(*wff)
+    rng = np.random.default_rng(seed)
+    per = (nframes - 1) // stride
+    x = torch.empty((nseq * per, size, size), dtype=torch.complex64, device="cuda")
+    t = torch.empty_like(x)
+    w = glsu.WFF2(size, size, "f32", wp)
+    buf = torch.empty((size, size), dtype=torch.float32, device="cuda")
+    k = 0
+    for s in range(nseq):
+        seq = synth.DeviceSequence(size, size, seed=seed + s, noise=float(rng.uniform(*noise)), n_gauss=n_gauss)
+        d = glsu.DPRA(seq.phi0.astype(np.float32), 1, radius, "f32", wp)
+        for f in range(1, nframes):
+            buf.copy_(seq.frame(f))
+            torch.cuda.synchronize()
+            d.per_frame_device(buf.data_ptr(), glsu.F32)
+            if f % stride == 0 and k < x.shape[0]:
+                d.lsq_device(x[k].data_ptr())
+                torch.cuda.synchronize()
+                w.run(x[k].data_ptr(), t[k].data_ptr())
+                k += 1
+            d.update_ref_phi()
+        d.close()
+    w.close()
+    torch.cuda.synchronize()
+    return x[:k], t[:k]
 
 
 def phase_rmse(out, t, mask_mag: float = 0.0) -> float:
@@ -169,6 +210,29 @@ def load(path: str = DEFAULT_WEIGHTS):
     return z["params"].astype(np.float32), [int(d) for d in z["dilations"]]
 
 
+def main_large(a):
+    """Train for a large deployment shape (e.g. 2048^2 with sigma 15): pairs
+    from sequences of the generator at that size, made on the GPU."""
+    wff = tuple(float(v) for v in a.wff.split(","))
+    dil = tuple(int(v) for v in a.dilations.split(","))
+    noise = tuple(float(v) for v in a.noise.split(","))
+    t0 = time.time()
+    pool = make_pool_device(a.size, a.seqs, a.frames, seed=30_000 + a.seed, noise=noise, wff=wff, radius=a.radius,
+                            n_gauss=a.n_gauss, stride=a.stride)
+    held = make_pool_device(a.size, 2, 6, seed=97_000 + a.seed, noise=noise, wff=wff, radius=a.radius,
+                            n_gauss=a.n_gauss)
+    print("pool: %d training frames of %d^2, generated in %.1f s" % (pool[0].shape[0], a.size, time.time() - t0),
+          flush=True)
+    params, hist = train([pool], a.steps, a.batch, lr=a.lr, dilations=dil, seed=a.seed, time_budget=a.time_budget,
+                         log=lambda m: print(m, flush=True))
+    r = evaluate(params, *held, dilations=dil, limit=8)
+    print("held-out phase RMSE vs WFF2 at %d^2: %.4f (identity %.4f)" % (a.size, r[0], r[1]), flush=True)
+    np.savez(a.out, params=params, dilations=np.array(dil, np.int32), wff=np.array(wff), radius=a.radius,
+             steps=int(hist[-1][0]) if hist else 0, batch=a.batch, lr=a.lr, seed=a.seed, size=a.size,
+             pairs=pool[0].shape[0], rmse_heldout=r[0], rmse_identity=r[1], loss_history=np.array(hist))
+    print("saved", a.out)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
@@ -179,7 +243,19 @@ def main(argv=None):
     ap.add_argument("--seqs1024", type=int, default=20, help="1024^2 sequences (20 frames each)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--time-budget", type=float, default=0.0, help="seconds of training (schedule over time)")
+    ap.add_argument("--size", type=int, default=0,
+                    help="large deployment size: train on pairs from sequences of that size only (GPU-made frames)")
+    ap.add_argument("--wff", default=",".join(str(v) for v in WFF), help="WFF2 parameters (with --size)")
+    ap.add_argument("--radius", type=int, default=RADIUS, help="DPRA window radius (with --size)")
+    ap.add_argument("--dilations", default=",".join(str(v) for v in DILATIONS), help="(with --size)")
+    ap.add_argument("--noise", default="0.01,0.08", help="noise range per sequence (with --size)")
+    ap.add_argument("--n-gauss", type=int, default=4, help="Gaussians of the phase (with --size)")
+    ap.add_argument("--seqs", type=int, default=16, help="sequences (with --size)")
+    ap.add_argument("--frames", type=int, default=41, help="frames per sequence (with --size)")
+    ap.add_argument("--stride", type=int, default=2, help="every stride-th frame gives a pair (with --size)")
     a = ap.parse_args(argv)
+    if a.size:
+        return main_large(a)
     t0 = time.time()
     small = make_pool(256, a.seqs256, 20, seed=10_000 + a.seed)
     big = make_pool(1024, a.seqs1024, 21, seed=20_000 + a.seed)

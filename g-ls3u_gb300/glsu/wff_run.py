@@ -27,7 +27,7 @@ def main(argv=None):
     ap.add_argument("--wh", type=float, default=1.0)
     ap.add_argument("--step", type=float, default=0.1)
     ap.add_argument("--thr", type=float, default=0.2)
-    ap.add_argument("--method", choices=["auto", "direct", "fft"], default="auto")
+    ap.add_argument("--method", choices=["auto", "direct", "fft", "timed"], default="auto")
     ap.add_argument("--runs", type=int, default=2)
     ap.add_argument("--f64", action="store_true")
     args = ap.parse_args(argv)
@@ -44,7 +44,8 @@ def main(argv=None):
     out = torch.empty_like(df)
     p = glsu.WffParams(args.sigma, args.wl, args.wh, args.step, args.sigma, args.wl, args.wh, args.step, args.thr)
     w = glsu.WFF2(n, n, prec, p)
-    w.set_method({"auto": glsu.METHOD_AUTO, "direct": glsu.METHOD_DIRECT, "fft": glsu.METHOD_FFT}[args.method])
+    w.set_method({"auto": glsu.METHOD_AUTO, "direct": glsu.METHOD_DIRECT, "fft": glsu.METHOD_FFT,
+                  "timed": glsu.METHOD_TIMED}[args.method])
     print("tuning:", w.tuning())
     for _ in range(args.runs):
         print("ms %.3f" % w.run(df.data_ptr(), out.data_ptr()))

@@ -295,6 +295,48 @@ def test_dpra_least_squares_matches_oracle(glsu, oracle, synth, prec, r, img, ls
     d.close()
 
 
+@pytest.mark.parametrize("tile", [(32, 8), (32, 32)])
+@pytest.mark.parametrize("r,img", [(1, "u8"), (3, "f32"), (8, "f32")])
+def test_dpra_ls_tiles_match_oracle(glsu, oracle, synth, tile, r, img):
+    """The float-float least squares with the other output tiles (the DPRA
+    tile-shape knob) against the oracle, on a ragged frame, within the same
+    bound as the default tile; and within float-float rounding of it."""
+    H, W = 61, 75
+    frames, phi0, _ = synth.sequence(H, W, 3, seed=r)
+    fr = frames[2] if img == "f32" else np.clip(np.round(frames[2] * 255), 0, 255).astype(np.uint8)
+    phi_in = phi0.astype(np.float32)
+    wp = glsu.WffParams(3.0, -0.5, 0.5, 0.5, 3.0, -0.5, 0.5, 0.5, 0.1)
+    out = []
+    for t in ((32, 16), tile):
+        d = glsu.DPRA(phi_in, 1, r, "f32", wp)
+        d.set_ls_tile(*t)
+        assert d.ls_tile() == t
+        d.per_frame(fr)
+        out.append(d.get_lsq())
+        d.close()
+    zr = oracle.dpra_ls(fr.astype(np.float64), phi_in.astype(np.float64), r)
+    err = np.abs(np.angle(out[1] * np.conj(zr)))
+    dif = np.abs(np.angle(out[1] * np.conj(out[0])))
+    print("LS tile %s r=%d %s: max %.3g rad against the oracle, %.3g against 32x16" % (tile, r, img, err.max(),
+                                                                                      dif.max()))
+    assert err.max() < 1e-4 and dif.max() < 1e-4
+
+
+def test_dpra_ls_tile_tuning(glsu, synth):
+    frames, phi0, _ = synth.sequence(512, 512, 2, seed=5)
+    d = glsu.DPRA(phi0.astype(np.float32), 1, 3, "f32", glsu.WffParams(10.0, -1, 1, 0.1, 10.0, -1, 1, 0.1, 0.2))
+    assert d.ls_tile() == (32, 16)
+    ms = d.tune_ls_tile()
+    tiles = [(32, 16), (32, 8), (32, 32)]
+    print("LS tile times (ms):", dict(zip(tiles, ms)), "chosen", d.ls_tile())
+    assert all(m > 0 for m in ms) and d.ls_tile() == tiles[int(np.argmin(ms))]
+    with pytest.raises(glsu.GlsuError):
+        d.set_ls_tile(16, 16)
+    d.per_frame(frames[1])  # runs with the chosen tile
+    assert np.isfinite(d.get(glsu.PHI_CURR)).all()
+    d.close()
+
+
 MASK_MAG = 0.1  # phase compared where |filtered| >= 0.1 (unit-modulus input; median ~0.9)
 
 
