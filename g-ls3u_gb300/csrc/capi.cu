@@ -1163,6 +1163,230 @@ extern "C" int glsu_dpra_batch_step(glsu_dpra *const *handles, int n, const void
     return GLSU_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Staged batch (glsu_dpra_batch_*): one frame of every active sequence per
+// step, stage by stage.  Per sequence, on its own stream: the least squares
+// and the WFF2 row pass.  Then the FFT column sweeps of all sequences that
+// share a transform length as one persistent launch over their work list
+// (one launch per length, the lengths on parallel streams); sequences on the
+// direct sweep run it on their own stream.  Then per sequence the final row
+// pass with the phase update.  The step is captured as one CUDA graph when
+// graph mode is on.
+// ---------------------------------------------------------------------------
+struct glsu_dpra_batch {
+    std::vector<glsu_dpra *> h;
+    cudaStream_t stream = nullptr;
+    std::vector<cudaStream_t> cls_stream;  // one per transform-length class
+    std::vector<cudaEvent_t> ev;           // fork/join events
+    bool use_graph = false;
+    bool warm = false;
+    struct Graph {
+        std::vector<char> key;
+        cudaGraphExec_t exec = nullptr;
+    };
+    Graph graphs[4];
+    int graph_next = 0;
+};
+
+static int batch_event(glsu_dpra_batch *b, size_t k, cudaEvent_t *e)
+{
+    while (b->ev.size() <= k) {
+        cudaEvent_t x = nullptr;
+        GLSU_CUDA_TRY(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+        b->ev.push_back(x);
+    }
+    *e = b->ev[k];
+    return GLSU_OK;
+}
+
+// Enqueue one step on the batch stream for the handles with active[i],
+// reading each handle's frame from in[i].
+static int batch_enqueue(glsu_dpra_batch *b, const std::vector<char> &active, const std::vector<const void *> &in,
+                         int img_type)
+{
+    size_t ne = 0;
+    cudaEvent_t fork, e;
+    GLSU_TRY(batch_event(b, ne++, &fork));
+    GLSU_CUDA_TRY(cudaEventRecord(fork, b->stream));
+    // stage 1: least squares and row pass (and the direct column sweep)
+    std::map<int, std::vector<const WffPlan *>> classes;
+    for (size_t i = 0; i < b->h.size(); i++) {
+        if (!active[i]) continue;
+        glsu_dpra *h = b->h[i];
+        GLSU_CUDA_TRY(cudaStreamWaitEvent(h->stream, fork, 0));
+        GLSU_TRY(launch_dpra_ls(h->prec, img_type, in[i], h->d_phi[GLSU_PHI_REF], h->d_z, h->W, h->H, h->r,
+                                h->stream, h->ls_method, h->ls_tile));
+        GLSU_TRY(h->wff.enqueue_pre(h->stream, h->d_z));
+        if (h->wff.use_colfft()) classes[h->wff.fft_L].push_back(&h->wff);
+        else GLSU_TRY(launch_column_sweep(h->wff, h->stream));
+        GLSU_TRY(batch_event(b, ne++, &e));
+        GLSU_CUDA_TRY(cudaEventRecord(e, h->stream));
+        GLSU_CUDA_TRY(cudaStreamWaitEvent(b->stream, e, 0));
+    }
+    // stage 2: the FFT column sweeps, one persistent launch per length
+    cudaEvent_t pre;
+    GLSU_TRY(batch_event(b, ne++, &pre));
+    GLSU_CUDA_TRY(cudaEventRecord(pre, b->stream));
+    size_t c = 0;
+    for (auto &kv : classes) {
+        if (b->cls_stream.size() <= c) {
+            cudaStream_t st = nullptr;
+            GLSU_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            b->cls_stream.push_back(st);
+        }
+        cudaStream_t st = b->cls_stream[c++];
+        GLSU_CUDA_TRY(cudaStreamWaitEvent(st, pre, 0));
+        GLSU_TRY(launch_colfft_batch(kv.second.data(), (int)kv.second.size(), st));
+        GLSU_TRY(batch_event(b, ne++, &e));
+        GLSU_CUDA_TRY(cudaEventRecord(e, st));
+        GLSU_CUDA_TRY(cudaStreamWaitEvent(b->stream, e, 0));
+    }
+    // stage 3: final row pass with the phase update
+    cudaEvent_t cols;
+    GLSU_TRY(batch_event(b, ne++, &cols));
+    GLSU_CUDA_TRY(cudaEventRecord(cols, b->stream));
+    for (size_t i = 0; i < b->h.size(); i++) {
+        if (!active[i]) continue;
+        glsu_dpra *h = b->h[i];
+        GLSU_CUDA_TRY(cudaStreamWaitEvent(h->stream, cols, 0));
+        GLSU_TRY(h->wff.enqueue_final(h->stream, nullptr, h->unwrap ? 2 : 1, h->d_phi[GLSU_PHI_REF],
+                                      h->d_phi[GLSU_DPHI_REF], h->d_phi[GLSU_PHI_CURR], h->d_phi[GLSU_DPHI]));
+        if (h->unwrap)
+            GLSU_TRY(launch_unwrap(h->prec, h->d_phi[GLSU_DPHI], h->d_phi[GLSU_DPHI_REF], h->W, h->H, h->unwrap_row,
+                                   h->unwrap_col, h->stream));
+        GLSU_TRY(batch_event(b, ne++, &e));
+        GLSU_CUDA_TRY(cudaEventRecord(e, h->stream));
+        GLSU_CUDA_TRY(cudaStreamWaitEvent(b->stream, e, 0));
+    }
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_batch_create(glsu_dpra_batch **out, glsu_dpra *const *handles, int n)
+{
+    if (!out || !handles || n < 1) return fail(GLSU_ERR_INVALID, "bad argument");
+    *out = nullptr;
+    for (int i = 0; i < n; i++) {
+        glsu_dpra *h = handles[i];
+        if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+        if (h->prec != GLSU_F32 || h->sur)
+            return fail(GLSU_ERR_UNSUPPORTED, "the staged batch runs FP32 handles in the plain form");
+        if (!h->stream) return fail(GLSU_ERR_INVALID, "batched handles need their own streams, not the legacy one");
+        for (int j = 0; j < i; j++)
+            if (handles[j] == h) return fail(GLSU_ERR_INVALID, "a handle appears twice in one batch");
+    }
+    glsu_dpra_batch *b = new glsu_dpra_batch();
+    b->h.assign(handles, handles + n);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete b;
+        return fail(GLSU_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    *out = b;
+    return GLSU_OK;
+}
+
+static void batch_drop_graphs(glsu_dpra_batch *b)
+{
+    for (auto &g : b->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = glsu_dpra_batch::Graph();
+    }
+    b->warm = false;
+}
+
+extern "C" int glsu_dpra_batch_destroy(glsu_dpra_batch *b)
+{
+    if (!b) return GLSU_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    batch_drop_graphs(b);
+    for (auto st : b->cls_stream) cudaStreamDestroy(st);
+    for (auto e : b->ev) cudaEventDestroy(e);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_batch_set_graph(glsu_dpra_batch *b, int enable)
+{
+    if (!b) return fail(GLSU_ERR_INVALID, "null batch");
+    GLSU_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    batch_drop_graphs(b);
+    b->use_graph = enable != 0;
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_batch_run(glsu_dpra_batch *b, const void *const *d_frames, int img_type)
+{
+    if (!b || !d_frames) return fail(GLSU_ERR_INVALID, "null argument");
+    const size_t n = b->h.size();
+    std::vector<char> active(n, 0);
+    std::vector<const void *> in(n, nullptr);
+    for (size_t i = 0; i < n; i++) {
+        if (!d_frames[i]) continue;  // this sequence has ended
+        GLSU_TRY(dpra_check_type(b->h[i], img_type));
+        if (img_type == GLSU_F64) return fail(GLSU_ERR_INVALID, "FP32 handles take U8 or F32 frames");
+        active[i] = 1;
+        in[i] = d_frames[i];
+    }
+    if (b->use_graph && b->warm) {
+        // the graph reads each handle's own frame buffer: copy the inputs in
+        std::vector<char> key(active);
+        key.push_back((char)img_type);
+        for (size_t i = 0; i < n; i++) {
+            glsu_dpra *h = b->h[i];
+            key.push_back((char)h->phi_parity);
+            if (!active[i]) continue;
+            GLSU_CUDA_TRY(cudaMemcpyAsync(h->d_img, d_frames[i], elem_size(img_type) * (size_t)h->W * h->H,
+                                          cudaMemcpyDeviceToDevice, b->stream));
+            in[i] = h->d_img;
+        }
+        glsu_dpra_batch::Graph *g = nullptr;
+        for (auto &c : b->graphs)
+            if (c.exec && c.key == key) g = &c;
+        if (!g) {
+            g = &b->graphs[b->graph_next];
+            b->graph_next = (b->graph_next + 1) % 4;
+            if (g->exec) cudaGraphExecDestroy(g->exec);
+            *g = glsu_dpra_batch::Graph();
+            GLSU_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            const int rc = batch_enqueue(b, active, in, img_type);
+            cudaGraph_t graph = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(b->stream, &graph);
+            if (rc != GLSU_OK) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture of a batch step");
+            cudaGraphExec_t exec = nullptr;
+            const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate of a batch step");
+            g->key = key;
+            g->exec = exec;
+        }
+        GLSU_CUDA_TRY(cudaGraphLaunch(g->exec, b->stream));
+    } else {
+        // eager (also the first step: one-time host work stays out of captures)
+        GLSU_TRY(batch_enqueue(b, active, in, img_type));
+        b->warm = true;
+    }
+    for (size_t i = 0; i < n; i++) {
+        if (!active[i]) continue;
+        glsu_dpra *h = b->h[i];
+        h->synced = false;
+        h->frames_done++;
+        if (h->batch_index++ % h->rr == 0) GLSU_TRY(glsu_dpra_update_ref_phi(h));
+    }
+    return GLSU_OK;
+}
+
+extern "C" int glsu_dpra_batch_sync(glsu_dpra_batch *b)
+{
+    if (!b) return fail(GLSU_ERR_INVALID, "null batch");
+    GLSU_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    for (auto h : b->h) GLSU_TRY(h->wff.check_device_error(h->stream));
+    return GLSU_OK;
+}
+
 extern "C" int glsu_dpra_batch_wait(glsu_dpra *const *handles, int n)
 {
     if (!handles || n < 0) return fail(GLSU_ERR_INVALID, "bad argument");

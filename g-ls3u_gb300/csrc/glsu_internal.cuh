@@ -141,6 +141,12 @@ struct WffPlan {
                 const void *dphi_ref, void *phi_curr, void *dphi, cudaEvent_t *stage_ev);
     // Only the row pass of d_f into the R planes (whole frame, no tile mask).
     int enqueue_rows(cudaStream_t s, const void *d_f);
+    // The stages of enqueue one at a time (whole frame): the threshold and
+    // the row pass; the column sweep (launch_column_sweep); the final row
+    // pass with final_mode as in enqueue.
+    int enqueue_pre(cudaStream_t s, const void *d_f);
+    int enqueue_final(cudaStream_t s, void *d_out, int final_mode, const void *phi_ref, const void *dphi_ref,
+                      void *phi_curr, void *dphi);
     int check_device_error(cudaStream_t s);
 
     // Tile mask of the next enqueue (flags == nullptr: whole frame), and the
@@ -204,6 +210,9 @@ int fft_length_candidates(const WffPlan &P, int *out, int n);
 int launch_column_sweep(WffPlan &P, cudaStream_t s);
 
 int launch_colfft(const WffPlan &P, cudaStream_t s);
+// The FFT column sweep of n plans of one transform length (each running the
+// FFT sweep, no tile mask) as one persistent launch over their work list.
+int launch_colfft_batch(const WffPlan *const *plans, int n, cudaStream_t s);
 // Compact the ncx x ncy tiles (ty_rows x tx_cols outputs each) of a column
 // sweep that a masked run needs into list / *count (device, index order).
 int launch_mask_list(const TileMask &m, int ncx, int ncy, int ty_rows, int tx_cols, int2 *list, int *count,

@@ -161,6 +161,51 @@ int launch_colfft(const WffPlan &P, cudaStream_t s)
     return rc;
 }
 
+// The FFT column sweep of n plans that share one transform length, as one
+// persistent launch (per 128 plans) over their (plan, plane, column group)
+// work list, at the length's default CTA width.  Each column is computed
+// exactly as launch_colfft computes it, so the outputs are the same bits.
+int launch_colfft_batch(const WffPlan *const *plans, int n, cudaStream_t s)
+{
+    if (n <= 0) return GLSU_OK;
+    const int L = plans[0]->fft_L;
+    colfft::LenInfo li;
+    if (!colfft::len_info(L, &li)) return fail(GLSU_ERR_UNSUPPORTED, "no compiled FFT plan for this length");
+    const int nc = li.ncol_default;
+    static thread_local colfft::BatchTable tab;
+    for (int i0 = 0; i0 < n; i0 += colfft::kMaxBatchSeqs) {
+        const int m = std::min(n - i0, colfft::kMaxBatchSeqs);
+        int nitems = 0;
+        for (int k = 0; k < m; k++) {
+            const WffPlan &P = *plans[i0 + k];
+            if (P.fft_L != L || !P.use_colfft() || P.prec != GLSU_F32 || P.pitch % nc != 0)
+                return fail(GLSU_ERR_INVALID, "batched column sweep: plans of one FFT length only");
+            const double N = 1.0 / P.inv_norm;
+            colfft::BatchSeq &q = tab.seq[k];
+            q.R = (const float2 *)P.d_R;
+            q.C = (float2 *)P.d_C;
+            q.khat = (const float2 *)P.d_khat;
+            q.thr = (const float *)P.d_thr;
+            q.H = P.H;
+            q.pitch = P.pitch;
+            q.nfy = P.nfy;
+            q.ngroups = P.pitch / nc;
+            q.LN = (float)(L * N);
+            q.out_scale = (float)(1.0 / ((double)L * L * N));
+            q.item0 = nitems;
+            q.pad_ = 0;
+            nitems += q.ngroups * P.nfx;
+        }
+        const float2 *tw = (const float2 *)plans[i0]->d_tw;
+        int rc = colfft::launch_batch_small(L, tab, m, nitems, tw, 0, s);
+        if (rc == GLSU_ERR_UNSUPPORTED) rc = colfft::launch_batch_mid(L, tab, m, nitems, tw, 0, s);
+        if (rc == GLSU_ERR_UNSUPPORTED) rc = colfft::launch_batch_large(L, tab, m, nitems, tw, 0, s);
+        if (rc == GLSU_ERR_UNSUPPORTED) return fail(GLSU_ERR_UNSUPPORTED, "no compiled FFT plan for this length");
+        GLSU_TRY(rc);
+    }
+    return GLSU_OK;
+}
+
 // ---------------------------------------------------------------------------
 // autotuner
 // ---------------------------------------------------------------------------

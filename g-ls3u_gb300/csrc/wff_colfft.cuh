@@ -28,6 +28,8 @@
 // (__syncwarp, or a named barrier when a column spans several warps).
 #pragma once
 
+#include <algorithm>
+
 #include "glsu_internal.cuh"
 
 namespace glsu {
@@ -249,6 +251,89 @@ template <class P, int NCOL> constexpr int min_ctas()
     return target_warps<P>() / (P::T * NCOL / 32) > 1 ? target_warps<P>() / (P::T * NCOL / 32) : 1;
 }
 
+// Geometry of the columns a CTA sweeps: one plane's input and output, the
+// window spectra, threshold and scale, and the CTA's first column.  It sits
+// in shared memory and is re-read where used, so that none of it occupies
+// registers across the transforms (the batched kernel below takes it from a
+// table with a run-time index; kept in registers it would spill).
+struct SweepGeom {
+    const float2 *R;
+    float2 *C;
+    const float2 *khat;
+    float thr2, out_scale;
+    int H, pitch, nfy, x0;
+};
+template <typename T> __device__ __forceinline__ T vld(const T &r) { return *(const volatile T *)&r; }
+
+// The 2 nfy + 2 transforms of column x0 + col of one plane, run by the T
+// threads (t) of column slot col through a single transform body.  Both
+// kernels below run every column through this function, so a column's
+// outputs are the same bits whichever kernel ran it.
+template <class P>
+__device__ __forceinline__ void sweep_column(const SweepGeom &g, const float2 *__restrict__ tw,
+                                             float2 *__restrict__ xb, float2 *__restrict__ S, int t, int col)
+{
+    constexpr int L = P::L, T = P::T, Q = P::Q;
+    const int nit = 2 * vld(g.nfy) + 2;
+    float2 v[Q], ch[Q];
+#pragma unroll 1
+    for (int it = 0; it < nit; it++) {
+        const int k = (it - 1) >> 1;  // wy index of the inverse (odd it) / forward (even it >= 2) pair
+        if (it == 0) {
+            const float2 *Ri = vld(g.R);
+            const int H = vld(g.H), pitch = vld(g.pitch), x = vld(g.x0) + col;
+#pragma unroll
+            for (int m = 0; m < Q; m++) {
+                const int row = t + T * m;
+                v[m] = row < H ? Ri[(size_t)row * pitch + x] : make_float2(0.f, 0.f);
+            }
+        } else if (it == nit - 1) {
+#pragma unroll
+            for (int m = 0; m < Q; m++) v[m] = conjf2(ch[m]);
+        } else if (it & 1) {
+            const float2 *hk = vld(g.khat) + (size_t)k * L;
+#pragma unroll
+            for (int m = 0; m < Q; m++) v[m] = conjf2(cmul(S[t + T * m], __ldg(hk + t + T * m)));
+        }
+        fft<P>(v, xb, tw, t, col);
+        if (it == 0) {
+#pragma unroll
+            for (int m = 0; m < Q; m++) {
+                S[t + T * m] = v[m];  // read back only by this thread
+                ch[m] = make_float2(0.f, 0.f);
+            }
+        } else if (it == nit - 1) {
+            float2 *Ci = vld(g.C);
+            const int H = vld(g.H), pitch = vld(g.pitch), x = vld(g.x0) + col;
+            const float out_scale = vld(g.out_scale);
+#pragma unroll
+            for (int m = 0; m < Q; m++) {
+                const int row = t + T * m;
+                if (row < H) Ci[(size_t)row * pitch + x] = make_float2(v[m].x * out_scale, -v[m].y * out_scale);
+            }
+        } else if (it & 1) {
+            // u = conj(v): hard threshold in the spatial domain, rows >= H dropped
+            const int H = vld(g.H);
+            const float thr2 = vld(g.thr2);
+#pragma unroll
+            for (int m = 0; m < Q; m++) {
+                const int row = t + T * m;
+                const float2 u = conjf2(v[m]);
+                const bool keep = row < H && (u.x * u.x + u.y * u.y >= thr2);
+                v[m] = keep ? u : make_float2(0.f, 0.f);
+            }
+        } else {
+            const float2 *hk = vld(g.khat) + (size_t)k * L;
+#pragma unroll
+            for (int m = 0; m < Q; m++) {
+                const float2 a = v[m], h = __ldg(hk + t + T * m);
+                ch[m].x += a.x * h.x - a.y * h.y;
+                ch[m].y += a.x * h.y + a.y * h.x;
+            }
+        }
+    }
+}
+
 template <class P, int NCOL>
 __global__ void __launch_bounds__(P::T *NCOL, (min_ctas<P, NCOL>())) wff_colfft_kernel(const float2 *__restrict__ R, float2 *__restrict__ Cout,
                                                                int H, int pitch, int nfy,
@@ -258,70 +343,79 @@ __global__ void __launch_bounds__(P::T *NCOL, (min_ctas<P, NCOL>())) wff_colfft_
                                                                float out_scale, const int2 *__restrict__ list,
                                                                const int *__restrict__ list_count)
 {
-    constexpr int L = P::L, T = P::T, Q = P::Q;
+    constexpr int L = P::L, T = P::T;
     extern __shared__ __align__(16) float2 cf_smem[];
+    __shared__ SweepGeom geom;
     const int col = threadIdx.x / T, t = threadIdx.x % T;
     float2 *xb = cf_smem + (size_t)col * (P::XBUF + L);
     float2 *S = xb + P::XBUF;
-    const size_t plane = (size_t)H * pitch;
-    const float2 *Ri = R + blockIdx.y * plane;
-    float2 *Ci = Cout + blockIdx.y * plane;
-    const float thr = LN * (*thr_ptr);
-    const float thr2 = thr * thr;
     const int nitems = list ? *list_count : (int)gridDim.x;
-    const int nit = 2 * nfy + 2;
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int x = (list ? list[item].x : item) * NCOL + col;
-        float2 v[Q], ch[Q];
-#pragma unroll 1
-        for (int it = 0; it < nit; it++) {
-            const int k = (it - 1) >> 1;  // wy index of the inverse (odd it) / forward (even it >= 2) pair
-            if (it == 0) {
-#pragma unroll
-                for (int m = 0; m < Q; m++) {
-                    const int row = t + T * m;
-                    v[m] = row < H ? Ri[(size_t)row * pitch + x] : make_float2(0.f, 0.f);
-                }
-            } else if (it == nit - 1) {
-#pragma unroll
-                for (int m = 0; m < Q; m++) v[m] = conjf2(ch[m]);
-            } else if (it & 1) {
-                const float2 *hk = khat + (size_t)k * L;
-#pragma unroll
-                for (int m = 0; m < Q; m++) v[m] = conjf2(cmul(S[t + T * m], __ldg(hk + t + T * m)));
-            }
-            fft<P>(v, xb, tw, t, col);
-            if (it == 0) {
-#pragma unroll
-                for (int m = 0; m < Q; m++) {
-                    S[t + T * m] = v[m];  // read back only by this thread
-                    ch[m] = make_float2(0.f, 0.f);
-                }
-            } else if (it == nit - 1) {
-#pragma unroll
-                for (int m = 0; m < Q; m++) {
-                    const int row = t + T * m;
-                    if (row < H) Ci[(size_t)row * pitch + x] = make_float2(v[m].x * out_scale, -v[m].y * out_scale);
-                }
-            } else if (it & 1) {
-                // u = conj(v): hard threshold in the spatial domain, rows >= H dropped
-#pragma unroll
-                for (int m = 0; m < Q; m++) {
-                    const int row = t + T * m;
-                    const float2 u = conjf2(v[m]);
-                    const bool keep = row < H && (u.x * u.x + u.y * u.y >= thr2);
-                    v[m] = keep ? u : make_float2(0.f, 0.f);
-                }
-            } else {
-                const float2 *hk = khat + (size_t)k * L;
-#pragma unroll
-                for (int m = 0; m < Q; m++) {
-                    const float2 a = v[m], h = __ldg(hk + t + T * m);
-                    ch[m].x += a.x * h.x - a.y * h.y;
-                    ch[m].y += a.x * h.y + a.y * h.x;
-                }
-            }
+        __syncthreads();  // every column is done with the previous item's geometry
+        if (threadIdx.x == 0) {
+            const size_t plane = (size_t)H * pitch;
+            const float thr = LN * (*thr_ptr);
+            geom = SweepGeom{R + blockIdx.y * plane, Cout + blockIdx.y * plane, khat, thr * thr, out_scale,
+                             H, pitch, nfy, (list ? list[item].x : item) * NCOL};
         }
+        __syncthreads();
+        sweep_column<P>(geom, tw, xb, S, t, col);
+    }
+}
+
+// One sequence of a batched column sweep (glsu_dpra_batch): its planes, its
+// window spectra and threshold, and where its items start in the batch's
+// work list.  Sequence s owns items item0[s] .. item0[s+1] - 1, item
+// (plane i, column group g) = item0 + i * ngroups + g.  The table travels
+// as a kernel parameter (constant bank).
+constexpr int kMaxBatchSeqs = 128;
+struct BatchSeq {
+    const float2 *R;
+    float2 *C;
+    const float2 *khat;
+    const float *thr;
+    int H, pitch, nfy, ngroups;
+    float LN, out_scale;
+    int item0;
+    int pad_;
+};
+struct BatchTable {
+    BatchSeq seq[kMaxBatchSeqs];
+};
+
+// The column sweep of many sequences of one transform length in one
+// persistent launch: each CTA walks the batch's work list of (sequence,
+// plane, column group) items with stride gridDim.x.
+template <class P, int NCOL>
+__global__ void __launch_bounds__(P::T *NCOL, (min_ctas<P, NCOL>()))
+    wff_colfft_batch_kernel(const __grid_constant__ BatchTable tab, int nseq, int nitems,
+                            const float2 *__restrict__ tw)
+{
+    constexpr int L = P::L, T = P::T;
+    extern __shared__ __align__(16) float2 cf_smem[];
+    __shared__ SweepGeom geom;
+    const int col = threadIdx.x / T, t = threadIdx.x % T;
+    float2 *xb = cf_smem + (size_t)col * (P::XBUF + L);
+    float2 *S = xb + P::XBUF;
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        __syncthreads();  // every column is done with the previous item's geometry
+        if (threadIdx.x == 0) {
+            int lo = 0, hi = nseq - 1;  // the last sequence with item0 <= item
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (tab.seq[mid].item0 <= item) lo = mid;
+                else hi = mid - 1;
+            }
+            const BatchSeq &q = tab.seq[lo];
+            const int local = item - q.item0;
+            const int i = local / q.ngroups, g = local - i * q.ngroups;
+            const size_t plane = (size_t)q.H * q.pitch;
+            const float thr = q.LN * (*q.thr);
+            geom = SweepGeom{q.R + i * plane, q.C + i * plane, q.khat, thr * thr, q.out_scale, q.H, q.pitch, q.nfy,
+                             g * NCOL};
+        }
+        __syncthreads();
+        sweep_column<P>(geom, tw, xb, S, t, col);
     }
 }
 
@@ -352,6 +446,25 @@ int launch(const WffPlan &Pl, cudaStream_t s, const int2 *list, const int *count
     return GLSU_OK;
 }
 
+// Launch the batched sweep of plan P (default CTA width NCOL) over nitems
+// items of nseq sequences (device array seqs), grid_x persistent CTAs.
+template <class P, int NCOL>
+int launch_batch(const BatchTable &tab, int nseq, int nitems, const float2 *tw, int grid_x, cudaStream_t s)
+{
+    const size_t smem = NCOL * smem_per_column<P>();
+    GLSU_TRY(raise_smem_limit((const void *)wff_colfft_batch_kernel<P, NCOL>, (int)smem));
+    if (grid_x <= 0) {  // persistent: as many CTAs as are resident at once
+        int per_sm = 0;
+        GLSU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wff_colfft_batch_kernel<P, NCOL>,
+                                                                    P::T * NCOL, smem));
+        grid_x = std::max(1, per_sm) * device_sm_count();
+    }
+    grid_x = std::max(1, std::min(grid_x, nitems));
+    wff_colfft_batch_kernel<P, NCOL><<<grid_x, P::T * NCOL, smem, s>>>(tab, nseq, nitems, tw);
+    GLSU_CUDA_TRY(cudaGetLastError());
+    return GLSU_OK;
+}
+
 // Per transform length: its plan, and the two CTA widths compiled for it
 // (the default first).  Each length group lives in its own translation unit
 // so that they compile in parallel; each returns GLSU_ERR_UNSUPPORTED for
@@ -362,6 +475,13 @@ int launch_len_mid(int L, int ncol, const WffPlan &Pl, cudaStream_t s, const int
                    int grid_x);
 int launch_len_large(int L, int ncol, const WffPlan &Pl, cudaStream_t s, const int2 *list, const int *count,
                      int grid_x);
+// The batched sweep at the length's default CTA width (same grouping).
+int launch_batch_small(int L, const BatchTable &tab, int nseq, int nitems, const float2 *tw, int grid_x,
+                       cudaStream_t s);
+int launch_batch_mid(int L, const BatchTable &tab, int nseq, int nitems, const float2 *tw, int grid_x,
+                     cudaStream_t s);
+int launch_batch_large(int L, const BatchTable &tab, int nseq, int nitems, const float2 *tw, int grid_x,
+                       cudaStream_t s);
 
 // Threads per column, passes and shared memory per column of each length
 // (host-side mirror of the plans).
@@ -373,6 +493,10 @@ bool len_info(int L, LenInfo *out);
 
 }  // namespace colfft
 }  // namespace glsu
+
+#define GLSU_COLFFT_BATCH_CASE(LEN, PLAN, NC0) \
+    case LEN:                                   \
+        return launch_batch<PLAN, NC0>(tab, nseq, nitems, tw, grid_x, s);
 
 #define GLSU_COLFFT_CASE(LEN, PLAN, NC0)                                                            \
     case LEN: {                                                                                     \

@@ -12,5 +12,13 @@ int launch_len_mid(int L, int ncol, const WffPlan &Pl, cudaStream_t s, const int
     default: return GLSU_ERR_UNSUPPORTED;
     }
 }
+int launch_batch_mid(int L, const BatchTable &tab, int nseq, int nitems, const float2 *tw, int grid_x, cudaStream_t s)
+{
+    switch (L) {
+        GLSU_COLFFT_BATCH_CASE(1024, P1024, 4)
+        GLSU_COLFFT_BATCH_CASE(1280, P1280, 4)
+    default: return GLSU_ERR_UNSUPPORTED;
+    }
+}
 }  // namespace colfft
 }  // namespace glsu

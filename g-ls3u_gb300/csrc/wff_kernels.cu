@@ -829,6 +829,53 @@ static int enqueue_t(WffPlan &P, cudaStream_t s, const void *d_f, void *d_out, i
     return GLSU_OK;
 }
 
+// The same three stages one at a time (the batched form interleaves them
+// across sequences): threshold + row pass, column sweep, final row pass.
+template <typename T> static int enqueue_pre_t(WffPlan &P, cudaStream_t s, const void *d_f)
+{
+    GLSU_TRY(P.ensure_threshold(s, d_f));
+    switch (P.sxi) {
+    case 12: return launch_rows_demod<T, 12>(P, d_f, s);
+    case 20: return launch_rows_demod<T, 20>(P, d_f, s);
+    case 30: return launch_rows_demod<T, 30>(P, d_f, s);
+    case 45: return launch_rows_demod<T, 45>(P, d_f, s);
+    default: return launch_rows_demod<T, 60>(P, d_f, s);
+    }
+}
+
+#define GLSU_FINAL(SS)                                                                              \
+    rc = mode == 0   ? launch_final<T, SS, 0>(P, d_out, phiref, dphiref, phicurr, dphi, s)          \
+         : mode == 1 ? launch_final<T, SS, 1>(P, d_out, phiref, dphiref, phicurr, dphi, s)          \
+                     : launch_final<T, SS, 2>(P, d_out, phiref, dphiref, phicurr, dphi, s);
+template <typename T>
+static int enqueue_final_t(WffPlan &P, cudaStream_t s, void *d_out, int mode, const void *phiref,
+                           const void *dphiref, void *phicurr, void *dphi)
+{
+    int rc = GLSU_OK;
+    switch (P.sxi) {
+    case 12: GLSU_FINAL(12) break;
+    case 20: GLSU_FINAL(20) break;
+    case 30: GLSU_FINAL(30) break;
+    case 45: GLSU_FINAL(45) break;
+    default: GLSU_FINAL(60) break;
+    }
+    return rc;
+}
+#undef GLSU_FINAL
+
+int WffPlan::enqueue_pre(cudaStream_t s, const void *d_f)
+{
+    if (mask.flags) return fail(GLSU_ERR_INVALID, "staged WFF2 with a tile mask set");
+    return prec == GLSU_F32 ? enqueue_pre_t<float>(*this, s, d_f) : enqueue_pre_t<double>(*this, s, d_f);
+}
+
+int WffPlan::enqueue_final(cudaStream_t s, void *d_out, int final_mode, const void *phi_ref, const void *dphi_ref,
+                           void *phi_curr, void *dphi)
+{
+    return prec == GLSU_F32 ? enqueue_final_t<float>(*this, s, d_out, final_mode, phi_ref, dphi_ref, phi_curr, dphi)
+                            : enqueue_final_t<double>(*this, s, d_out, final_mode, phi_ref, dphi_ref, phi_curr, dphi);
+}
+
 int WffPlan::ensure_threshold(cudaStream_t s, const void *d_f)
 {
     if (p.thr >= 0 || thr_ready) return GLSU_OK;

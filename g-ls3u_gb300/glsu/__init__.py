@@ -187,6 +187,11 @@ def lib() -> ctypes.CDLL:
             "glsu_dpra_lsq_device": ([c_void_p, c_void_p], c_int),
             "glsu_dpra_set_ls_method": ([c_void_p, c_int], c_int),
             "glsu_dpra_set_ls_tile": ([c_void_p, c_int, c_int], c_int),
+            "glsu_dpra_batch_create": ([pp, c_void_p, c_int], c_int),
+            "glsu_dpra_batch_destroy": ([c_void_p], c_int),
+            "glsu_dpra_batch_set_graph": ([c_void_p, c_int], c_int),
+            "glsu_dpra_batch_run": ([c_void_p, c_void_p, c_int], c_int),
+            "glsu_dpra_batch_sync": ([c_void_p], c_int),
             "glsu_dpra_get_ls_tile": ([c_void_p, intp, intp], c_int),
             "glsu_dpra_tune_ls_tile": ([c_void_p, fltp], c_int),
         }
@@ -547,6 +552,34 @@ def dpra_batch_step(handles, d_frames, img_type: int):
     waiting: call dpra_batch_wait."""
     fs = (ctypes.c_void_p * len(handles))(*[f or None for f in d_frames])
     check(lib().glsu_dpra_batch_step(_handle_array(handles), len(handles), fs, img_type))
+
+
+class DpraBatch:
+    """Staged batch of FP32 plain-form DPRA handles (glsu_dpra_batch_*): one
+    frame of each active sequence per step, the FFT column sweeps of all
+    sequences of a transform length in one persistent launch."""
+
+    def __init__(self, handles, graph: bool = False):
+        self._handles = list(handles)
+        arr = _handle_array(self._handles)
+        h = ctypes.c_void_p()
+        check(lib().glsu_dpra_batch_create(ctypes.byref(h), arr, len(self._handles)))
+        self._h = h
+        if graph:
+            check(lib().glsu_dpra_batch_set_graph(self._h, 1))
+
+    def close(self):
+        if self._h:
+            lib().glsu_dpra_batch_destroy(self._h)
+            self._h = None
+
+    def run(self, d_frames, img_type: int):
+        """d_frames: one device pointer (or 0 / None for an ended sequence) per handle."""
+        arr = (ctypes.c_void_p * len(d_frames))(*[p or None for p in d_frames])
+        check(lib().glsu_dpra_batch_run(self._h, arr, img_type))
+
+    def sync(self):
+        check(lib().glsu_dpra_batch_sync(self._h))
 
 
 def dpra_batch_wait(handles):

@@ -257,6 +257,31 @@ int glsu_dpra_update_ref_phi(glsu_dpra *h);
  * handles before i have already taken their frame of this step. */
 int glsu_dpra_batch_step(glsu_dpra *const *handles, int n, const void *const *d_frames, int img_type);
 int glsu_dpra_batch_wait(glsu_dpra *const *handles, int n);
+/* Staged batch (no counterpart in the reference): many FP32 plain-form DPRA
+ * handles (any sizes, windows and WFF parameters; at most 128 per transform
+ * length and launch, more are split) run one frame each per step, stage by
+ * stage: per sequence on its own stream the least squares and the WFF2 row
+ * pass; then the FFT column sweeps of all sequences that share a transform
+ * length as one persistent launch over their (sequence, plane, column group)
+ * work list, one launch per length, the lengths on parallel streams
+ * (sequences on the direct sweep run it on their own stream); then per
+ * sequence the final row pass and the phase update.  Outputs equal each
+ * handle's own frames bit for bit.  Each handle follows the sequence rule
+ * (after its i-th batched frame the reference is updated when i % rr == 0).
+ * glsu_dpra_batch_run returns after enqueueing on the batch's stream;
+ * d_frames[i] is handle i's device frame (U8 or F32) or NULL when its
+ * sequence has ended.  In graph mode (glsu_dpra_batch_set_graph) each step
+ * after the first is one CUDA graph launch (one graph per set of active
+ * sequences and reference parities, inputs first copied into the handles'
+ * frame buffers).  The handles must outlive the batch and are not used
+ * elsewhere while it runs. */
+typedef struct glsu_dpra_batch glsu_dpra_batch;
+int glsu_dpra_batch_create(glsu_dpra_batch **out, glsu_dpra *const *handles, int n);
+int glsu_dpra_batch_destroy(glsu_dpra_batch *b);
+int glsu_dpra_batch_set_graph(glsu_dpra_batch *b, int enable);
+int glsu_dpra_batch_run(glsu_dpra_batch *b, const void *const *d_frames, int img_type);
+/* Waits for the batch's steps and reports device errors. */
+int glsu_dpra_batch_sync(glsu_dpra_batch *b);
 /* DPRA_CPU::operator() semantics for a block of frames: for frame i, run
  * per_frame, store its dphi, update the reference when i % rr == 0
  * (DPRA/dpra_cpu.cpp:58-89; the CUDA reference's overloads are empty,

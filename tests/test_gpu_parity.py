@@ -596,6 +596,57 @@ def test_batched_uneven_sequences_equal_sequential(glsu, synth, graph):
             h.close()
 
 
+@pytest.mark.parametrize("graph", [False, True])
+def test_staged_batch_equals_sequential(glsu, synth, graph):
+    """The staged batch (glsu_dpra_batch_*): sequences of uneven sizes,
+    window radii 2..4, reference rates 1..3, WFF parameters with different
+    column sweeps (FFT sweeps of three transform lengths batched per length,
+    and a narrow window on the direct sweep), ended sequences passing no
+    frame: every sequence's phases bit for bit as its own glsu_dpra_sequence
+    gives them; FP32, u8 and f32 frames."""
+    torch = _torch()
+    w21 = glsu.WffParams(10.0, -1.0, 1.0, 0.1, 10.0, -1.0, 1.0, 0.1, 0.2)   # FFT sweep (model)
+    w11 = glsu.WffParams(10.0, -1.0, 1.0, 0.2, 10.0, -1.0, 1.0, 0.2, 0.2)   # direct sweep at 96x80
+    w4 = glsu.WffParams(4.0, -1.0, 1.0, 0.25, 4.0, -1.0, 1.0, 0.25, 0.3)    # direct sweep
+    specs = [((128, 128), 2, 1, 5, w21), ((96, 80), 3, 2, 3, w11), ((256, 256), 4, 3, 6, w21),
+             ((128, 128), 3, 1, 4, w21), ((384, 512), 2, 1, 3, w21), ((64, 80), 3, 2, 4, w4)]
+    for img in ("u8", "f32"):
+        seqs, handles, ref, methods = [], [], [], []
+        for k, ((H, W), r, rr, nf, wp) in enumerate(specs):
+            frames, phi0, _ = synth.sequence(H, W, nf, seed=70 + k)
+            fr = np.clip(np.round(frames * 255), 0, 255).astype(np.uint8) if img == "u8" else frames
+            d = glsu.DPRA(phi0.astype(np.float32), rr, r, "f32", wp)
+            out, _ = d.sequence(fr)
+            ref.append((out, d.get(glsu.PHI_REF).copy()))
+            d.close()
+            d = glsu.DPRA(phi0.astype(np.float32), rr, r, "f32", wp)
+            methods.append((d.tuning()["method"], d.tuning()["fft_length"]))
+            handles.append(d)
+            seqs.append(torch.from_numpy(fr).cuda())
+        assert {m for m, _ in methods} == {glsu.METHOD_FFT, glsu.METHOD_DIRECT}, methods
+        assert len({L for m, L in methods if m == glsu.METHOD_FFT}) >= 2, methods
+        b = glsu.DpraBatch(handles, graph=graph)
+        dphi = [[] for _ in specs]
+        for step in range(max(s[3] for s in specs)):
+            ptrs = [seqs[k][step].data_ptr() if step < specs[k][3] else None for k in range(len(specs))]
+            b.run(ptrs, glsu.U8 if img == "u8" else glsu.F32)
+            b.sync()
+            for k in range(len(specs)):
+                if step < specs[k][3]:
+                    dphi[k].append(handles[k].get(glsu.DPHI).copy())
+        b.close()
+        for k, d in enumerate(handles):
+            assert np.array_equal(np.stack(dphi[k]), ref[k][0]), (img, k, methods[k])
+            assert np.array_equal(d.get(glsu.PHI_REF), ref[k][1]), (img, k)
+            d.close()
+    print("methods (sweep, length):", methods)
+    h = glsu.DPRA(np.zeros((16, 16)), 1, 1, "f64", w4)
+    with pytest.raises(glsu.GlsuError) as e:
+        glsu.DpraBatch([h])
+    assert e.value.code == glsu.ERR_UNSUPPORTED
+    h.close()
+
+
 def test_aia_reference_bmp_frames(glsu, oracle):
     """AIA on the reference's own test frames Test/{1,2,3}.bmp with the
     deltas of its tests (uint8 path, as AIA_CUDAF receives cv::Mat CV_8UC1)."""
