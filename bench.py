@@ -545,18 +545,24 @@ def precision_form(glsu, torch, seed, size=SIZE, nframes=200, every=20):
 CONFIG4 = dict(size=2048, radius=4, wff=(15.0, -1.5, 1.5, 0.1, 15.0, -1.5, 1.5, 0.1, 0.2), noise=0.05, n_gauss=8)
 
 
-def large_workload(glsu, torch, seed, nframes=12, warm=2, fp64_frames=(6, 12)):
-    """The large streaming workload (2048^2, 8 Gaussians, noise 0.05, DPRA
-    9x9, WFF2 sigma 15 with 31 x 31 frequencies on [-1.5, 1.5]), plain FP32
-    form in graph mode: device frames/s over `nframes` frames after `warm`,
-    the column sweep's share, HBM throughput figures, and the FP64 check on
-    sampled frames."""
+SIGMA15_WEIGHTS = os.path.join(PKG, "glsu", "surrogate_sigma15.npz")
+
+
+def _large_run(glsu, torch, seed, form, nframes, warm, fp64_frames):
+    """One form of the large workload (plain, or the surrogate with the
+    sigma-15 network): device time per frame over `nframes` frames after
+    `warm`, graph mode, stage split of one further eager frame, and the
+    FP64 check of the sampled frames."""
     from glsu import synth
+    from glsu import train_surrogate as TS
     c = CONFIG4
     size, wp = c["size"], glsu.WffParams(*c["wff"])
     seq = synth.DeviceSequence(size, size, seed=seed, noise=c["noise"], n_gauss=c["n_gauss"])
     d = glsu.DPRA(seq.phi0.astype(np.float32), 1, c["radius"], "f32", wp)
     tu = d.tuning()
+    if form == "surrogate":
+        params, dil = TS.load(SIGMA15_WEIGHTS)
+        d.set_surrogate(params, dil, SUR_TILE, 0, SUR_TOL)
     st = torch.cuda.Stream()
     d.set_stream(st.cuda_stream)
     d.set_graph(True)
@@ -581,30 +587,56 @@ def large_workload(glsu, torch, seed, nframes=12, warm=2, fp64_frames=(6, 12)):
     d.stage_timing(True)
     buf.copy_(seq.frame(warm + nframes + 1))
     d.per_frame_device(buf.data_ptr(), glsu.F32)
-    st = d.stage_times()
+    stg = d.stage_times()
+    stats = d.surrogate_stats() if form == "surrogate" else None
     d.close()
+    mean_ms = float(np.mean(ms))
+    out = {"frames_per_s": 1e3 / mean_ms, "ms_per_frame": mean_ms, "frames_timed": nframes,
+           "fp64_samples": [{"frame": k, "rmse": r, "max": m} for k, r, m in errs],
+           "rmse_vs_fp64": float(np.sqrt(np.mean([r * r for _, r, _ in errs]))) if errs else None,
+           "max_abs_vs_fp64": max(m for _, _, m in errs) if errs else None}
+    if form == "plain":
+        out["stages_ms"] = {"dpra_ls": stg[0], "wff_rows": stg[1], "wff_column_sweep": stg[2],
+                            "wff_final_update": stg[3]}
+        out["column_sweep"] = tu
+    else:
+        out["stages_ms"] = {"dpra_ls": stg[0], "network": stg[1], "wff2_probe_and_residuals": stg[2],
+                            "fallback_and_update": stg[3], "wff2_probe_sweep": stg[7]}
+        out["tiles_probed_recomputed"] = list(stats)
+    return out
+
+
+def large_workload(glsu, torch, seed, nframes=12, warm=2, fp64_frames=(6, 12)):
+    """The large streaming workload (2048^2, 8 Gaussians, noise 0.05, DPRA
+    9x9, WFF2 sigma 15 with 31 x 31 frequencies on [-1.5, 1.5]): the plain
+    FP32 form and, with the sigma-15 network (glsu/surrogate_sigma15.npz),
+    the surrogate form, on the same sequence in graph mode; frames/s, stage
+    split, HBM figures and the FP64 check on sampled frames."""
+    c = CONFIG4
+    size = c["size"]
+    plain = _large_run(glsu, torch, seed, "plain", nframes, warm, fp64_frames)
     s = int(np.floor(3 * c["wff"][0] + 0.5))
     nfx = glsu.wff_count(c["wff"][1], c["wff"][2], c["wff"][3], glsu.F32)
     P = fft_padded(size + 2 * s) ** 2
     fft_bytes = (64 * nfx * nfx + 32) * P
     pitch = (size + 127) // 128 * 128
     col_bytes = 2 * nfx * size * pitch * 8
-    mean_ms = float(np.mean(ms))
-    return {
-        "workload": "2048x2048 FP32, 8 Gaussians, noise 0.05, DPRA 9x9, WFF2 sigma 15, xi in [-1.5, 1.5] step "
-                    "0.1 (%dx%d frequencies), thr 0.2, plain form, graph mode" % (nfx, nfx),
-        "frames_per_s": 1e3 / mean_ms, "ms_per_frame": mean_ms, "frames_timed": nframes,
-        "stages_ms": {"dpra_ls": st[0], "wff_rows": st[1], "wff_column_sweep": st[2], "wff_final_update": st[3]},
-        "column_sweep": tu,
-        "hbm": {"compulsory_gb_per_s": col_bytes / (st[2] * 1e-3) / 1e9,
-                "fft_model_bytes_per_frame": fft_bytes, "fft_model_gb_per_s": fft_bytes / (mean_ms * 1e-3) / 1e9,
-                "what": "compulsory: the column sweep's R-plane read and C-plane write over its time; fft_model: "
-                        "frame throughput x the FFT formulation's algorithmic bytes per frame ((64 n_freq + 32) P, "
-                        "P = %d^2)" % int(P ** 0.5)},
-        "fp64_samples": [{"frame": k, "rmse": r, "max": m} for k, r, m in errs],
-        "rmse_vs_fp64": float(np.sqrt(np.mean([r * r for _, r, _ in errs]))) if errs else None,
-        "max_abs_vs_fp64": max(m for _, _, m in errs) if errs else None,
-    }
+    plain["hbm"] = {"compulsory_gb_per_s": col_bytes / (plain["stages_ms"]["wff_column_sweep"] * 1e-3) / 1e9,
+                    "fft_model_bytes_per_frame": fft_bytes,
+                    "fft_model_gb_per_s": fft_bytes / (plain["ms_per_frame"] * 1e-3) / 1e9,
+                    "what": "compulsory: the column sweep's R-plane read and C-plane write over its time; "
+                            "fft_model: frame throughput x the FFT formulation's algorithmic bytes per frame "
+                            "((64 n_freq + 32) P, P = %d^2)" % int(P ** 0.5)}
+    out = {"workload": "2048x2048 FP32, 8 Gaussians, noise 0.05, DPRA 9x9, WFF2 sigma 15, xi in [-1.5, 1.5] step "
+                       "0.1 (%dx%d frequencies), thr 0.2, graph mode" % (nfx, nfx),
+           "plain": plain}
+    if os.path.exists(SIGMA15_WEIGHTS):
+        sur = _large_run(glsu, torch, seed, "surrogate", nframes, warm, fp64_frames)
+        out["surrogate"] = sur
+        out["speedup_surrogate_vs_plain"] = sur["frames_per_s"] / plain["frames_per_s"]
+    else:
+        out["surrogate"] = {"unavailable": "no sigma-15 weights (glsu/surrogate_sigma15.npz)"}
+    return out
 
 
 BATCH_SIZES = ((256, 256), (384, 512), (1024, 1024), (1536, 2048))  # (H, W) of the batched form's mix
@@ -667,6 +699,84 @@ def batched_measure(glsu, torch, seed, sizes=BATCH_SIZES, per_size=2, nframes=4)
             "batched_ms": ms_b, "sequential_ms": ms_s, "frames": nf, "megapixels": px / 1e6,
             "batched_frames_per_s": nf / (ms_b * 1e-3), "batched_mpixels_per_s": px / 1e6 / (ms_b * 1e-3),
             "speedup_vs_sequential": ms_s / ms_b}
+
+
+MIX_SIZES = ((256, 256), (384, 512), (1024, 1024), (1536, 2048))  # (H, W), 16 sequences each
+
+
+def batched_mix(glsu, torch, seed, per_size=16, fmin=10, fmax=100):
+    """The batched form at its full mix: 16 sequences each of 256^2,
+    512x384, 1024^2 and 1536x2048 (W x H), frame counts U[fmin, fmax],
+    DPRA windows 5, 7 or 9, WFF2 with 21 x 21 frequencies, FP32, frames of
+    each sequence's own seeded generator (made on the GPU before each step,
+    outside the timing).  The staged batch (glsu_dpra_batch_*, graph mode:
+    the FFT column sweeps of all sequences of a transform length in one
+    persistent launch) against the same sequences run one after another
+    (graph-mode handles, one frame at a time); device time per step bracketed
+    by synchronisation, summed over the steps.  The two runs' final phases
+    are compared bit for bit."""
+    from glsu import synth
+    rng = np.random.default_rng(seed + 77)
+    wp = glsu.WffParams(*WFF)
+    specs = []
+    for (H, W) in MIX_SIZES:
+        for k in range(per_size):
+            specs.append((H, W, int(rng.integers(fmin, fmax + 1)), int(rng.choice([2, 3, 4])),
+                          seed * 1000 + len(specs)))
+    nsteps = max(sp[2] for sp in specs)
+    frames_total = sum(sp[2] for sp in specs)
+    px_total = sum(sp[0] * sp[1] * sp[2] for sp in specs)
+
+    def make():
+        seqs, hs = [], []
+        for (H, W, nf, r, sd) in specs:
+            q = synth.DeviceSequence(H, W, seed=sd)
+            d = glsu.DPRA(q.phi0.astype(np.float32), 1, r, "f32", wp)
+            d.set_graph(True)
+            seqs.append(q)
+            hs.append(d)
+        return seqs, hs
+
+    def run(batched):
+        seqs, hs = make()
+        bufs = [torch.empty((H, W), dtype=torch.float32, device="cuda") for (H, W, _, _, _) in specs]
+        b = glsu.DpraBatch(hs, graph=True) if batched else None
+        total = 0.0
+        for step in range(nsteps):
+            act = [step < sp[2] for sp in specs]
+            for k, q in enumerate(seqs):
+                if act[k]:
+                    bufs[k].copy_(q.frame(step + 1))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if batched:
+                b.run([bufs[k].data_ptr() if act[k] else None for k in range(len(specs))], glsu.F32)
+                b.sync()
+            else:
+                for k, d in enumerate(hs):
+                    if act[k]:
+                        d.per_frame_device(bufs[k].data_ptr(), glsu.F32)
+                        d.update_ref_phi()
+                        torch.cuda.synchronize()
+            total += time.perf_counter() - t0
+        phases = [d.get(glsu.PHI_REF) for d in hs]
+        if b is not None:
+            b.close()
+        for d in hs:
+            d.close()
+        return total, phases
+
+    t_b, ph_b = run(True)
+    t_s, ph_s = run(False)
+    same = all(np.array_equal(a, c) for a, c in zip(ph_b, ph_s))
+    return {"workload": "64 sequences: 16 each of 256x256, 512x384, 1024x1024, 2048x1536 (W x H), frame counts "
+                        "U[%d, %d] (%d frames, %.0f megapixels in all), DPRA windows 5/7/9, WFF2 21x21 "
+                        "frequencies, FP32; staged batch in graph mode against the same sequences one after "
+                        "another" % (fmin, fmax, frames_total, px_total / 1e6),
+            "batched_s": t_b, "sequential_s": t_s, "steps": nsteps, "frames": frames_total,
+            "batched_frames_per_s": frames_total / t_b, "sequential_frames_per_s": frames_total / t_s,
+            "batched_mpixels_per_s": px_total / 1e6 / t_b, "speedup_vs_sequential": t_s / t_b,
+            "outputs_identical": bool(same)}
 
 
 def plain_accuracy(glsu, torch, dfr, phi0, wp, nframes):
@@ -749,8 +859,10 @@ def run_ours(args, rank, world, local):
     wfr = batched = prec1 = large = None
     if extras:
         wfr = wfr_measure(glsu, torch, phi0, size, seed)
-        batched = {"uneven_sizes": batched_measure(glsu, torch, seed),
-                   "small_frames": batched_measure(glsu, torch, seed, sizes=((256, 256),), per_size=16, nframes=8)}
+        batched = {"config_mix": batched_mix(glsu, torch, seed),
+                   "streams_uneven_sizes": batched_measure(glsu, torch, seed),
+                   "streams_small_frames": batched_measure(glsu, torch, seed, sizes=((256, 256),), per_size=16,
+                                                           nframes=8)}
         prec1 = precision_form(glsu, torch, seed, size)
         large = large_workload(glsu, torch, seed)
 
