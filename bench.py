@@ -543,6 +543,11 @@ def precision_form(glsu, torch, seed, size=SIZE, nframes=200, every=20):
 
 
 CONFIG4 = dict(size=2048, radius=4, wff=(15.0, -1.5, 1.5, 0.1, 15.0, -1.5, 1.5, 0.1, 0.2), noise=0.05, n_gauss=8)
+# Surrogate tiles of the large workload: 512^2.  An exact probe patch at
+# sigma 15 with 31 x 31 frequencies costs about 7x one at sigma 10 with
+# 21 x 21 (window area x frequency count), so 512^2 tiles keep the probe's
+# share of the frame near the 1024^2 benchmark's (16 probes a frame).
+SUR4_TILE = 512
 
 
 SIGMA15_WEIGHTS = os.path.join(PKG, "glsu", "surrogate_sigma15.npz")
@@ -562,12 +567,12 @@ def _large_run(glsu, torch, seed, form, nframes, warm, fp64_frames):
     tu = d.tuning()
     if form == "surrogate":
         params, dil = TS.load(SIGMA15_WEIGHTS)
-        d.set_surrogate(params, dil, SUR_TILE, 0, SUR_TOL)
+        d.set_surrogate(params, dil, SUR4_TILE, 0, SUR_TOL)
     st = torch.cuda.Stream()
     d.set_stream(st.cuda_stream)
     d.set_graph(True)
     buf = torch.empty((size, size), dtype=torch.float32, device="cuda")
-    ms, errs = [], []
+    ms, errs, fp64_s = [], [], 0.0
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     for k in range(1, warm + nframes + 1):
         buf.copy_(seq.frame(k))
@@ -582,8 +587,12 @@ def _large_run(glsu, torch, seed, form, nframes, warm, fp64_frames):
         if k > warm:
             ms.append(e0.elapsed_time(e1))
         if sample:
+            t0 = time.perf_counter()
             errs.append((k,) + fp64_frame_error(glsu, pref, buf, c["radius"], wp, d.get(glsu.PHI_REF)))
+            fp64_s += time.perf_counter() - t0
     d.set_graph(False)
+    if form == "surrogate":
+        d.set_probe_overlap(False)  # stage split with the stages one after another
     d.stage_timing(True)
     buf.copy_(seq.frame(warm + nframes + 1))
     d.per_frame_device(buf.data_ptr(), glsu.F32)
@@ -594,7 +603,7 @@ def _large_run(glsu, torch, seed, form, nframes, warm, fp64_frames):
     out = {"frames_per_s": 1e3 / mean_ms, "ms_per_frame": mean_ms, "frames_timed": nframes,
            "fp64_samples": [{"frame": k, "rmse": r, "max": m} for k, r, m in errs],
            "rmse_vs_fp64": float(np.sqrt(np.mean([r * r for _, r, _ in errs]))) if errs else None,
-           "max_abs_vs_fp64": max(m for _, _, m in errs) if errs else None}
+           "max_abs_vs_fp64": max(m for _, _, m in errs) if errs else None, "fp64_check_s": fp64_s}
     if form == "plain":
         out["stages_ms"] = {"dpra_ls": stg[0], "wff_rows": stg[1], "wff_column_sweep": stg[2],
                             "wff_final_update": stg[3]}
@@ -603,10 +612,11 @@ def _large_run(glsu, torch, seed, form, nframes, warm, fp64_frames):
         out["stages_ms"] = {"dpra_ls": stg[0], "network": stg[1], "wff2_probe_and_residuals": stg[2],
                             "fallback_and_update": stg[3], "wff2_probe_sweep": stg[7]}
         out["tiles_probed_recomputed"] = list(stats)
+        out["probe"] = {"tile": SUR4_TILE, "patch": 4, "tol_rad": SUR_TOL}
     return out
 
 
-def large_workload(glsu, torch, seed, nframes=12, warm=2, fp64_frames=(6, 12)):
+def large_workload(glsu, torch, seed, nframes=20, warm=2, fp64_frames=tuple(range(2, 21, 2))):
     """The large streaming workload (2048^2, 8 Gaussians, noise 0.05, DPRA
     9x9, WFF2 sigma 15 with 31 x 31 frequencies on [-1.5, 1.5]): the plain
     FP32 form and, with the sigma-15 network (glsu/surrogate_sigma15.npz),
@@ -837,6 +847,58 @@ def fft_sweep_flops(size, nfx, nfy, L, pitch):
     return float(pitch) * nfx * ((2 * nfy + 2) * 5.0 * L * np.log2(L) + nfy * 16.0 * L)
 
 
+def surrogate_training(glsu, torch, steps=20, warm=3, batch=16, crop=256):
+    """Training throughput of the surrogate's own kernels: one step is the
+    forward pass, the loss, the backward pass (data gradients on the tensor
+    cores, weight gradients on the CUDA cores) and the Adam update, for a
+    batch of `batch` crop x crop pairs already on the device; CUDA events on
+    the handle's stream around `steps` steps after `warm`.  The forward pass
+    alone is timed the same way, so the backward + update share follows."""
+    from glsu import train_surrogate as TS
+    net = glsu.Surrogate(batch, crop, crop, TS.DILATIONS, training=True)
+    net.params = TS.init_params(0)
+    st = torch.cuda.Stream()
+    net.set_stream(st.cuda_stream)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    ph = torch.rand((batch, crop, crop), generator=g, device="cuda") * (2 * np.pi)
+    z = torch.polar(torch.ones_like(ph), ph).to(torch.complex64)
+    t = torch.polar(torch.ones_like(ph), ph + 0.1 * torch.randn(ph.shape, generator=g, device="cuda"))
+    t = t.to(torch.complex64)
+    out = torch.empty_like(z)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(steps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    def step():
+        net.backward(z.data_ptr(), t.data_ptr(), want_loss=False)
+        net.adam(1e-4)
+
+    ms_step = timed(step)
+    ms_fwd = timed(lambda: net.forward(z.data_ptr(), out.data_ptr()))
+    loss, _ = net.backward(z.data_ptr(), t.data_ptr(), want_loss=True)
+    net.close()
+    px = batch * crop * crop
+    hidden = 2 * 288 * 32  # flops a pixel of one 32 -> 32 layer
+    fwd = 2 * 9 * 2 * 32 + 6 * hidden + 2 * 288 * 2
+    flops = 3 * fwd * px  # forward, data gradients, weight gradients
+    return {"steps_per_s": 1e3 / ms_step, "ms_per_step": ms_step, "pairs_per_s": batch * 1e3 / ms_step,
+            "batch": batch, "crop": crop, "ms_forward": ms_fwd, "ms_backward_and_update": ms_step - ms_fwd,
+            "tflops": flops / (ms_step * 1e-3) / 1e12, "flops_per_step": flops,
+            "tensor_core_share_of_flops": 2 * 6 * hidden / (3 * fwd),
+            "loss_after": loss, "steps_timed": steps,
+            "what": "forward + loss + backward + Adam on device-resident synthetic pairs; hidden layers' "
+                    "forward and data gradients on tcgen05, weight gradients on CUDA cores (FP32)"}
+
+
 def run_ours(args, rank, world, local):
     import torch
     import glsu
@@ -856,7 +918,7 @@ def run_ours(args, rank, world, local):
     frames, phi0, _ = synth.sequence(size, size, nfr, seed=seed)
     extras = not args.frames_only and rank == 0  # the legs beside the headline run on rank 0
 
-    wfr = batched = prec1 = large = None
+    wfr = batched = prec1 = large = training = None
     if extras:
         wfr = wfr_measure(glsu, torch, phi0, size, seed)
         batched = {"config_mix": batched_mix(glsu, torch, seed),
@@ -865,6 +927,7 @@ def run_ours(args, rank, world, local):
                                                            nframes=8)}
         prec1 = precision_form(glsu, torch, seed, size)
         large = large_workload(glsu, torch, seed)
+        training = surrogate_training(glsu, torch)
 
     stream = torch.cuda.Stream()
     dfr = torch.from_numpy(frames).cuda()
@@ -1042,6 +1105,7 @@ def run_ours(args, rank, world, local):
         "surrogate": sur,
         "precision_form": prec1,
         "large_workload": large,
+        "surrogate_training": training,
         "wfr": wfr,
         "batched_form": batched,
     }
