@@ -847,6 +847,25 @@ def fft_sweep_flops(size, nfx, nfy, L, pitch):
     return float(pitch) * nfx * ((2 * nfy + 2) * 5.0 * L * np.log2(L) + nfy * 16.0 * L)
 
 
+def probe_recall(glsu, SE, params, dil, size):
+    """The sparse probe's recall on tiles the network gets wrong (network-only
+    RMSE above the tolerance over the pixels where the WFF2 phase is
+    defined): with the network's last layer negated (wrong on every tile: the
+    probe, flag and fallback mechanism), and with a 0.9 rad/px carrier in the
+    phase change over the centre quarter of the frame (tile-local, partial
+    errors), 12 frames with every 2nd checked."""
+    keys = ("frames_sampled", "tiles_over_tol", "probe_recall", "tiles_flagged_within_tol", "rmse_median",
+            "rmse_network_only_median", "tiles_recomputed_fraction")
+    out = {}
+    for name, prm, kw, nf, ev in (("reversed_residual", SE.reversed_residual(params), {}, 4, 4),
+                                  ("carrier_0.9", params, {"delta_extra": SE.carrier_region(size)}, 12, 2)):
+        r = SE.deployment(glsu, prm, dil, [60100], nf, ev, size, wff=WFF, radius=RADIUS, tile=SUR_TILE,
+                          patch=SUR_PATCH, tol=SUR_TOL, **kw)
+        out[name] = {k: r[k] for k in keys}
+        out[name]["bad_tile_rmse"] = [round(v, 4) for x in r["per_frame"] for v in x["bad_tile_rmse"]]
+    return out
+
+
 def surrogate_training(glsu, torch, steps=20, warm=3, batch=16, crop=256):
     """Training throughput of the surrogate's own kernels: one step is the
     forward pass, the loss, the backward pass (data gradients on the tensor
@@ -972,6 +991,21 @@ def run_ours(args, rank, world, local):
         s_val, s_ms, s_st, s_clk = timed_frames(glsu, torch, ds, dfr, nfr, args, stream, flush, world, local)
         probed, flagged = ds.surrogate_stats()
         ds.close()
+        # the probe's cost scales with the number of tiles: the same frames
+        # with 128^2 tiles (64 probes a frame) and 512^2 tiles (4 probes)
+        tile_variants = None
+        if extras:
+            tile_variants = {}
+            for tv in (128, 512):
+                dv = glsu.DPRA(phi0.astype(np.float32), 1, RADIUS, "f32", wp)
+                dv.set_stream(stream.cuda_stream)
+                dv.set_surrogate(params, dil, tv, SUR_PATCH, SUR_TOL)
+                dv.set_graph(True)
+                v_val, v_ms, v_st, _ = timed_frames(glsu, torch, dv, dfr, nfr, args, stream, flush, world, local)
+                dv.close()
+                tile_variants["tile_%d" % tv] = {"frames_per_s": v_val, "ms_per_step": v_ms / args.steps,
+                                                 "probes_per_frame": (-(-size // tv)) ** 2,
+                                                 "probe_sweep_ms": v_st[7]}
 
         def sur_handle():
             h = plain_handle()
@@ -993,7 +1027,9 @@ def run_ours(args, rank, world, local):
                                   "the surrogate form (graph mode); every %d-th frame against the FP64 frame from "
                                   "the same reference phase" % (DEPLOY_SEEDS, DEPLOY_SEED0, DEPLOY_FRAMES,
                                                                  DEPLOY_EVERY))
+            deploy["probe_recall"] = probe_recall(glsu, SE, params, dil, size)
         sur = {"frames_per_s": s_val, "ms_per_step": s_ms / args.steps, "speedup_vs_plain": s_val / p_val,
+               "tile_variants": tile_variants,
                "e2e_frames_per_s": s_e2e, "e2e_runs": s_e2e_runs,
                "stages_ms": {"dpra_ls": s_st[0], "network": s_st[1], "wff2_probe_and_residuals": s_st[2],
                              "fallback_and_update": s_st[3]},

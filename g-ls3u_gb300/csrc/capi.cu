@@ -40,11 +40,31 @@ int raise_smem_limit(const void *func, int bytes, int carveout)
     int dev = 0;
     GLSU_CUDA_TRY(cudaGetDevice(&dev));
     if (!g_attr.needs(func, dev, bytes)) return GLSU_OK;
-    GLSU_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    if (carveout >= 0)
-        GLSU_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributePreferredSharedMemoryCarveout, carveout));
+    // a refused attribute would stay the runtime's last error and surface at
+    // the next launch check: clear it and report it here
+    if (cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GLSU_ERR_UNSUPPORTED,
+                    "a kernel's dynamic shared memory (" + std::to_string(bytes) + " bytes) exceeds the device limit");
+    }
+    if (carveout >= 0 &&
+        cudaFuncSetAttribute(func, cudaFuncAttributePreferredSharedMemoryCarveout, carveout) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GLSU_ERR_CUDA, "cudaFuncSetAttribute (shared-memory carveout) failed");
+    }
     g_attr.done(func, dev, bytes);
     return GLSU_OK;
+}
+
+int device_smem_optin()
+{
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
 }
 
 int device_sm_count()
@@ -974,11 +994,25 @@ extern "C" int glsu_dpra_set_ls_method(glsu_dpra *h, int method)
 
 static const int kLsTiles[3][2] = {{32, 16}, {32, 8}, {32, 32}};
 
+// The float-float tile's shared memory grows with the radius: 32 x 32 does
+// not fit at r = 8 (246 KB).
+static bool ls_tile_fits(int t, int r)
+{
+    const int lim = device_smem_optin();
+    return lim > 0 && dpra_ls_ff_smem(kLsTiles[t][0], kLsTiles[t][1], r) <= (size_t)lim;
+}
+
 extern "C" int glsu_dpra_set_ls_tile(glsu_dpra *h, int tile_width, int tile_height)
 {
     if (!h) return fail(GLSU_ERR_INVALID, "null handle");
     for (int t = 0; t < 3; t++)
         if (kLsTiles[t][0] == tile_width && kLsTiles[t][1] == tile_height) {
+            if (!ls_tile_fits(t, h->r))
+                return fail(GLSU_ERR_UNSUPPORTED,
+                            "a " + std::to_string(tile_width) + "x" + std::to_string(tile_height) +
+                                " least-squares tile at radius " + std::to_string(h->r) + " needs " +
+                                std::to_string(dpra_ls_ff_smem(tile_width, tile_height, h->r)) +
+                                " bytes of shared memory, above the device limit");
             dpra_drop_graphs(h);
             GLSU_CUDA_TRY(cudaStreamSynchronize(h->stream));
             h->ls_tile = t;
@@ -1012,7 +1046,12 @@ extern "C" int glsu_dpra_tune_ls_tile(glsu_dpra *h, float *ms)
     }
     int best = 0, rc = GLSU_OK;
     float best_ms = 0;
+    bool any = false;
     for (int t = 0; t < 3 && rc == GLSU_OK; t++) {
+        if (!ls_tile_fits(t, h->r)) {  // not a candidate at this radius
+            if (ms) ms[t] = -1.f;
+            continue;
+        }
         for (int k = 0; k < 4 && rc == GLSU_OK; k++) {
             if (k == 1 && cudaEventRecord(e0, s) != cudaSuccess) rc = fail(GLSU_ERR_CUDA, "cudaEventRecord");
             if (rc == GLSU_OK)
@@ -1025,9 +1064,10 @@ extern "C" int glsu_dpra_tune_ls_tile(glsu_dpra *h, float *ms)
             rc = fail(GLSU_ERR_CUDA, "timing a least-squares tile failed");
         t_ms /= 3;
         if (ms) ms[t] = t_ms;
-        if (rc == GLSU_OK && (t == 0 || t_ms < best_ms)) {
+        if (rc == GLSU_OK && (!any || t_ms < best_ms)) {
             best = t;
             best_ms = t_ms;
+            any = true;
         }
     }
     cudaEventDestroy(e0);

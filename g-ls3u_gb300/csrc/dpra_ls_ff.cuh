@@ -168,15 +168,22 @@ __device__ __forceinline__ void dpra_solve_ff(const ff *P, float mi, float cnt, 
     *Y = ys;
 }
 
+// Dynamic shared memory of a TX x TY output tile at radius r: per halo
+// element 8 float-float values (C-1, S, I-I_t and the five products), per
+// horizontal sum 8 float-float; odd row strides (in float-float elements):
+// the running-sum passes walk rows with consecutive threads, which then meet
+// distinct bank pairs.
+__host__ __device__ constexpr size_t ff_ls_smem_bytes(int tx, int ty, int r)
+{
+    return sizeof(float) * 2 * (8 * (size_t)((tx + 2 * r) | 1) * (ty + 2 * r) + 8 * (size_t)(ty + 2 * r) * (tx + 1));
+}
+
 template <int R, int TX, int TY> struct FfGeom {
     static constexpr int SW = TX + 2 * R, SH = TY + 2 * R;
-    // odd row strides (in float-float elements): the running-sum passes walk
-    // rows with consecutive threads, which then meet distinct bank pairs
     static constexpr int SWP = SW | 1, HSP = TX + 1;
     static constexpr int NE = SWP * SH, NH = SH * HSP;
-    // per halo element 8 float-float values (C-1, S, I-I_t and the five
-    // products), per horizontal sum 8 float-float
-    static constexpr size_t SMEM = sizeof(ff) * (8 * (size_t)NE + 8 * (size_t)NH);
+    static constexpr size_t SMEM = ff_ls_smem_bytes(TX, TY, R);
+    static_assert(SMEM == sizeof(ff) * (8 * (size_t)NE + 8 * (size_t)NH), "shared-memory layout");
     static_assert(NE >= TX * TY, "the vertical sums reuse the product buffer");
     static_assert(TX % 8 == 0 && TY % 8 == 0, "running sums over segments of 8 outputs");
 };

@@ -30,6 +30,8 @@ static int launch_tile(int img_type, const void *d_img, const void *d_phiref, vo
 #undef GLSU_TILE_R
 }
 
+size_t dpra_ls_ff_smem(int tx, int ty, int r) { return ff_ls_smem_bytes(tx, ty, r); }
+
 int launch_dpra_ls_ff_tile(int tile, int img_type, const void *d_img, const void *d_phiref, void *d_z, int W, int H,
                            int r, cudaStream_t s)
 {

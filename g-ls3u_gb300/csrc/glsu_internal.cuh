@@ -36,6 +36,10 @@ int cuda_fail(cudaError_t e, const char *what);
 int raise_smem_limit(const void *func, int bytes, int carveout = -1);
 // Multiprocessor count of the current device (looked up once per device).
 int device_sm_count();
+// Largest dynamic shared memory a block may opt into on the current device (0 if unknown).
+int device_smem_optin();
+// Dynamic shared memory of the float-float least squares with a tx x ty tile at radius r.
+size_t dpra_ls_ff_smem(int tx, int ty, int r);
 
 // ---------------------------------------------------------------------------
 // complex element types

@@ -477,7 +477,8 @@ class DPRA:
         return w.value, h.value
 
     def tune_ls_tile(self):
-        """Time the three least-squares tiles and select the fastest; returns their times (ms)."""
+        """Time the three least-squares tiles and select the fastest; returns their times (ms),
+        -1 for a tile whose shared memory does not fit at the handle's radius."""
         ms = (ctypes.c_float * 3)()
         check(lib().glsu_dpra_tune_ls_tile(self._h, ms))
         return list(ms)

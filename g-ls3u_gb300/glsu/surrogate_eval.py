@@ -19,9 +19,18 @@ each against phi_curr64, the tiles recomputed, and the probe's recall: of
 the tiles whose network-only RMSE against phi_curr64 exceeds the tolerance
 (over the tile's pixels where the FP64 WFF2 magnitude is at least 0.1, the
 probe's own mask: elsewhere the phase is not defined), the fraction the
-probe flagged; and the tiles flagged although within the tolerance.  ``noisy_region`` gives a noise map
-with a region far outside the training noise, where the network's output
-degrades, so that the recall is measured on tiles that need the fallback.
+probe flagged; and the tiles flagged although within the tolerance.
+
+The recall needs tiles that the network gets wrong, which the generator's
+sequences do not produce (nor do noise far outside the training range, steps
+and high-frequency ripples in the phase change: the network stays within
+0.015 rad on them).  Two cases make them:
+* ``carrier_region``: a linear phase ramp of 0.9 rad/px in the per-frame
+  phase change over a centred square, near the edge of the WFF2 frequency
+  range; the network's error there is tile-local and partial;
+* ``reversed_residual``: the network with its last layer negated (its
+  correction applied backwards), wrong on every tile: the mechanism check of
+  probe, flag and fallback.
 
     python -m glsu.surrogate_eval [--seeds 10] [--frames 200] [--every 20]
 """
@@ -135,6 +144,28 @@ def noisy_region(size, level=0.2, base=0.02, frac=0.25):
     c = size // 2
     m[c - h:c + h, c - h:c + h] = level
     return m
+
+
+def carrier_region(size, slope=0.9, frac=0.25):
+    """A per-frame phase-change addition for the probe's recall check: a
+    linear ramp of `slope` rad/px along x in a centred square covering `frac`
+    of the frame, zero elsewhere."""
+    m = np.zeros((size, size))
+    h = int(round(size * np.sqrt(frac) / 2))
+    c = size // 2
+    x = np.arange(size, dtype=np.float64)[None, :]
+    m[c - h:c + h, c - h:c + h] = (slope * x)[:, c - h:c + h]
+    return m
+
+
+def reversed_residual(params):
+    """The network's parameters with the last layer (weights and bias)
+    negated: y = z - conv7(a6) instead of z + conv7(a6)."""
+    from .train_surrogate import LAYER_SIZES
+    p = np.array(params, np.float32, copy=True)
+    n_last = LAYER_SIZES[-1][0] * LAYER_SIZES[-1][1] * 9 + LAYER_SIZES[-1][0]
+    p[-n_last:] = -p[-n_last:]
+    return p
 
 
 def summarise(recs, tol=0.05):

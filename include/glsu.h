@@ -301,13 +301,15 @@ int glsu_dpra_set_ls_method(glsu_dpra *h, int method);
  * knob): 32 x 16 (the default), 32 x 8 or 32 x 32 outputs per CTA.  The
  * regressors are rotated to each tile's centre phase, so tiles give the
  * same results to float-float rounding, not bit for bit; the default is
- * fixed so that outputs are reproducible unless a tile is chosen. */
+ * fixed so that outputs are reproducible unless a tile is chosen.  A tile
+ * whose shared memory exceeds the device's per-block limit at the handle's
+ * radius (32 x 32 at r = 8) returns GLSU_ERR_UNSUPPORTED. */
 int glsu_dpra_set_ls_tile(glsu_dpra *h, int tile_width, int tile_height);
 int glsu_dpra_get_ls_tile(const glsu_dpra *h, int *tile_width, int *tile_height);
 /* Time the three tiles on this handle's shape and window (a zero frame
  * against its reference phase, three launches each) and select the
- * fastest; ms (optional, 3 floats) receives the times in the order above.
- * Overwrites the handle's frame buffer and least-squares output. */
+ * fastest; ms (optional, 3 floats) receives the times in the order above,
+ * -1 for a tile that does not fit at the handle's radius.  Overwrites the handle's frame buffer and least-squares output. */
 int glsu_dpra_tune_ls_tile(glsu_dpra *h, float *ms);
 /* Copy the last frame's least-squares output exp(j dphi) (complex, W*H) to a
  * device buffer, enqueued on the handle's stream. */

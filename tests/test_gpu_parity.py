@@ -306,6 +306,15 @@ def test_dpra_ls_tiles_match_oracle(glsu, oracle, synth, tile, r, img):
     fr = frames[2] if img == "f32" else np.clip(np.round(frames[2] * 255), 0, 255).astype(np.uint8)
     phi_in = phi0.astype(np.float32)
     wp = glsu.WffParams(3.0, -0.5, 0.5, 0.5, 3.0, -0.5, 0.5, 0.5, 0.1)
+    if tile == (32, 32) and r == 8:
+        # 246 KB of shared memory: above the per-block limit, refused up front
+        d = glsu.DPRA(phi_in, 1, r, "f32", wp)
+        with pytest.raises(glsu.GlsuError) as e:
+            d.set_ls_tile(*tile)
+        assert e.value.code == glsu.ERR_UNSUPPORTED and d.ls_tile() == (32, 16)
+        d.per_frame(fr)  # the handle is still usable
+        d.close()
+        return
     out = []
     for t in ((32, 16), tile):
         d = glsu.DPRA(phi_in, 1, r, "f32", wp)
@@ -333,6 +342,14 @@ def test_dpra_ls_tile_tuning(glsu, synth):
     with pytest.raises(glsu.GlsuError):
         d.set_ls_tile(16, 16)
     d.per_frame(frames[1])  # runs with the chosen tile
+    assert np.isfinite(d.get(glsu.PHI_CURR)).all()
+    d.close()
+    # at r = 8 the 32 x 32 tile does not fit in shared memory: not a candidate
+    d = glsu.DPRA(phi0.astype(np.float32), 1, 8, "f32", glsu.WffParams(10.0, -1, 1, 0.1, 10.0, -1, 1, 0.1, 0.2))
+    ms = d.tune_ls_tile()
+    print("LS tile times at r = 8 (ms):", dict(zip(tiles, ms)), "chosen", d.ls_tile())
+    assert ms[2] < 0 and ms[0] > 0 and ms[1] > 0 and d.ls_tile() == tiles[int(np.argmin(ms[:2]))]
+    d.per_frame(frames[1])
     assert np.isfinite(d.get(glsu.PHI_CURR)).all()
     d.close()
 
