@@ -13,7 +13,7 @@
 namespace glsu {
 
 constexpr int kSurPixBlocks = 152 * 8;  // grid of the per-pixel CUDA-core kernels
-constexpr int kSurSmallPix = 1024;      // pixels per block of the small weight-gradient kernels
+constexpr int kSurDbPix = 4096;         // pixels per block of the bias-gradient sums
 
 static int grid_for(size_t n) { return (int)std::min<size_t>((n + 255) / 256, kSurPixBlocks); }
 
@@ -65,9 +65,12 @@ int SurNet::init(int batch, int width, int height, const int *dilations, bool tr
              A((void **)&d_v, kSurParams * 4) && A((void **)&d_lpart, (size_t)kSurPixBlocks * 8) &&
              A((void **)&d_y, n * 8) &&
              A((void **)&d_loss, 8);
-        nb32 = sur_dw32_blocks(B, H, W);
-        nbs = (int)((n + kSurSmallPix - 1) / kSurSmallPix);
-        ok = ok && A((void **)&d_part, (size_t)std::max(nb32 * (9216 + 32), nbs * kSurL0Params) * 4);
+        nbs = sur_dw_small_blocks(B, H, W);
+        ndb = (int)((n + kSurDbPix - 1) / kSurDbPix);
+        const size_t part = std::max<size_t>(std::max<size_t>((size_t)device_sm_count() * 9216,
+                                                              (size_t)nbs * kSurL0Params),
+                                             (size_t)ndb * 32);
+        ok = ok && A((void **)&d_part, part * 4);
     }
     if (!ok) return fail(GLSU_ERR_ALLOC, "surrogate: device allocation failed");
     GLSU_CUDA_TRY(cudaMemset(d_err, 0, sizeof(int)));
@@ -88,6 +91,8 @@ int SurNet::init(int batch, int width, int height, const int *dilations, bool tr
         }
     }
     GLSU_TRY(sur_make_map(&map7, a6(), B, H, W, dil[7]));
+    if (training)
+        for (int k = 0; k < 2; k++) GLSU_TRY(sur_make_map_box(&map_g[k], d_g[k], B, H, W, 128));
     return pack();
 }
 
@@ -188,17 +193,30 @@ int SurNet::backward(const void *d_z, const void *d_target)
                                                           d_dh, d_lpart);
     sur_sum_kernel<<<1, 32, 0, stream>>>(d_lpart, kSurPixBlocks, d_loss);
     // layer 7: weight gradient and dL/da6 (masked)
-    sur_dw_small_kernel<2, 32><<<nbs, 256, 0, stream>>>(d_dh, d_act[6], B, H, W, dil[7], kSurSmallPix, d_part);
-    sur_reduce_kernel<<<(kSurL7Params + 255) / 256, 256, 0, stream>>>(d_part, nbs, kSurL7Params,
-                                                                       d_grad + sur_layer_offset(7));
+    GLSU_TRY(raise_smem_limit((const void *)sur_dw_small_kernel<2, 32>, sur_dw_small_smem(64, 2, 32)));
+    GLSU_TRY(raise_smem_limit((const void *)sur_dw_small_kernel<32, 2>, sur_dw_small_smem(64, 32, 2)));
+    sur_dw_small_kernel<2, 32><<<nbs, 288, sur_dw_small_smem(dil[7], 2, 32), stream>>>(d_dh, d_act[6], B, H, W,
+                                                                                       dil[7], d_part);
+    sur_reduce_kernel<<<(kSurL7Params + 31) / 32, 256, 0, stream>>>(d_part, nbs, kSurL7Params,
+                                                                     d_grad + sur_layer_offset(7));
     sur_l7_bwd_kernel<<<g, 256, 0, stream>>>(d_dh, d_act[6], B, H, W, dil[7], d_w7r, d_g[0]);
     GLSU_CUDA_TRY(cudaGetLastError());
-    GLSU_TRY(raise_smem_limit((const void *)sur_dw32_kernel, sur_dw32_smem(64)));
+    const size_t npx = (size_t)B * H * W;
     for (int l = 6; l >= 1; l--) {
         uint16_t *gl = d_g[(6 - l) & 1], *gprev = d_g[(7 - l) & 1];
-        sur_dw32_kernel<<<nb32, 256, sur_dw32_smem(dil[l]), stream>>>(gl, d_act[l - 1], B, H, W, dil[l], d_part);
-        sur_reduce_kernel<<<(kSurL32Params + 255) / 256, 256, 0, stream>>>(d_part, nb32, kSurL32Params,
-                                                                            d_grad + sur_layer_offset(l));
+        // weights on the tensor cores, bias on CUDA cores, each summed over its partials in a fixed order
+        SurWgradArgs wa;
+        wa.B = B;
+        wa.H = H;
+        wa.W = W;
+        wa.dil = dil[l];
+        wa.part = d_part;
+        wa.err = d_err;
+        int nblk = 0;
+        GLSU_TRY(launch_sur_wgrad(map_fwd[l], map_g[(6 - l) & 1], wa, stream, &nblk));
+        sur_reduce_kernel<<<9216 / 32, 256, 0, stream>>>(d_part, nblk, 9216, d_grad + sur_layer_offset(l));
+        sur_db32_kernel<<<ndb, 256, 0, stream>>>(gl, npx, kSurDbPix, d_part);
+        sur_reduce_kernel<<<1, 256, 0, stream>>>(d_part, ndb, 32, d_grad + sur_layer_offset(l) + 9216);
         GLSU_CUDA_TRY(cudaGetLastError());
         SurConvArgs a;
         a.B = B;
@@ -214,8 +232,9 @@ int SurNet::backward(const void *d_z, const void *d_target)
         GLSU_TRY(launch_sur_conv(map_bwd[l], map_bwd_out[l], a, stream));
     }
     // layer 0: weight gradient from g0 (in d_g[0] after six swaps) and the input
-    sur_dw_small_kernel<32, 2><<<nbs, 256, 0, stream>>>(d_g[0], z, B, H, W, dil[0], kSurSmallPix, d_part);
-    sur_reduce_kernel<<<(kSurL0Params + 255) / 256, 256, 0, stream>>>(d_part, nbs, kSurL0Params, d_grad);
+    sur_dw_small_kernel<32, 2><<<nbs, 288, sur_dw_small_smem(dil[0], 32, 2), stream>>>(d_g[0], z, B, H, W, dil[0],
+                                                                                       d_part);
+    sur_reduce_kernel<<<(kSurL0Params + 31) / 32, 256, 0, stream>>>(d_part, nbs, kSurL0Params, d_grad);
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
 }
@@ -416,4 +435,63 @@ extern "C" int glsu_sur_conv32(const void *d_in, void *d_out, int batch, int wid
     cudaFree(d_w7r);
     cudaFree(d_err);
     return rc;
+}
+
+namespace glsu {
+int sur_wgrad32_once(const void *d_g, const void *d_in, int batch, int width, int height, int dilation, float *h_dw,
+                     cudaStream_t s)
+{
+    const size_t n = (size_t)batch * height * width;
+    const int ndb = (int)((n + kSurDbPix - 1) / kSurDbPix);
+    float *d_part = nullptr, *d_out = nullptr;
+    int *d_err = nullptr;
+    int rc = GLSU_OK;
+    const size_t part = std::max<size_t>((size_t)device_sm_count() * 9216, (size_t)ndb * 32);
+    if (cudaMalloc(&d_part, part * 4) != cudaSuccess || cudaMalloc(&d_out, kSurL32Params * 4) != cudaSuccess ||
+        cudaMalloc(&d_err, 4) != cudaSuccess)
+        rc = fail(GLSU_ERR_ALLOC, "allocation failed");
+    CUtensorMap tma, tmg;
+    if (rc == GLSU_OK) rc = sur_make_map(&tma, d_in, batch, height, width, dilation);
+    if (rc == GLSU_OK) rc = sur_make_map_box(&tmg, d_g, batch, height, width, 128);
+    if (rc == GLSU_OK && cudaMemsetAsync(d_err, 0, 4, s) != cudaSuccess) rc = fail(GLSU_ERR_CUDA, "memset failed");
+    if (rc == GLSU_OK) {
+        SurWgradArgs wa;
+        wa.B = batch;
+        wa.H = height;
+        wa.W = width;
+        wa.dil = dilation;
+        wa.part = d_part;
+        wa.err = d_err;
+        int nblk = 0;
+        rc = launch_sur_wgrad(tma, tmg, wa, s, &nblk);
+        if (rc == GLSU_OK) {
+            sur_reduce_kernel<<<9216 / 32, 256, 0, s>>>(d_part, nblk, 9216, d_out);
+            sur_db32_kernel<<<ndb, 256, 0, s>>>((const uint16_t *)d_g, n, kSurDbPix, d_part);
+            sur_reduce_kernel<<<1, 256, 0, s>>>(d_part, ndb, 32, d_out + 9216);
+            if (cudaGetLastError() != cudaSuccess) rc = fail(GLSU_ERR_CUDA, "weight-gradient launch failed");
+        }
+    }
+    int e = 0;
+    if (rc == GLSU_OK && (cudaMemcpyAsync(h_dw, d_out, kSurL32Params * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                          cudaMemcpyAsync(&e, d_err, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess))
+        rc = fail(GLSU_ERR_CUDA, "copy failed");
+    if (rc == GLSU_OK && cudaStreamSynchronize(s) != cudaSuccess) rc = fail(GLSU_ERR_CUDA, "weight gradient failed");
+    if (rc == GLSU_OK && e) rc = fail(e, "weight gradient: a bounded wait timed out");
+    cudaFree(d_part);
+    cudaFree(d_out);
+    cudaFree(d_err);
+    return rc;
+}
+}  // namespace glsu
+
+// Weight and bias gradient of one 32 -> 32 layer on caller buffers (the
+// building block of the training pass; synchronous).  d_g: the gradient
+// w.r.t. the layer's output, d_in: its input, both [B][H][W][32] BF16;
+// h_dw: 9216 + 32 floats, W[co][ci][3][3] then b[co].
+extern "C" int glsu_sur_wgrad32(const void *d_g, const void *d_in, int batch, int width, int height, int dilation,
+                                float *h_dw, void *stream)
+{
+    if (!d_g || !d_in || !h_dw) return glsu::fail(GLSU_ERR_INVALID, "null argument");
+    if (batch < 1 || width < 1 || height < 1) return glsu::fail(GLSU_ERR_INVALID, "bad size");
+    return glsu::sur_wgrad32_once(d_g, d_in, batch, width, height, dilation, h_dw, (cudaStream_t)stream);
 }

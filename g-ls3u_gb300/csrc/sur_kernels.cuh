@@ -591,145 +591,290 @@ __global__ void __launch_bounds__(256) sur_l7_bwd_kernel(const float2 *__restric
 }
 
 // ---------------------------------------------------------------------------
-// weight gradients (CUDA cores, FP32), per-block partials
+// weight gradients
 // ---------------------------------------------------------------------------
-// 32 -> 32 layer: part[blk][co][ci][t] (+ part[blk][9216 + co] for the bias)
-// = sum over the block's pixels of g[p][co] * a[p + off_t][ci].  A block
-// takes output rows of one 64-pixel segment.
-constexpr int kDwSeg = 64;
-constexpr int kDwRowsPerBlock = 8;
+// 32 -> 32 layer on the tensor cores.  With d the dilation and g the
+// gradient w.r.t. the layer's output,
+//   dW[co][ci][ky][kx] = sum_{b, y', x} g[b, y' - (ky-1) d, x, co] a[b, y', x + (kx-1) d, ci]
+// (y' = y + (ky-1) d: each activation row y' meets the gradient rows y' + d,
+// y', y' - d).  A work item is one 128-pixel segment of one activation row.
+// Per 16 pixels one MMA D[M = 128][N = 96] += A[M][K = 16] B[K][N]:
+//   A: the three gradient rows, M = ky * 32 + co (a zeroed fourth block pads
+//      M to 128);
+//   B: the activation row, N = kx * 32 + ci, its three kx blocks d pixels
+//      apart.
+// Both operands are the pixel-major rows that TMA writes with 64-byte
+// swizzle, read MN-major: per pixel the 32 channels (64 bytes, the M or N
+// direction), pixels 64 bytes apart and 8-pixel groups 512 bytes apart (K),
+// the 32-channel blocks LBO apart (the gradient slot stride for A, 64 d bytes
+// for B).  The accumulator stays in TMEM across all of a CTA's items; the
+// epilogue writes it once as the CTA's partial, part[blk][co][ci][ky*3+kx].
+constexpr int kWgStages = 4;
+constexpr int kWgSlot = 128 * 64;          // one 128-pixel gradient row segment
+constexpr int kWgPad = 16 * 1024;          // slack after the stages
+constexpr uint32_t kWgTmemCols = 128;
 
-__global__ void __launch_bounds__(256) sur_dw32_kernel(const uint16_t *__restrict__ g, const uint16_t *__restrict__ a,
-                                                       int B, int H, int W, int dil, float *__restrict__ part)
+__host__ __device__ inline int sur_wgrad_act_bytes(int dil) { return ((128 + 2 * dil) * 64 + 1023) & ~1023; }
+__host__ __device__ inline int sur_wgrad_stage_bytes(int dil) { return 4 * kWgSlot + sur_wgrad_act_bytes(dil); }
+inline int sur_wgrad_smem_bytes(int dil) { return kWgStages * sur_wgrad_stage_bytes(dil) + kWgPad + 256; }
+
+// MN-major operand in the 64-byte swizzle layout: 32-element blocks `lbo`
+// bytes apart, 8-row (K) groups 512 bytes apart.
+__device__ __forceinline__ uint64_t umma_desc_mn_sw64(uint32_t saddr, uint32_t lbo)
 {
-    extern __shared__ __align__(16) float dsm[];
-    const int SW = kDwSeg + 2 * dil;
-    float *gs = dsm;                  // [64][32]
-    float *as = gs + kDwSeg * 32;     // [3][SW][32]
-    const int nsx = (W + kDwSeg - 1) / kDwSeg;
-    const int nby = (H + kDwRowsPerBlock - 1) / kDwRowsPerBlock;
+    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)(512 >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
+}
+
+struct SurWgradArgs {
+    int B = 0, H = 0, W = 0, dil = 1;
+    float *part = nullptr;  // [gridDim.x][9216]
+    int *err = nullptr;
+};
+
+__global__ void __launch_bounds__(256, 1) sur_wgrad_tc_kernel(const __grid_constant__ CUtensorMap tma,
+                                                              const __grid_constant__ CUtensorMap tmg,
+                                                              SurWgradArgs a, int nitems)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const int stage_bytes = sur_wgrad_stage_bytes(a.dil);
+    uint64_t *full = reinterpret_cast<uint64_t *>(sm + kWgStages * stage_bytes + kWgPad);
+    uint64_t *sfree = full + kWgStages;
+    uint64_t *done = sfree + kWgStages;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nsx = (a.W + 127) / 128;
+    if (tid == 0) {
+        for (int s = 0; s < kWgStages; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&sfree[s], 1);
+        }
+        mbar_init(done, 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) tmem_alloc(tslot, kWgTmemCols);
+    // the fourth gradient block of every stage stays zero: it pads M to 128
+    for (int s = 0; s < kWgStages; s++)
+        for (int e = tid; e < kWgSlot / 16; e += 256)
+            reinterpret_cast<uint4 *>(sm + s * stage_bytes + 3 * kWgSlot)[e] = make_uint4(0, 0, 0, 0);
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    if (warp == 0 && lane == 0) {
+        // ---- producer: per item three gradient rows and one activation row ----
+        uint32_t g = 0;
+        bool ok = true;
+        for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x, g++) {
+            const int sx = item % nsx, yb = item / nsx, y = yb % a.H, b = yb / a.H;
+            const int s = g % kWgStages;
+            if (g >= (uint32_t)kWgStages && !mbar_wait_bounded(&sfree[s], ((g / kWgStages) - 1) & 1)) {
+                ok = false;
+                break;
+            }
+            unsigned char *st = sm + s * stage_bytes;
+            mbar_expect_tx(&full[s], 3u * kWgSlot + (uint32_t)(128 + 2 * a.dil) * 64);
+            // rows outside the image arrive as zeros
+            tma_load_4d(st, &tmg, &full[s], 0, sx * 128, y + a.dil, b);
+            tma_load_4d(st + kWgSlot, &tmg, &full[s], 0, sx * 128, y, b);
+            tma_load_4d(st + 2 * kWgSlot, &tmg, &full[s], 0, sx * 128, y - a.dil, b);
+            tma_load_4d(st + 4 * kWgSlot, &tma, &full[s], 0, sx * 128 - a.dil, y, b);
+        }
+        if (!ok) atomicExch(a.err, GLSU_ERR_TIMEOUT);
+        for (uint32_t j = g > (uint32_t)kWgStages ? g - kWgStages : 0; j < g; j++)
+            mbar_wait_bounded(&full[j % kWgStages], (j / kWgStages) & 1);
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer ----
+        const uint32_t idesc = umma_idesc_bf16(128, 96) | (1u << 15) | (1u << 16);  // A and B MN-major
+        uint32_t g = 0, acc = 0;
+        bool ok = true;
+        for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x, g++) {
+            const int s = g % kWgStages;
+            if (!mbar_wait_bounded(&full[s], (g / kWgStages) & 1)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t gb = smem_u32(sm + s * stage_bytes), ab = gb + 4 * kWgSlot;
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                umma_bf16(tmem, umma_desc_mn_sw64(gb + k * 1024, kWgSlot),
+                          umma_desc_mn_sw64(ab + k * 1024, (uint32_t)a.dil * 64), idesc, acc);
+                acc = 1;
+            }
+            umma_commit(&sfree[s]);
+        }
+        if (!ok) atomicExch(a.err, GLSU_ERR_TIMEOUT);
+        umma_commit(done);  // every MMA has completed before the epilogue reads and TMEM is released
+        mbar_wait_bounded(done, 0);
+    } else if (warp >= 4 && warp < 7) {
+        // ---- epilogue: lanes 0-95 (ky = warp - 4, co = lane) -> the CTA's partial ----
+        const int ky = warp - 4;
+        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(done, 0));
+        if (!ok && lane == 0) atomicExch(a.err, GLSU_ERR_TIMEOUT);
+        tc_fence_after();
+        const bool any = blockIdx.x < nitems;
+        float *pp = a.part + (size_t)blockIdx.x * 9216 + (size_t)lane * 288;
+#pragma unroll
+        for (int kx = 0; kx < 3; kx++) {
+            float v[32];
+            tmem_ld32(tmem + ((uint32_t)(ky * 32) << 16) + (uint32_t)(kx * 32), v);
+#pragma unroll
+            for (int ci = 0; ci < 32; ci++) pp[ci * 9 + ky * 3 + kx] = (any && ok) ? v[ci] : 0.f;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, kWgTmemCols);
+}
+
+int launch_sur_wgrad(const CUtensorMap &tma, const CUtensorMap &tmg, const SurWgradArgs &a, cudaStream_t s,
+                     int *nblocks)
+{
+    if (a.dil < 1 || a.dil > 64) return fail(GLSU_ERR_INVALID, "surrogate dilation must be 1..64");
+    GLSU_TRY(raise_smem_limit((const void *)sur_wgrad_tc_kernel, sur_wgrad_smem_bytes(64),
+                              (int)cudaSharedmemCarveoutMaxShared));
+    const int items = a.B * a.H * ((a.W + 127) / 128);
+    const int grid = std::max(1, std::min(items, device_sm_count()));
+    sur_wgrad_tc_kernel<<<grid, 256, sur_wgrad_smem_bytes(a.dil), s>>>(tma, tmg, a, items);
+    GLSU_CUDA_TRY(cudaGetLastError());
+    *nblocks = grid;
+    return GLSU_OK;
+}
+
+// Bias gradient of a 32-channel layer: part[blk][c] = sum of g[p][c] over
+// the block's pixel range (8 pixel lanes per channel, then a fixed-order sum).
+__global__ void __launch_bounds__(256) sur_db32_kernel(const uint16_t *__restrict__ g, size_t n, int per_block,
+                                                       float *__restrict__ part)
+{
+    __shared__ float s[8][33];
+    const int c = threadIdx.x & 31, pl = threadIdx.x >> 5;
+    const size_t p0 = (size_t)blockIdx.x * per_block;
+    float acc = 0.f;
+    for (size_t p = p0 + pl; p < p0 + per_block && p < n; p += 8) acc += bf2f(g[p * 32 + c]);
+    s[pl][c] = acc;
+    __syncthreads();
+    if (pl == 0) {
+        float t = s[0][c];
+        for (int k = 1; k < 8; k++) t += s[k][c];
+        part[(size_t)blockIdx.x * 32 + c] = t;
+    }
+}
+
+// Layer 0 (g: BF16 32 channels, input z: complex) and layer 7 (g = dh:
+// complex, input a6: BF16 32 channels) on CUDA cores: a block takes 8 rows
+// of one 64-pixel segment, staging per row the gradient and the three input
+// rows (with the dilated halo) in shared memory as FP32; thread c < 288
+// owns (tap t = c / 32, j = c % 32) and accumulates the two weights that
+// pair j with both channels of the 2-channel side.  part[blk][co][ci][t]
+// then the biases part[blk][576 + co].
+constexpr int kDsSeg = 64, kDsRows = 8;
+
+template <int COUT, int CIN>
+__global__ void __launch_bounds__(288) sur_dw_small_kernel(const void *__restrict__ gptr,
+                                                           const void *__restrict__ inptr, int B, int H, int W,
+                                                           int dil, float *__restrict__ part)
+{
+    static_assert((COUT == 2 && CIN == 32) || (COUT == 32 && CIN == 2), "layer 0 or layer 7");
+    extern __shared__ __align__(16) float dss[];
+    const int SW = kDsSeg + 2 * dil;
+    float *gs = dss;                      // [64][COUT]
+    float *is = gs + kDsSeg * COUT;       // [3][SW][CIN]
+    const int nsx = (W + kDsSeg - 1) / kDsSeg, nby = (H + kDsRows - 1) / kDsRows;
     int item = blockIdx.x;
     const int sx = item % nsx;
     item /= nsx;
-    const int by = item % nby;
-    const int b = item / nby;
-    const int x0 = sx * kDwSeg;
-    const int tid = threadIdx.x, co = tid >> 3, ci0 = (tid & 7) * 4;
-    float acc[9][4];
-    float bacc = 0.f;
-#pragma unroll
-    for (int t = 0; t < 9; t++)
-#pragma unroll
-        for (int i = 0; i < 4; i++) acc[t][i] = 0.f;
-    for (int yy = 0; yy < kDwRowsPerBlock; yy++) {
-        const int y = by * kDwRowsPerBlock + yy;
+    const int by = item % nby, b = item / nby;
+    const int x0 = sx * kDsSeg;
+    const int tid = threadIdx.x, t = tid >> 5, j = tid & 31;
+    const int ky = t / 3, kx = t % 3;
+    float acc0 = 0.f, acc1 = 0.f, bacc = 0.f;
+    for (int yy = 0; yy < kDsRows; yy++) {
+        const int y = by * kDsRows + yy;
         if (y >= H) break;
         __syncthreads();
-        for (int e = tid; e < kDwSeg * 4; e += 256) {  // 16-byte groups of g
-            const int px = e >> 2, grp = e & 3, x = x0 + px;
-            float v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            if (x < W) unpack8(reinterpret_cast<const uint4 *>(g + (((size_t)b * H + y) * W + x) * 32)[grp], v);
-#pragma unroll
-            for (int i = 0; i < 8; i++) gs[px * 32 + grp * 8 + i] = v[i];
+        for (int e = tid; e < kDsSeg * COUT; e += 288) {
+            const int px = e / COUT, c = e % COUT, x = x0 + px;
+            float v = 0.f;
+            if (x < W) {
+                const size_t p = ((size_t)b * H + y) * W + x;
+                if (COUT == 32) v = bf2f(reinterpret_cast<const uint16_t *>(gptr)[p * 32 + c]);
+                else v = c == 0 ? reinterpret_cast<const float2 *>(gptr)[p].x
+                                : reinterpret_cast<const float2 *>(gptr)[p].y;
+            }
+            gs[e] = v;
         }
-        for (int e = tid; e < 3 * SW * 4; e += 256) {
-            const int grp = e & 3, rest = e >> 2, px = rest % SW, ky = rest / SW;
-            const int ys = y + (ky - 1) * dil, xs = x0 - dil + px;
-            float v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            if (ys >= 0 && ys < H && xs >= 0 && xs < W)
-                unpack8(reinterpret_cast<const uint4 *>(a + (((size_t)b * H + ys) * W + xs) * 32)[grp], v);
-#pragma unroll
-            for (int i = 0; i < 8; i++) as[(ky * SW + px) * 32 + grp * 8 + i] = v[i];
+        for (int e = tid; e < 3 * SW * CIN; e += 288) {
+            const int c = e % CIN, rest = e / CIN, px = rest % SW, r = rest / SW;
+            const int ys = y + (r - 1) * dil, xs = x0 - dil + px;
+            float v = 0.f;
+            if (ys >= 0 && ys < H && xs >= 0 && xs < W) {
+                const size_t q = ((size_t)b * H + ys) * W + xs;
+                if (CIN == 32) v = bf2f(reinterpret_cast<const uint16_t *>(inptr)[q * 32 + c]);
+                else v = c == 0 ? reinterpret_cast<const float2 *>(inptr)[q].x
+                                : reinterpret_cast<const float2 *>(inptr)[q].y;
+            }
+            is[e] = v;
         }
         __syncthreads();
-        for (int px = 0; px < kDwSeg; px++) {
-            const float gv = gs[px * 32 + co];
-            bacc += gv;
-#pragma unroll
-            for (int t = 0; t < 9; t++) {
-                const float4 av =
-                    *reinterpret_cast<const float4 *>(&as[((t / 3) * SW + px + (t % 3) * dil) * 32 + ci0]);
-                acc[t][0] = fmaf(gv, av.x, acc[t][0]);
-                acc[t][1] = fmaf(gv, av.y, acc[t][1]);
-                acc[t][2] = fmaf(gv, av.z, acc[t][2]);
-                acc[t][3] = fmaf(gv, av.w, acc[t][3]);
+        const float *ir = is + (size_t)(ky * SW + kx * dil) * CIN;
+        if (COUT == 2) {  // layer 7: j = ci, the two output channels
+            for (int px = 0; px < kDsSeg; px++) {
+                const float iv = ir[px * CIN + j];
+                acc0 = fmaf(gs[px * 2], iv, acc0);
+                acc1 = fmaf(gs[px * 2 + 1], iv, acc1);
             }
+            if (tid < 2)
+                for (int px = 0; px < kDsSeg; px++) bacc += gs[px * 2 + tid];
+        } else {  // layer 0: j = co, the two input channels
+            for (int px = 0; px < kDsSeg; px++) {
+                const float gv = gs[px * 32 + j];
+                acc0 = fmaf(gv, ir[px * 2], acc0);
+                acc1 = fmaf(gv, ir[px * 2 + 1], acc1);
+            }
+            if (tid < 32)
+                for (int px = 0; px < kDsSeg; px++) bacc += gs[px * 32 + tid];
         }
     }
-    float *pp = part + (size_t)blockIdx.x * (9216 + 32);
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int t = 0; t < 9; t++) pp[(co * 32 + ci0 + i) * 9 + t] = acc[t][i];
-    if ((tid & 7) == 0) pp[9216 + co] = bacc;
-}
-
-int sur_dw32_blocks(int B, int H, int W)
-{
-    return B * ((H + kDwRowsPerBlock - 1) / kDwRowsPerBlock) * ((W + kDwSeg - 1) / kDwSeg);
-}
-int sur_dw32_smem(int dil) { return (kDwSeg * 32 + 3 * (kDwSeg + 2 * dil) * 32) * 4; }
-
-// Layer 0 (g0 BF16 32 ch, input x = z 2 ch) and layer 7 (g = dh 2 ch FP32,
-// input a6 32 ch): part[blk][co][ci][t] + bias, one combination per thread
-// stride.  COUT x CIN = 32 x 2 or 2 x 32.
-template <int COUT, int CIN>
-__global__ void __launch_bounds__(256) sur_dw_small_kernel(const void *__restrict__ gptr,
-                                                           const void *__restrict__ inptr, int B, int H, int W,
-                                                           int dil, int pix_per_block, float *__restrict__ part)
-{
-    constexpr int NW = COUT * CIN * 9, NT = NW + COUT;
-    constexpr int PER = (NT + 255) / 256;
-    float acc[PER];
-#pragma unroll
-    for (int i = 0; i < PER; i++) acc[i] = 0.f;
-    const size_t n = (size_t)B * H * W;
-    const size_t p0 = (size_t)blockIdx.x * pix_per_block;
-    for (size_t p = p0; p < p0 + pix_per_block && p < n; p++) {
-        const int x = (int)(p % W);
-        const int y = (int)((p / W) % H);
-        const size_t img = p - (size_t)y * W - x;
-#pragma unroll
-        for (int i = 0; i < PER; i++) {
-            const int c = threadIdx.x + 256 * i;
-            if (c >= NT) continue;
-            const int co = c < NW ? c / (CIN * 9) : c - NW;
-            float gv;
-            if (COUT == 32) gv = bf2f(reinterpret_cast<const uint16_t *>(gptr)[p * 32 + co]);
-            else gv = co == 0 ? reinterpret_cast<const float2 *>(gptr)[p].x : reinterpret_cast<const float2 *>(gptr)[p].y;
-            if (c >= NW) {
-                acc[i] += gv;
-                continue;
-            }
-            const int ci = (c / 9) % CIN, t = c % 9;
-            const int yy = y + (t / 3 - 1) * dil, xx = x + (t % 3 - 1) * dil;
-            if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
-            const size_t q = img + (size_t)yy * W + xx;
-            float iv;
-            if (CIN == 2) {
-                const float2 zv = reinterpret_cast<const float2 *>(inptr)[q];
-                iv = ci == 0 ? zv.x : zv.y;
-            } else {
-                iv = bf2f(reinterpret_cast<const uint16_t *>(inptr)[q * 32 + ci]);
-            }
-            acc[i] = fmaf(gv, iv, acc[i]);
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < PER; i++) {
-        const int c = threadIdx.x + 256 * i;
-        if (c < NT) part[(size_t)blockIdx.x * NT + c] = acc[i];
+    float *pp = part + (size_t)blockIdx.x * (COUT * CIN * 9 + COUT);
+    if (COUT == 2) {
+        pp[(0 * 32 + j) * 9 + t] = acc0;
+        pp[(1 * 32 + j) * 9 + t] = acc1;
+        if (tid < 2) pp[576 + tid] = bacc;
+    } else {
+        pp[(j * 2 + 0) * 9 + t] = acc0;
+        pp[(j * 2 + 1) * 9 + t] = acc1;
+        if (tid < 32) pp[576 + tid] = bacc;
     }
 }
 
-// Deterministic column sums of per-block partials: out[c] = sum_b part[b][c].
-__global__ void sur_reduce_kernel(const float *__restrict__ part, int nblocks, int ncols, float *__restrict__ out)
+int sur_dw_small_blocks(int B, int H, int W)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncols) return;
-    double s = 0;
-    for (int b = 0; b < nblocks; b++) s += part[(size_t)b * ncols + c];
-    out[c] = (float)s;
+    return B * ((H + kDsRows - 1) / kDsRows) * ((W + kDsSeg - 1) / kDsSeg);
+}
+int sur_dw_small_smem(int dil, int cout, int cin) { return (kDsSeg * cout + 3 * (kDsSeg + 2 * dil) * cin) * 4; }
+
+// Deterministic column sums of per-block partials: out[c] = sum_b part[b][c]
+// (+ out[c] when accumulate).  A block takes 32 columns; its 8 warps sum
+// every 8th partial in FP64, then the 8 sums are added in warp order.
+__global__ void __launch_bounds__(256) sur_reduce_kernel(const float *__restrict__ part, int nblocks, int ncols,
+                                                         float *__restrict__ out)
+{
+    __shared__ double s[8][32];
+    const int c = blockIdx.x * 32 + (threadIdx.x & 31), w = threadIdx.x >> 5;
+    double acc = 0;
+    if (c < ncols)
+        for (int b = w; b < nblocks; b += 8) acc += part[(size_t)b * ncols + c];
+    s[w][threadIdx.x & 31] = acc;
+    __syncthreads();
+    if (w == 0 && c < ncols) {
+        double t = s[0][threadIdx.x];
+        for (int k = 1; k < 8; k++) t += s[k][threadIdx.x];
+        out[c] = (float)t;
+    }
 }
 
 __global__ void sur_sum_kernel(const double *__restrict__ part, int n, double *__restrict__ out)

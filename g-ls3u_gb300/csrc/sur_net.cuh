@@ -25,12 +25,13 @@ struct SurNet {
     float2 *d_dh = nullptr, *d_out = nullptr, *d_y = nullptr;  // y = z + h7 before the renormalisation
     float *d_grad = nullptr, *d_m = nullptr, *d_v = nullptr, *d_part = nullptr;
     double *d_lpart = nullptr, *d_loss = nullptr;
-    int nb32 = 0, nbs = 0, adam_t = 0;
+    int nbs = 0, ndb = 0, adam_t = 0;  // blocks of the small weight-gradient and bias-gradient kernels
     int conv_ctas_per_sm = 0;  // cap of the tensor-core layers' CTAs per SM (0: none)
     int *d_err = nullptr;
     CUtensorMap map_fwd[7], map_bwd[7];        // conv inputs (box 128 + 2d)
     CUtensorMap map_fwd_out[7], map_bwd_out[7];  // conv outputs (32-pixel tiles)
     CUtensorMap map7;                            // the last layer's input a6
+    CUtensorMap map_g[2];                        // d_g[0], d_g[1] in 128-pixel boxes (weight gradients)
 
     int init(int batch, int width, int height, const int *dilations, bool train);
     void release();

@@ -179,6 +179,7 @@ def lib() -> ctypes.CDLL:
                                 c_int),
             "glsu_sur_conv32": ([c_void_p, c_void_p, c_int, c_int, c_int, c_int, fltp, fltp, c_int, c_void_p,
                                  c_void_p], c_int),
+            "glsu_sur_wgrad32": ([c_void_p, c_void_p, c_int, c_int, c_int, c_int, fltp, c_void_p], c_int),
             "glsu_dpra_set_surrogate": ([c_void_p, fltp, intp, c_int, c_int, c_double], c_int),
             "glsu_dpra_set_probe_overlap": ([c_void_p, c_int, c_int], c_int),
             "glsu_dpra_set_graph": ([c_void_p, c_int], c_int),
@@ -643,6 +644,16 @@ def conv32(d_in: int, d_out: int, batch: int, width: int, height: int, dilation:
                                 w.ctypes.data_as(fp), None if bb is None else bb.ctypes.data_as(fp), int(relu),
                                 ctypes.c_void_p(d_mask) if d_mask else None,
                                 ctypes.c_void_p(stream) if stream else None))
+
+
+def wgrad32(d_g: int, d_in: int, batch: int, width: int, height: int, dilation: int, stream: int = 0):
+    """Weight and bias gradient of one 32 -> 32 layer (BF16 NHWC device
+    buffers; synchronous): (dW [32][32][3][3], db [32])."""
+    out = np.empty(9216 + 32, np.float32)
+    check(lib().glsu_sur_wgrad32(ctypes.c_void_p(d_g), ctypes.c_void_p(d_in), batch, width, height, dilation,
+                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                 ctypes.c_void_p(stream) if stream else None))
+    return out[:9216].reshape(32, 32, 3, 3), out[9216:]
 
 
 class Surrogate:

@@ -431,6 +431,13 @@ int glsu_sur_gather(glsu_sur *h, const void *d_pool_x, const void *d_pool_t, int
  * may be NULL).  h_w: W[co][ci][3][3] (rounded to BF16), h_b: [32] or NULL. */
 int glsu_sur_conv32(const void *d_in, void *d_out, int batch, int width, int height, int dilation,
                     const float *h_w, const float *h_b, int relu, const void *d_mask, void *cuda_stream);
+/* Weight and bias gradient of one 32 -> 32 layer on caller BF16 NHWC buffers
+ * (synchronous): d_g the gradient w.r.t. the layer's output, d_in its input;
+ * h_dw receives 9216 + 32 floats, dW[co][ci][3][3] then db[co].  The
+ * weights on the tensor cores, the bias on CUDA cores, each summed over
+ * per-CTA partials in a fixed order. */
+int glsu_sur_wgrad32(const void *d_g, const void *d_in, int batch, int width, int height, int dilation,
+                     float *h_dw, void *cuda_stream);
 
 /* ---- DPRA surrogate form ---------------------------------------------------
  * FP32 DPRA handles: replace WFF2 by the surrogate (h_params, dilations as

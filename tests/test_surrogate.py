@@ -122,6 +122,38 @@ def test_tensor_core_conv_matches_oracle(glsu, shape, dil, relu, mask):
     assert (diff == 0).mean() > 0.99
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape,dil", [((1, 5, 40), 1), ((2, 36, 136), 16), ((1, 70, 300), 3), ((3, 17, 129), 24),
+                                       ((1, 64, 128), 64), ((2, 33, 257), 2)])
+def test_tensor_core_weight_gradient_matches_fp64(glsu, shape, dil):
+    """Weight and bias gradient of one 32 -> 32 layer: tcgen05 MMAs with
+    MN-major operands (rows of the gradient and the activation by TMA) and
+    the CUDA-core bias sums, against FP64 sums of the same BF16 values
+    (ragged widths, widths below one 128-pixel segment, dilations up to 64,
+    rows beyond the image)."""
+    torch = _torch()
+    rng = np.random.default_rng(dil * 10 + shape[2])
+    B, H, W = shape
+    gb = _bf16_bits(rng.uniform(-1, 1, (B, H, W, 32)).astype(np.float32))
+    ab = _bf16_bits(rng.uniform(-1, 1, (B, H, W, 32)).astype(np.float32))
+    dg = torch.from_numpy(gb.view(np.int16)).cuda()
+    da = torch.from_numpy(ab.view(np.int16)).cuda()
+    dw, db = glsu.wgrad32(dg.data_ptr(), da.data_ptr(), B, W, H, dil)
+    g, a = _from_bits(gb), _from_bits(ab)
+    ap = np.zeros((B, H + 2 * dil, W + 2 * dil, 32))
+    ap[:, dil:dil + H, dil:dil + W] = a
+    ref = np.zeros((32, 32, 3, 3))
+    for ky in range(3):
+        for kx in range(3):
+            sh = ap[:, ky * dil:ky * dil + H, kx * dil:kx * dil + W]
+            ref[:, :, ky, kx] = np.einsum("bhwo,bhwi->oi", g, sh)
+    rdb = g.sum((0, 1, 2))
+    e = np.abs(dw - ref).max() / np.abs(ref).max()
+    eb = np.abs(db - rdb).max() / np.abs(rdb).max()
+    print("wgrad32 %s d=%d: max |dW - ref| / max |ref| %.3g, bias %.3g" % (shape, dil, e, eb))
+    assert e < 1e-5 and eb < 1e-5
+
+
 def _net_case(glsu, B, H, W, seed):
     torch = _torch()
     rng = np.random.default_rng(seed)
