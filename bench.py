@@ -868,8 +868,8 @@ def probe_recall(glsu, SE, params, dil, size):
 
 def surrogate_training(glsu, torch, steps=20, warm=3, batch=16, crop=256):
     """Training throughput of the surrogate's own kernels: one step is the
-    forward pass, the loss, the backward pass (data gradients on the tensor
-    cores, weight gradients on the CUDA cores) and the Adam update, for a
+    forward pass, the loss, the backward pass (data and weight gradients of
+    the hidden layers on the tensor cores) and the Adam update, for a
     batch of `batch` crop x crop pairs already on the device; CUDA events on
     the handle's stream around `steps` steps after `warm`.  The forward pass
     alone is timed the same way, so the backward + update share follows."""
@@ -912,10 +912,11 @@ def surrogate_training(glsu, torch, steps=20, warm=3, batch=16, crop=256):
     return {"steps_per_s": 1e3 / ms_step, "ms_per_step": ms_step, "pairs_per_s": batch * 1e3 / ms_step,
             "batch": batch, "crop": crop, "ms_forward": ms_fwd, "ms_backward_and_update": ms_step - ms_fwd,
             "tflops": flops / (ms_step * 1e-3) / 1e12, "flops_per_step": flops,
-            "tensor_core_share_of_flops": 2 * 6 * hidden / (3 * fwd),
+            "tensor_core_share_of_flops": 3 * 6 * hidden / (3 * fwd),
             "loss_after": loss, "steps_timed": steps,
-            "what": "forward + loss + backward + Adam on device-resident synthetic pairs; hidden layers' "
-                    "forward and data gradients on tcgen05, weight gradients on CUDA cores (FP32)"}
+            "what": "forward + loss + backward + Adam on device-resident synthetic pairs; the hidden layers' "
+                    "forward, data gradients and weight gradients on tcgen05 (FP32 accumulation), layers 0 and 7 "
+                    "and the bias gradients on CUDA cores"}
 
 
 def run_ours(args, rank, world, local):

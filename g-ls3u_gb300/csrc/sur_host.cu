@@ -197,7 +197,7 @@ int SurNet::backward(const void *d_z, const void *d_target)
     GLSU_TRY(raise_smem_limit((const void *)sur_dw_small_kernel<32, 2>, sur_dw_small_smem(64, 32, 2)));
     sur_dw_small_kernel<2, 32><<<nbs, 288, sur_dw_small_smem(dil[7], 2, 32), stream>>>(d_dh, d_act[6], B, H, W,
                                                                                        dil[7], d_part);
-    sur_reduce_kernel<<<(kSurL7Params + 31) / 32, 256, 0, stream>>>(d_part, nbs, kSurL7Params,
+    sur_reduce_kernel<<<(kSurL7Params + 31) / 32, sur_reduce_threads(nbs), 0, stream>>>(d_part, nbs, kSurL7Params,
                                                                      d_grad + sur_layer_offset(7));
     sur_l7_bwd_kernel<<<g, 256, 0, stream>>>(d_dh, d_act[6], B, H, W, dil[7], d_w7r, d_g[0]);
     GLSU_CUDA_TRY(cudaGetLastError());
@@ -214,9 +214,9 @@ int SurNet::backward(const void *d_z, const void *d_target)
         wa.err = d_err;
         int nblk = 0;
         GLSU_TRY(launch_sur_wgrad(map_fwd[l], map_g[(6 - l) & 1], wa, stream, &nblk));
-        sur_reduce_kernel<<<9216 / 32, 256, 0, stream>>>(d_part, nblk, 9216, d_grad + sur_layer_offset(l));
+        sur_reduce_kernel<<<9216 / 32, sur_reduce_threads(nblk), 0, stream>>>(d_part, nblk, 9216, d_grad + sur_layer_offset(l));
         sur_db32_kernel<<<ndb, 256, 0, stream>>>(gl, npx, kSurDbPix, d_part);
-        sur_reduce_kernel<<<1, 256, 0, stream>>>(d_part, ndb, 32, d_grad + sur_layer_offset(l) + 9216);
+        sur_reduce_kernel<<<1, sur_reduce_threads(ndb), 0, stream>>>(d_part, ndb, 32, d_grad + sur_layer_offset(l) + 9216);
         GLSU_CUDA_TRY(cudaGetLastError());
         SurConvArgs a;
         a.B = B;
@@ -234,7 +234,7 @@ int SurNet::backward(const void *d_z, const void *d_target)
     // layer 0: weight gradient from g0 (in d_g[0] after six swaps) and the input
     sur_dw_small_kernel<32, 2><<<nbs, 288, sur_dw_small_smem(dil[0], 32, 2), stream>>>(d_g[0], z, B, H, W, dil[0],
                                                                                        d_part);
-    sur_reduce_kernel<<<(kSurL0Params + 31) / 32, 256, 0, stream>>>(d_part, nbs, kSurL0Params, d_grad);
+    sur_reduce_kernel<<<(kSurL0Params + 31) / 32, sur_reduce_threads(nbs), 0, stream>>>(d_part, nbs, kSurL0Params, d_grad);
     GLSU_CUDA_TRY(cudaGetLastError());
     return GLSU_OK;
 }
@@ -360,26 +360,19 @@ extern "C" int glsu_sur_gather(glsu_sur *h, const void *d_pool_x, const void *d_
 {
     if (!h || !d_pool_x || !d_pool_t || !h_crops || !d_x || !d_t) return fail(GLSU_ERR_INVALID, "null argument");
     SurNet &N = h->net;
-    std::vector<int> c4(4 * (size_t)N.B);
+    if (N.B > kSurMaxBatch) return fail(GLSU_ERR_UNSUPPORTED, "gather: at most 512 crops a batch");
+    SurCrops c;
     for (int b = 0; b < N.B; b++) {
         const int oy = h_crops[3 * b + 1], ox = h_crops[3 * b + 2];
         if (h_crops[3 * b] < 0 || h_crops[3 * b] >= pool_n || oy < 0 || ox < 0 || oy + N.H > pool_h ||
             ox + N.W > pool_w)
             return fail(GLSU_ERR_INVALID, "crop outside the pool image");
-        c4[4 * b] = h_crops[3 * b];
-        c4[4 * b + 1] = oy;
-        c4[4 * b + 2] = ox;
-        c4[4 * b + 3] = 0;
+        c.c[b] = make_int4(h_crops[3 * b], oy, ox, 0);
     }
-    int4 *d_c = nullptr;
-    GLSU_CUDA_TRY(cudaMallocAsync((void **)&d_c, c4.size() * 4, N.stream));
-    GLSU_CUDA_TRY(cudaMemcpyAsync(d_c, c4.data(), c4.size() * 4, cudaMemcpyHostToDevice, N.stream));
     const size_t n = (size_t)N.B * N.H * N.W;
     sur_gather_kernel<<<grid_for(n), 256, 0, N.stream>>>((const float2 *)d_pool_x, (const float2 *)d_pool_t, pool_h,
-                                                         pool_w, d_c, N.B, N.H, N.W, (float2 *)d_x, (float2 *)d_t);
+                                                         pool_w, c, N.B, N.H, N.W, (float2 *)d_x, (float2 *)d_t);
     GLSU_CUDA_TRY(cudaGetLastError());
-    GLSU_CUDA_TRY(cudaFreeAsync(d_c, N.stream));
-    GLSU_CUDA_TRY(cudaStreamSynchronize(N.stream));  // the host crop list may go away
     return GLSU_OK;
 }
 
@@ -465,9 +458,9 @@ int sur_wgrad32_once(const void *d_g, const void *d_in, int batch, int width, in
         int nblk = 0;
         rc = launch_sur_wgrad(tma, tmg, wa, s, &nblk);
         if (rc == GLSU_OK) {
-            sur_reduce_kernel<<<9216 / 32, 256, 0, s>>>(d_part, nblk, 9216, d_out);
+            sur_reduce_kernel<<<9216 / 32, sur_reduce_threads(nblk), 0, s>>>(d_part, nblk, 9216, d_out);
             sur_db32_kernel<<<ndb, 256, 0, s>>>((const uint16_t *)d_g, n, kSurDbPix, d_part);
-            sur_reduce_kernel<<<1, 256, 0, s>>>(d_part, ndb, 32, d_out + 9216);
+            sur_reduce_kernel<<<1, sur_reduce_threads(ndb), 0, s>>>(d_part, ndb, 32, d_out + 9216);
             if (cudaGetLastError() != cudaSuccess) rc = fail(GLSU_ERR_CUDA, "weight-gradient launch failed");
         }
     }

@@ -746,32 +746,45 @@ int launch_sur_wgrad(const CUtensorMap &tma, const CUtensorMap &tmg, const SurWg
 }
 
 // Bias gradient of a 32-channel layer: part[blk][c] = sum of g[p][c] over
-// the block's pixel range (8 pixel lanes per channel, then a fixed-order sum).
+// the block's pixel range.  Thread = (pixel lane 0..63, 8-channel group) with
+// 16-byte loads; the 64 lanes' sums are added in lane order.
 __global__ void __launch_bounds__(256) sur_db32_kernel(const uint16_t *__restrict__ g, size_t n, int per_block,
                                                        float *__restrict__ part)
 {
-    __shared__ float s[8][33];
-    const int c = threadIdx.x & 31, pl = threadIdx.x >> 5;
+    __shared__ float s[64][33];
+    const int cg = threadIdx.x & 3, pl = threadIdx.x >> 2;
     const size_t p0 = (size_t)blockIdx.x * per_block;
-    float acc = 0.f;
-    for (size_t p = p0 + pl; p < p0 + per_block && p < n; p += 8) acc += bf2f(g[p * 32 + c]);
-    s[pl][c] = acc;
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (size_t p = p0 + pl; p < p0 + per_block && p < n; p += 64) {
+        float v[8];
+        unpack8(reinterpret_cast<const uint4 *>(g + p * 32)[cg], v);
+#pragma unroll
+        for (int i = 0; i < 8; i++) acc[i] += v[i];
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) s[pl][cg * 8 + i] = acc[i];
     __syncthreads();
-    if (pl == 0) {
-        float t = s[0][c];
-        for (int k = 1; k < 8; k++) t += s[k][c];
-        part[(size_t)blockIdx.x * 32 + c] = t;
+    if (threadIdx.x < 32) {
+        float t = s[0][threadIdx.x];
+        for (int k = 1; k < 64; k++) t += s[k][threadIdx.x];
+        part[(size_t)blockIdx.x * 32 + threadIdx.x] = t;
     }
 }
 
 // Layer 0 (g: BF16 32 channels, input z: complex) and layer 7 (g = dh:
 // complex, input a6: BF16 32 channels) on CUDA cores: a block takes 8 rows
 // of one 64-pixel segment, staging per row the gradient and the three input
-// rows (with the dilated halo) in shared memory as FP32; thread c < 288
-// owns (tap t = c / 32, j = c % 32) and accumulates the two weights that
-// pair j with both channels of the 2-channel side.  part[blk][co][ci][t]
-// then the biases part[blk][576 + co].
+// rows (with the dilated halo) in shared memory as FP32 (16-byte loads of
+// 8 BF16 channels); thread c < 288 owns (tap t = c / 32, j = c % 32) and
+// accumulates the two weights that pair j with both channels of the
+// 2-channel side.  part[blk][co][ci][t] then the biases part[blk][576 + co].
 constexpr int kDsSeg = 64, kDsRows = 8;
+
+__device__ __forceinline__ void store8(float *d, const float *v)
+{
+    reinterpret_cast<float4 *>(d)[0] = make_float4(v[0], v[1], v[2], v[3]);
+    reinterpret_cast<float4 *>(d)[1] = make_float4(v[4], v[5], v[6], v[7]);
+}
 
 template <int COUT, int CIN>
 __global__ void __launch_bounds__(288) sur_dw_small_kernel(const void *__restrict__ gptr,
@@ -792,48 +805,66 @@ __global__ void __launch_bounds__(288) sur_dw_small_kernel(const void *__restric
     const int tid = threadIdx.x, t = tid >> 5, j = tid & 31;
     const int ky = t / 3, kx = t % 3;
     float acc0 = 0.f, acc1 = 0.f, bacc = 0.f;
+    const float zero8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int yy = 0; yy < kDsRows; yy++) {
         const int y = by * kDsRows + yy;
         if (y >= H) break;
         __syncthreads();
-        for (int e = tid; e < kDsSeg * COUT; e += 288) {
-            const int px = e / COUT, c = e % COUT, x = x0 + px;
-            float v = 0.f;
-            if (x < W) {
-                const size_t p = ((size_t)b * H + y) * W + x;
-                if (COUT == 32) v = bf2f(reinterpret_cast<const uint16_t *>(gptr)[p * 32 + c]);
-                else v = c == 0 ? reinterpret_cast<const float2 *>(gptr)[p].x
-                                : reinterpret_cast<const float2 *>(gptr)[p].y;
+        if (COUT == 32) {  // g0: 4 x 16 bytes a pixel
+            for (int e = tid; e < kDsSeg * 4; e += 288) {
+                const int px = e >> 2, c8 = e & 3, x = x0 + px;
+                float v[8];
+                if (x < W) unpack8(reinterpret_cast<const uint4 *>(gptr)[(((size_t)b * H + y) * W + x) * 4 + c8], v);
+                store8(gs + px * 32 + c8 * 8, x < W ? v : zero8);
             }
-            gs[e] = v;
+        } else {  // dh: one complex a pixel
+            for (int px = tid; px < kDsSeg; px += 288) {
+                const int x = x0 + px;
+                float2 v = make_float2(0.f, 0.f);
+                if (x < W) v = reinterpret_cast<const float2 *>(gptr)[((size_t)b * H + y) * W + x];
+                gs[px * 2] = v.x;
+                gs[px * 2 + 1] = v.y;
+            }
         }
-        for (int e = tid; e < 3 * SW * CIN; e += 288) {
-            const int c = e % CIN, rest = e / CIN, px = rest % SW, r = rest / SW;
-            const int ys = y + (r - 1) * dil, xs = x0 - dil + px;
-            float v = 0.f;
-            if (ys >= 0 && ys < H && xs >= 0 && xs < W) {
-                const size_t q = ((size_t)b * H + ys) * W + xs;
-                if (CIN == 32) v = bf2f(reinterpret_cast<const uint16_t *>(inptr)[q * 32 + c]);
-                else v = c == 0 ? reinterpret_cast<const float2 *>(inptr)[q].x
-                                : reinterpret_cast<const float2 *>(inptr)[q].y;
+        if (CIN == 32) {  // a6: 4 x 16 bytes a pixel
+            for (int e = tid; e < 3 * SW * 4; e += 288) {
+                const int c8 = e & 3, rest = e >> 2, px = rest % SW, r = rest / SW;
+                const int ys = y + (r - 1) * dil, xs = x0 - dil + px;
+                const bool in = ys >= 0 && ys < H && xs >= 0 && xs < W;
+                float v[8];
+                if (in) unpack8(reinterpret_cast<const uint4 *>(inptr)[(((size_t)b * H + ys) * W + xs) * 4 + c8], v);
+                store8(is + (r * SW + px) * 32 + c8 * 8, in ? v : zero8);
             }
-            is[e] = v;
+        } else {  // z: one complex a pixel
+            for (int e = tid; e < 3 * SW; e += 288) {
+                const int px = e % SW, r = e / SW;
+                const int ys = y + (r - 1) * dil, xs = x0 - dil + px;
+                float2 v = make_float2(0.f, 0.f);
+                if (ys >= 0 && ys < H && xs >= 0 && xs < W)
+                    v = reinterpret_cast<const float2 *>(inptr)[((size_t)b * H + ys) * W + xs];
+                is[(r * SW + px) * 2] = v.x;
+                is[(r * SW + px) * 2 + 1] = v.y;
+            }
         }
         __syncthreads();
         const float *ir = is + (size_t)(ky * SW + kx * dil) * CIN;
         if (COUT == 2) {  // layer 7: j = ci, the two output channels
+#pragma unroll 8
             for (int px = 0; px < kDsSeg; px++) {
                 const float iv = ir[px * CIN + j];
-                acc0 = fmaf(gs[px * 2], iv, acc0);
-                acc1 = fmaf(gs[px * 2 + 1], iv, acc1);
+                const float2 gv = reinterpret_cast<const float2 *>(gs)[px];
+                acc0 = fmaf(gv.x, iv, acc0);
+                acc1 = fmaf(gv.y, iv, acc1);
             }
             if (tid < 2)
                 for (int px = 0; px < kDsSeg; px++) bacc += gs[px * 2 + tid];
         } else {  // layer 0: j = co, the two input channels
+#pragma unroll 8
             for (int px = 0; px < kDsSeg; px++) {
                 const float gv = gs[px * 32 + j];
-                acc0 = fmaf(gv, ir[px * 2], acc0);
-                acc1 = fmaf(gv, ir[px * 2 + 1], acc1);
+                const float2 iv = reinterpret_cast<const float2 *>(ir)[px];
+                acc0 = fmaf(gv, iv.x, acc0);
+                acc1 = fmaf(gv, iv.y, acc1);
             }
             if (tid < 32)
                 for (int px = 0; px < kDsSeg; px++) bacc += gs[px * 32 + tid];
@@ -857,25 +888,29 @@ int sur_dw_small_blocks(int B, int H, int W)
 }
 int sur_dw_small_smem(int dil, int cout, int cin) { return (kDsSeg * cout + 3 * (kDsSeg + 2 * dil) * cin) * 4; }
 
-// Deterministic column sums of per-block partials: out[c] = sum_b part[b][c]
-// (+ out[c] when accumulate).  A block takes 32 columns; its 8 warps sum
-// every 8th partial in FP64, then the 8 sums are added in warp order.
-__global__ void __launch_bounds__(256) sur_reduce_kernel(const float *__restrict__ part, int nblocks, int ncols,
-                                                         float *__restrict__ out)
+// Deterministic column sums of per-block partials: out[c] = sum_b part[b][c].
+// A block takes 32 columns; its warps (blockDim.x / 32 of them) sum every
+// nw-th partial in FP64, then the warps' sums are added in warp order.
+__global__ void __launch_bounds__(1024) sur_reduce_kernel(const float *__restrict__ part, int nblocks, int ncols,
+                                                          float *__restrict__ out)
 {
-    __shared__ double s[8][32];
-    const int c = blockIdx.x * 32 + (threadIdx.x & 31), w = threadIdx.x >> 5;
+    __shared__ double s[32][32];
+    const int nw = blockDim.x >> 5, w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int c = blockIdx.x * 32 + l;
     double acc = 0;
     if (c < ncols)
-        for (int b = w; b < nblocks; b += 8) acc += part[(size_t)b * ncols + c];
-    s[w][threadIdx.x & 31] = acc;
+        for (int b = w; b < nblocks; b += nw) acc += part[(size_t)b * ncols + c];
+    s[w][l] = acc;
     __syncthreads();
     if (w == 0 && c < ncols) {
-        double t = s[0][threadIdx.x];
-        for (int k = 1; k < 8; k++) t += s[k][threadIdx.x];
+        double t = s[0][l];
+        for (int k = 1; k < nw; k++) t += s[k][l];
         out[c] = (float)t;
     }
 }
+
+// Threads of a reduction: more warps when there are many partials.
+inline int sur_reduce_threads(int nblocks) { return nblocks >= 1024 ? 1024 : nblocks >= 256 ? 512 : 256; }
 
 __global__ void sur_sum_kernel(const double *__restrict__ part, int n, double *__restrict__ out)
 {
@@ -946,15 +981,21 @@ __global__ void sur_pack_kernel(const float *__restrict__ master, uint16_t *__re
 }
 
 // Gather training crops: x[b] = pool_x[idx[b]][oy:oy+h, ox:ox+w] (complex),
-// same for the target.
+// same for the target.  The crop list travels as a kernel parameter, so a
+// step needs no copy and no synchronisation.
+constexpr int kSurMaxBatch = 512;
+struct SurCrops {
+    int4 c[kSurMaxBatch];  // (pool index, oy, ox, unused)
+};
+
 __global__ void sur_gather_kernel(const float2 *__restrict__ px, const float2 *__restrict__ pt, int PH, int PW,
-                                  const int4 *__restrict__ crops, int B, int h, int w, float2 *__restrict__ x,
-                                  float2 *__restrict__ t)
+                                  const __grid_constant__ SurCrops crops, int B, int h, int w,
+                                  float2 *__restrict__ x, float2 *__restrict__ t)
 {
     const size_t n = (size_t)B * h * w;
     for (size_t p = (size_t)blockIdx.x * 256 + threadIdx.x; p < n; p += (size_t)gridDim.x * 256) {
         const int xx = (int)(p % w), yy = (int)((p / w) % h), b = (int)(p / ((size_t)w * h));
-        const int4 c = crops[b];  // (pool index, oy, ox, unused)
+        const int4 c = crops.c[b];
         const size_t src = ((size_t)c.x * PH + c.y + yy) * PW + c.z + xx;
         x[p] = px[src];
         t[p] = pt[src];

@@ -423,7 +423,9 @@ int glsu_sur_adam(glsu_sur *h, float lr, float beta1, float beta2, float eps);
 int glsu_sur_output(glsu_sur *h, void *h_out);
 /* Training crops: for b < batch, copy the width x height window at
  * (row h_crops[3b+1], col h_crops[3b+2]) of pool image h_crops[3b] (pool:
- * complex [pool_n][pool_h][pool_w], input and target) into d_x / d_t. */
+ * complex [pool_n][pool_h][pool_w], input and target) into d_x / d_t.
+ * Enqueued on the handle's stream (the crop list is passed by value; at
+ * most 512 crops). */
 int glsu_sur_gather(glsu_sur *h, const void *d_pool_x, const void *d_pool_t, int pool_n, int pool_h, int pool_w,
                     const int *h_crops, void *d_x, void *d_t);
 /* One 32 -> 32 tensor-core layer on caller BF16 NHWC buffers (synchronous):
