@@ -762,12 +762,12 @@ def batched_mix(glsu, torch, seed, per_size=16, fmin=10, fmax=100):
             if batched:
                 b.run([bufs[k].data_ptr() if act[k] else None for k in range(len(specs))], glsu.F32)
                 b.sync()
-            else:
+            else:  # the handles share the legacy stream: one frame after another, no host round trips
                 for k, d in enumerate(hs):
                     if act[k]:
                         d.per_frame_device(bufs[k].data_ptr(), glsu.F32)
                         d.update_ref_phi()
-                        torch.cuda.synchronize()
+                torch.cuda.synchronize()
             total += time.perf_counter() - t0
         phases = [d.get(glsu.PHI_REF) for d in hs]
         if b is not None:
