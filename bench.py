@@ -199,8 +199,9 @@ def dist_init():
     if world > 1:
         import torch
         import torch.distributed as dist
+        from datetime import timedelta
         backend = "nccl" if torch.cuda.is_available() else "gloo"
-        dist.init_process_group(backend)
+        dist.init_process_group(backend, timeout=timedelta(minutes=30))
     return rank, world, local
 
 
@@ -936,7 +937,10 @@ def run_ours(args, rank, world, local):
     # wrapped index would feed frame 0 after frame k, a k-frame phase jump)
     nfr = args.warmup + args.steps + STAGE_FRAMES + 1
     frames, phi0, _ = synth.sequence(size, size, nfr, seed=seed)
-    extras = not args.frames_only and rank == 0  # the legs beside the headline run on rank 0
+    # the legs beside the headline run in the single-GPU run only (rank 0 of
+    # one): under torchrun the other ranks would wait for them at the first
+    # collective
+    extras = not args.frames_only and rank == 0 and world == 1
 
     wfr = batched = prec1 = large = training = None
     if extras:
