@@ -383,15 +383,22 @@ def copy_times(torch, size, reps=20):
 
 def e2e_sequence(glsu, torch, make_handle, hframes, args, stream, flush, world):
     """Frames/s end to end through glsu_dpra_sequence, the public sequence
-    call: after W warm-up frames on a fresh handle (reference phase phi0), one
-    call runs E2E_FRAMES pinned host frames, uploads, compute and dphi
-    downloads overlapped on the handle's copy streams, and returns when every
-    output is on the host; wall clock around that call, max over ranks, the
-    median of E2E_RUNS runs."""
+    call: after one untimed pass over the pinned buffers, and W warm-up
+    frames on a fresh handle (reference phase phi0), one call runs
+    E2E_FRAMES pinned host frames, uploads, compute and dphi downloads
+    overlapped on the handle's copy streams, and returns when every output is
+    on the host; wall clock around that call, max over ranks, the median of
+    E2E_RUNS runs."""
     W = args.warmup
     K = hframes.shape[0] - W
     hout = torch.empty(hframes.shape[1:], dtype=torch.float32).unsqueeze(0).expand(K, -1, -1).contiguous()
     hout = hout.pin_memory()
+    # one untimed pass over the whole pinned input and output first: the
+    # first DMA through freshly pinned pages is slower (about 1300 against
+    # 1700 frames/s for the surrogate form), a one-time cost of the buffers
+    d = make_handle()
+    d.sequence_ptr(K, hframes[W].data_ptr(), glsu.F32, hout.data_ptr())
+    d.close()
     vals = []
     for _ in range(E2E_RUNS):
         d = make_handle()
