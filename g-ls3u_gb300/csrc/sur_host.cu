@@ -190,7 +190,7 @@ int SurNet::backward(const void *d_z, const void *d_target)
     const int g = rows_grid();
     GLSU_TRY(last(z, nullptr, d_y));
     sur_l7_loss_kernel<<<kSurPixBlocks, 256, 0, stream>>>(d_y, (const float2 *)d_target, (size_t)B * H * W, d_out,
-                                                          d_dh, d_lpart);
+                                                          d_dh, d_lpart, loss_scale);
     sur_sum_kernel<<<1, 32, 0, stream>>>(d_lpart, kSurPixBlocks, d_loss);
     // layer 7: weight gradient and dL/da6 (masked)
     GLSU_TRY(raise_smem_limit((const void *)sur_dw_small_kernel<2, 32>, sur_dw_small_smem(64, 2, 32)));
@@ -337,6 +337,14 @@ extern "C" int glsu_sur_backward(glsu_sur *h, const void *d_z, const void *d_tar
                 cudaMemcpyAsync(h_grad, h->net.d_grad, kSurParams * 4, cudaMemcpyDeviceToHost, h->net.stream));
         GLSU_TRY(h->net.check_error());
     }
+    return GLSU_OK;
+}
+
+extern "C" int glsu_sur_set_loss_scale(glsu_sur *h, float scale)
+{
+    if (!h) return fail(GLSU_ERR_INVALID, "null handle");
+    if (!(scale > 0.f) || !std::isfinite(scale)) return fail(GLSU_ERR_INVALID, "loss scale must be positive");
+    h->net.loss_scale = scale;
     return GLSU_OK;
 }
 

@@ -512,13 +512,14 @@ __global__ void __launch_bounds__(256) sur_l0_kernel(const float2 *__restrict__ 
 
 // Training loss of the last layer's output: from y = z + conv7(a6) (written
 // by the tensor-core last layer), out = y / |y| (the same rounding as the
-// inference epilogue), per pixel loss wgt |out - t|^2 with wgt = min(|target|,
-// 1) and t = target / |target|, the gradient dL/dh7 of the mean loss into dh
+// inference epilogue), per pixel loss wgt |out - t|^2 with wgt =
+// min(wscale |target|, 1) and t = target / |target|, the gradient dL/dh7 of
+// the mean loss into dh
 // and per-block loss sums (fixed order) into part.
 __global__ void __launch_bounds__(256) sur_l7_loss_kernel(const float2 *__restrict__ yv,
                                                           const float2 *__restrict__ target, size_t n,
                                                           float2 *__restrict__ out, float2 *__restrict__ dh,
-                                                          double *__restrict__ part)
+                                                          double *__restrict__ part, float wscale)
 {
     __shared__ double red[256];
     const int tid = threadIdx.x;
@@ -531,7 +532,7 @@ __global__ void __launch_bounds__(256) sur_l7_loss_kernel(const float2 *__restri
         out[p] = make_float2(orr, oii);
         const float2 tv = target[p];
         const float tn = sqrtf(tv.x * tv.x + tv.y * tv.y);
-        const float wgt = fminf(tn, 1.f);
+        const float wgt = fminf(tn * wscale, 1.f);
         const float ti = tn > 1e-20f ? 1.f / tn : 0.f;
         const float er = orr - tv.x * ti, ei = oii - tv.y * ti;
         lsum += (double)(wgt * (er * er + ei * ei)) * inv_n;

@@ -27,6 +27,7 @@ struct SurNet {
     double *d_lpart = nullptr, *d_loss = nullptr;
     int nbs = 0, ndb = 0, adam_t = 0;  // blocks of the small weight-gradient and bias-gradient kernels
     int conv_ctas_per_sm = 0;  // cap of the tensor-core layers' CTAs per SM (0: none)
+    float loss_scale = 1.f;    // training loss weight min(loss_scale |target|, 1)
     int *d_err = nullptr;
     CUtensorMap map_fwd[7], map_bwd[7];        // conv inputs (box 128 + 2d)
     CUtensorMap map_fwd_out[7], map_bwd_out[7];  // conv outputs (32-pixel tiles)

@@ -174,6 +174,7 @@ def lib() -> ctypes.CDLL:
             "glsu_sur_forward": ([c_void_p, c_void_p, c_void_p], c_int),
             "glsu_sur_backward": ([c_void_p, c_void_p, c_void_p, dblp, fltp], c_int),
             "glsu_sur_adam": ([c_void_p, c_float, c_float, c_float, c_float], c_int),
+            "glsu_sur_set_loss_scale": ([c_void_p, c_float], c_int),
             "glsu_sur_output": ([c_void_p, c_void_p], c_int),
             "glsu_sur_gather": ([c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, intp, c_void_p, c_void_p],
                                 c_int),
@@ -704,6 +705,10 @@ class Surrogate:
 
     def adam(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8):
         check(lib().glsu_sur_adam(self._h, lr, beta1, beta2, eps))
+
+    def set_loss_scale(self, scale: float):
+        """Training loss weight of a pixel: min(scale |target|, 1)."""
+        check(lib().glsu_sur_set_loss_scale(self._h, float(scale)))
 
     def output(self) -> np.ndarray:
         o = np.empty((self.batch, self.height, self.width), np.complex64)

@@ -163,16 +163,20 @@ def one_cycle(step: int, steps: int, peak: float, warm: float = 0.25) -> float:
 
 
 def train(pools, steps: int, batch: int = 16, crop: int = 256, lr: float = 1.5e-3, dilations=DILATIONS,
-          seed: int = 0, init=None, log_every: int = 500, log=print, time_budget: float = 0.0):
+          seed: int = 0, init=None, log_every: int = 500, log=print, time_budget: float = 0.0,
+          loss_scale: float = 1.0):
     """Train on a list of (x, t) pools, alternating between them; returns the
     FP32 parameters and a list of (step, loss).  With time_budget > 0 the
     learning-rate schedule runs over elapsed seconds instead of steps and
-    training stops when the budget is spent (at most `steps` steps)."""
+    training stops when the budget is spent (at most `steps` steps).  A
+    pixel's loss weight is min(loss_scale |target|, 1)."""
     torch = _torch()
     import glsu
     rng = np.random.default_rng(seed)
     net = glsu.Surrogate(batch, crop, crop, dilations, training=True)
     net.params = init_params(seed) if init is None else np.asarray(init, np.float32)
+    if loss_scale != 1.0:
+        net.set_loss_scale(loss_scale)
     xb = torch.empty((batch, crop, crop), dtype=torch.complex64, device="cuda")
     tb = torch.empty_like(xb)
     hist = []
@@ -224,12 +228,13 @@ def main_large(a):
     print("pool: %d training frames of %d^2, generated in %.1f s" % (pool[0].shape[0], a.size, time.time() - t0),
           flush=True)
     params, hist = train([pool], a.steps, a.batch, lr=a.lr, dilations=dil, seed=a.seed, time_budget=a.time_budget,
-                         log=lambda m: print(m, flush=True))
+                         log=lambda m: print(m, flush=True), loss_scale=a.loss_scale)
     r = evaluate(params, *held, dilations=dil, limit=8)
     print("held-out phase RMSE vs WFF2 at %d^2: %.4f (identity %.4f)" % (a.size, r[0], r[1]), flush=True)
     np.savez(a.out, params=params, dilations=np.array(dil, np.int32), wff=np.array(wff), radius=a.radius,
              steps=int(hist[-1][0]) if hist else 0, batch=a.batch, lr=a.lr, seed=a.seed, size=a.size,
-             pairs=pool[0].shape[0], rmse_heldout=r[0], rmse_identity=r[1], loss_history=np.array(hist))
+             pairs=pool[0].shape[0], rmse_heldout=r[0], rmse_identity=r[1], loss_history=np.array(hist),
+             loss_scale=a.loss_scale)
     print("saved", a.out)
 
 
@@ -243,6 +248,7 @@ def main(argv=None):
     ap.add_argument("--seqs1024", type=int, default=20, help="1024^2 sequences (20 frames each)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--time-budget", type=float, default=0.0, help="seconds of training (schedule over time)")
+    ap.add_argument("--loss-scale", type=float, default=1.0, help="pixel loss weight min(scale |WFF2|, 1)")
     ap.add_argument("--size", type=int, default=0,
                     help="large deployment size: train on pairs from sequences of that size only (GPU-made frames)")
     ap.add_argument("--wff", default=",".join(str(v) for v in WFF), help="WFF2 parameters (with --size)")
@@ -264,7 +270,7 @@ def main(argv=None):
     print("pools: %d + %d training frames, generated in %.1f s" % (small[0].shape[0], big[0].shape[0],
                                                                    time.time() - t0), flush=True)
     params, hist = train([big, small], a.steps, a.batch, lr=a.lr, seed=a.seed, time_budget=a.time_budget,
-                         log=lambda m: print(m, flush=True))
+                         log=lambda m: print(m, flush=True), loss_scale=a.loss_scale)
     r_small = evaluate(params, *held_small)
     r_big = evaluate(params, *held_big)
     print("held-out phase RMSE vs WFF2: 256^2 %.4f (identity %.4f), 1024^2 %.4f (identity %.4f)"
@@ -273,7 +279,8 @@ def main(argv=None):
              radius=RADIUS, steps=int(hist[-1][0]) if hist else 0, batch=a.batch, lr=a.lr, seed=a.seed,
              pairs=small[0].shape[0] + 16 * big[0].shape[0],
              rmse_heldout_256=r_small[0], rmse_heldout_1024=r_big[0],
-             rmse_identity_256=r_small[1], rmse_identity_1024=r_big[1], loss_history=np.array(hist))
+             rmse_identity_256=r_small[1], rmse_identity_1024=r_big[1], loss_history=np.array(hist),
+             loss_scale=a.loss_scale)
     print("saved", a.out)
 
 

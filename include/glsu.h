@@ -417,6 +417,10 @@ int glsu_sur_forward(glsu_sur *h, const void *d_z, void *d_out);
  * and h_grad (param_count floats) are optional; when given, the call
  * synchronises. */
 int glsu_sur_backward(glsu_sur *h, const void *d_z, const void *d_target, double *loss, float *h_grad);
+/* Training loss weight of a pixel: min(scale |target|, 1) (scale 1 by
+ * default; scale 10 weighs every pixel with |WFF2| >= 0.1 fully, the pixels
+ * the probe judges). */
+int glsu_sur_set_loss_scale(glsu_sur *h, float scale);
 /* One Adam step with the gradient of the last glsu_sur_backward. */
 int glsu_sur_adam(glsu_sur *h, float lr, float beta1, float beta2, float eps);
 /* Training handles: the output of the last glsu_sur_backward (synchronous). */

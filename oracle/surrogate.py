@@ -9,7 +9,7 @@ parameter gradient can be checked:
     a_l = relu(conv(a_{l-1}, W_l, b_l, d_l))   l = 1..6, 32 -> 32
     y   = x + conv(a6, W7, b7, d7)          32 -> 2
     out = y / |y|
-    loss = mean_p  min(|t|, 1) |out - t/|t||^2
+    loss = mean_p  min(s |t|, 1) |out - t/|t||^2   (s = 1 by default)
 
 conv is a 3x3 convolution with dilation d and zero padding.  With
 ``bf16=True`` the oracle rounds (to nearest even) where the CUDA path stores
@@ -122,14 +122,15 @@ def forward(params, z, dil, bf16_emul=True):
     return out[..., 0] + 1j * out[..., 1], dict(x=x, acts=acts, y=y, n=n, out=out)
 
 
-def loss_and_grad(params, z, target, dil, bf16_emul=True):
-    """(loss, flat gradient FP64) of the training loss."""
+def loss_and_grad(params, z, target, dil, bf16_emul=True, wscale=1.0):
+    """(loss, flat gradient FP64) of the training loss (pixel weight
+    min(wscale |target|, 1))."""
     r = bf16 if bf16_emul else (lambda a: np.asarray(a, np.float64))
     layers = unpack(params)
     _, c = forward(params, z, dil, bf16_emul)
     t = np.stack([np.real(target), np.imag(target)], -1).astype(np.float64)
     tn = np.sqrt((t ** 2).sum(-1, keepdims=True))
-    wgt = np.minimum(tn, 1.0)
+    wgt = np.minimum(wscale * tn, 1.0)
     tt = t / np.where(tn > 0, tn, 1.0)
     out, n = c["out"], c["n"]
     npix = out.shape[0] * out.shape[1] * out.shape[2]

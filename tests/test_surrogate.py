@@ -25,13 +25,15 @@ def test_bf16_rounding_is_nearest_even():
     assert r[5] == 0.0
 
 
-def test_oracle_gradient_matches_finite_differences():
+@pytest.mark.parametrize("wscale", [1.0, 10.0])
+def test_oracle_gradient_matches_finite_differences(wscale):
     rng = np.random.default_rng(0)
     p = S.init_params(1, scale_last=1.0).astype(np.float64)
     z = np.exp(1j * rng.uniform(-np.pi, np.pi, (1, 9, 11)))
-    t = 0.8 * np.exp(1j * rng.uniform(-np.pi, np.pi, (1, 9, 11)))
+    # target magnitudes on both sides of 1 / wscale
+    t = rng.uniform(0.02, 1.2, (1, 9, 11)) * np.exp(1j * rng.uniform(-np.pi, np.pi, (1, 9, 11)))
     dil = [1, 2, 1, 3, 1, 2, 1, 1]
-    loss, g = S.loss_and_grad(p, z, t, dil, bf16_emul=False)
+    loss, g = S.loss_and_grad(p, z, t, dil, bf16_emul=False, wscale=wscale)
     idx = rng.choice(p.size, 40, replace=False)
     # include every layer's bias and one weight of each layer
     offs = np.cumsum([0] + [co * ci * 9 + co for co, ci in S.SIZES])
@@ -41,8 +43,8 @@ def test_oracle_gradient_matches_finite_differences():
         pp, pm = p.copy(), p.copy()
         pp[k] += eps
         pm[k] -= eps
-        lp, _ = S.loss_and_grad(pp, z, t, dil, bf16_emul=False)
-        lm, _ = S.loss_and_grad(pm, z, t, dil, bf16_emul=False)
+        lp, _ = S.loss_and_grad(pp, z, t, dil, bf16_emul=False, wscale=wscale)
+        lm, _ = S.loss_and_grad(pm, z, t, dil, bf16_emul=False, wscale=wscale)
         fd = (lp - lm) / (2 * eps)
         assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(g[k])) + 1e-9, (k, fd, g[k])
 
@@ -165,19 +167,23 @@ def _net_case(glsu, B, H, W, seed):
 
 
 @pytest.mark.gpu
-def test_network_forward_and_gradients_match_oracle(glsu):
+@pytest.mark.parametrize("wscale", [1.0, 10.0])
+def test_network_forward_and_gradients_match_oracle(glsu, wscale):
     """Every parameter gradient of the CUDA training pass (tensor-core
-    forward, backward-data with the flipped weights, CUDA-core weight
-    gradients) against the oracle with the same BF16 rounding points."""
+    forward, backward-data with the flipped weights, tensor-core weight
+    gradients of the hidden layers) against the oracle with the same BF16
+    rounding points, for two loss weightings."""
     B, H, W = 2, 36, 136
     torch, p, z, t = _net_case(glsu, B, H, W, 7)
     net = glsu.Surrogate(B, W, H, DIL, training=True)
     net.params = p
+    if wscale != 1.0:
+        net.set_loss_scale(wscale)
     dz, dt = torch.from_numpy(z).cuda(), torch.from_numpy(t).cuda()
     loss, g = net.backward(dz.data_ptr(), dt.data_ptr(), want_grad=True)
     out = net.output()
     rout, cache = S.forward(p, z.astype(np.complex128), DIL)
-    rloss, rg = S.loss_and_grad(p, z.astype(np.complex128), t.astype(np.complex128), DIL)
+    rloss, rg = S.loss_and_grad(p, z.astype(np.complex128), t.astype(np.complex128), DIL, wscale=wscale)
     d = np.abs(out - rout)
     # out = y/|y|: where |y| is small a one-ulp BF16 difference upstream turns the direction
     firm = cache["n"][..., 0] >= 0.05
