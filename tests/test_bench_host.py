@@ -79,3 +79,25 @@ def test_fft_sweep_flop_count():
     import bench
     f = bench.fft_sweep_flops(1024, 21, 21, 1280, 1024)
     assert abs(f - 1024 * 21 * (44 * 5 * 1280 * 10.321928094887362 + 21 * 16 * 1280)) < 1e3
+
+
+def test_recall_cases_and_summary():
+    """Host side of the probe-recall legs: the carrier ramp covers the centre
+    quarter only, the reversed network negates exactly the last layer, and
+    the summary counts bad and caught tiles."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "g-ls3u_gb300"))
+    from glsu import surrogate_eval as SE
+    from glsu import train_surrogate as T
+    m = SE.carrier_region(64, slope=0.9)
+    assert m[:16].max() == 0 and m[48:].max() == 0 and m[:, :16].max() == 0
+    assert np.allclose(np.diff(m[32, 16:48]), 0.9)
+    p = T.init_params(3)
+    r = SE.reversed_residual(p)
+    n_last = T.LAYER_SIZES[-1][0] * T.LAYER_SIZES[-1][1] * 9 + T.LAYER_SIZES[-1][0]
+    assert np.array_equal(r[:-n_last], p[:-n_last]) and np.array_equal(r[-n_last:], -p[-n_last:])
+    recs = [{"seed": 1, "frame": 2, "rmse": 0.01, "max": 1.0, "rmse_network_only": 0.02, "max_network_only": 1.0,
+             "rmse_without_network": 0.6, "max_without_network": 3.0, "tiles_flagged": 1, "tiles": 16,
+             "tiles_bad": 2, "tiles_bad_flagged": 1, "tiles_good_flagged": 0, "bad_tile_rmse": [0.06, 0.1]}]
+    s = SE.summarise(recs, 0.05)
+    assert s["tiles_over_tol"] == 2 and s["probe_recall"] == 0.5 and s["tiles_recomputed_fraction"] == 1 / 16
