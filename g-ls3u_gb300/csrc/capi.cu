@@ -1245,7 +1245,7 @@ static int batch_enqueue(glsu_dpra_batch *b, const std::vector<char> &active, co
                          int img_type)
 {
     size_t ne = 0;
-    cudaEvent_t fork, e;
+    cudaEvent_t fork = nullptr, e = nullptr;
     GLSU_TRY(batch_event(b, ne++, &fork));
     GLSU_CUDA_TRY(cudaEventRecord(fork, b->stream));
     // stage 1: least squares and row pass (and the direct column sweep)
@@ -1264,7 +1264,7 @@ static int batch_enqueue(glsu_dpra_batch *b, const std::vector<char> &active, co
         GLSU_CUDA_TRY(cudaStreamWaitEvent(b->stream, e, 0));
     }
     // stage 2: the FFT column sweeps, one persistent launch per length
-    cudaEvent_t pre;
+    cudaEvent_t pre = nullptr;
     GLSU_TRY(batch_event(b, ne++, &pre));
     GLSU_CUDA_TRY(cudaEventRecord(pre, b->stream));
     size_t c = 0;
@@ -1282,7 +1282,7 @@ static int batch_enqueue(glsu_dpra_batch *b, const std::vector<char> &active, co
         GLSU_CUDA_TRY(cudaStreamWaitEvent(b->stream, e, 0));
     }
     // stage 3: final row pass with the phase update
-    cudaEvent_t cols;
+    cudaEvent_t cols = nullptr;
     GLSU_TRY(batch_event(b, ne++, &cols));
     GLSU_CUDA_TRY(cudaEventRecord(cols, b->stream));
     for (size_t i = 0; i < b->h.size(); i++) {

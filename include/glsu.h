@@ -385,8 +385,9 @@ int glsu_aia_run(glsu_aia *h, const void *const *h_frames, int img_type, float *
 #define GLSU_AIA_ERR_RELATIVE 1
 int glsu_aia_set_convergence(glsu_aia *h, int mode);
 /* Same on M device frames stored back to back (M*cols*rows), enqueued on
- * the stream; results stay on the device (d_phi, d_deltas) and *iters/*err
- * are written after an internal synchronisation. */
+ * the stream: the phase stays on the device (d_phi); the deltas (h_deltas,
+ * host, in/out as in glsu_aia_run), the iteration count and the error are
+ * written after an internal synchronisation. */
 int glsu_aia_run_device(glsu_aia *h, const void *d_frames, int img_type, float *d_phi, float *h_deltas,
                         int n_deltas_in, int *iters, float *err, int max_iter, float max_err,
                         uint64_t seed);
