@@ -1157,7 +1157,7 @@ def run_ours(args, rank, world, local):
         "wfr": wfr,
         "batched_form": batched,
     }
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:  # the CPU baseline: rank 0 at N = 1 only
         v32, secs, threads, rows = cpu_sample(size, prec="f32")
         v64, secs64, _, _ = cpu_sample(size, prec="f64")
         out["cpu_baseline"] = {
